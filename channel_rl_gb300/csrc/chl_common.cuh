@@ -1,0 +1,96 @@
+// Shared definitions for the GB300 channel-LES kernels.
+//
+// Data layout (per channel instance, all FP64, x fastest):
+//   * x and z are periodic and stored on their unique points only:
+//     i in [0,Nx) is Fortran index i_f = i+2 (faces and centres alike),
+//     k in [0,Nz) is k_f = k+2.  Face i is the right face of centre i.
+//     Neighbours wrap: i-1 of 0 is Nx-1 (the reference's ghost copies,
+//     boundary_conditions.f90:60-226).
+//   * y is stored with the reference's full extent: centre rows
+//     jc in [0,Ny+1] (Fortran j_f = jc+1, rows 0 and Ny+1 are the ghost
+//     rows that apply_Dirichlet_bc_y keeps at minus the first interior row)
+//     and face rows jv in [0,Ny] (Fortran j_f = jv+1, rows 0 and Ny are the
+//     walls).  Centre row jc lies between face rows jc-1 and jc.
+//   * a centre field has Ny+2 rows: index i + Nx*(jc + (Ny+2)*k);
+//     U and W are stored the same way; V has Ny+1 rows.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define CHL_NQ 18   // filtered DSM components
+
+struct ChlInst {
+  int Nx, Ny, Nz, Nxh;          // unique cells; Nxh = Nx/2+1
+  int LES_model, Dirichlet_nu_t, wall_model, x_mass_cte;
+  double nu, CFL, Cs;
+  double dxmin, dymin, dzmin;   // initialization.f90:233-235
+  double dyw;                   // yg(2)-yg(1), used for both walls (wallmodel.f90:448-450)
+  double hb, ht;                // matching heights of the log-law wall model
+  double cbc1, cbc2;            // coef_bc_1*(yg(2)-yg(1)), coef_bc_2*(yg(nyg)-yg(nyg-1))
+  double ybot, ytop;            // y(1), y(ny)
+  double gb1, gb2, gt1, gt2;    // pressure-BC metric factors g, g2 (pressure.f90:282-316)
+  double dygb, dygt;            // yg(2)-yg(1), yg(nyg)-yg(nyg-1)
+  double mass_norm;             // 1/(Nx*Nz)
+  // geometry (reciprocal spacings; see chl_host.cpp for the exact list)
+  const double *rdxc, *rdxf, *rdyc, *rdyf, *rdzc, *rdzf;
+  const double *dxf, *dyf, *dzf;  // raw spacings (dt)
+  const double *w0, *w1;          // weight_y_0/1 by face row jv
+  const double *smag_csdelta;     // Cs*Delta_j by centre row (static Smagorinsky)
+  const double *smag_dwall;       // distance of centre row to the nearer wall (van Driest)
+  // Fourier / tridiagonal
+  const double2 *twx, *twz;       // exp(-2 pi i m/N), m in [0,N)
+  const double *tri_inv, *tri_m, *tri_c;   // [Ny][Nz][Nxh] Thomas factors
+  // state: three velocity sets (start-of-step / stage 1 / stage 2)
+  double *U[3], *V[3], *W[3];
+  double *F1[3];                  // stage-1 RHS (kept for stages 2 and 3)
+  double *Fp[3];                  // RHS for the actual pressure
+  double *nut, *S;                // eddy viscosity (Ny+2 rows), |S| (Ny+2 rows)
+  double *q[CHL_NQ], *r[CHL_NQ];  // DSM filter ping-pong
+  double *E[3];                   // edge fields (S12, S13, S23 numerators)
+  double2 *spec;                  // [Ny+2][Nz][Nxh] spectra (rows 1..Ny used)
+  double *p;                      // pseudo-pressure (centres)
+  double *P;                      // actual pressure (centres)
+  double *alpha;                  // wall stress [2][Nz][Nx]
+  double *bc;                     // pressure BC planes [2][Nz][Nx]
+  double *part;                   // DSM plane partial sums [2][Ny+2][npart]
+  int npart;
+  double *coef;                   // nu_t coefficient per centre row [Ny+2]
+  double *scal;                   // device scalars (CHL_S_*)
+  unsigned long long *minabs;     // [Nx+1 | Nz] min |u| bit patterns (dt)
+  double *red;                    // reduction scratch [nblocks]
+  int *status;                    // device status word (0 ok)
+};
+
+// device scalar slots
+enum {
+  CHL_S_DT = 0, CHL_S_T, CHL_S_DPDX, CHL_S_Q0, CHL_S_SHIFT, CHL_S_DIVMAX,
+  CHL_S_NSCAL = 16
+};
+
+// block -> instance map shared by all multi-instance kernels
+struct ChlMap {
+  const ChlInst* inst;   // device array of instances
+  const int* off;        // prefix sum of blocks per instance, off[n] = total
+  int n;
+};
+
+__device__ __forceinline__ int chl_find(const ChlMap& m, int b, int& local) {
+  int lo = 0, hi = m.n - 1;
+  while (lo < hi) {                 // last instance with off[idx] <= b
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(m.off + mid) <= b) lo = mid; else hi = mid - 1;
+  }
+  local = b - __ldg(m.off + lo);
+  return lo;
+}
+
+__device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+__device__ __forceinline__ size_t cidx(const ChlInst& I, int i, int jc, int k) {
+  return (size_t)i + (size_t)I.Nx * ((size_t)jc + (size_t)(I.Ny + 2) * (size_t)k);
+}
+__device__ __forceinline__ size_t vidx(const ChlInst& I, int i, int jv, int k) {
+  return (size_t)i + (size_t)I.Nx * ((size_t)jv + (size_t)(I.Ny + 1) * (size_t)k);
+}
+
+#define LDG(p) __ldg(p)

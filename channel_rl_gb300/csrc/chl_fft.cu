@@ -1,0 +1,347 @@
+// Fractional-step projection: divergence, 2-D Fourier transform in x and z,
+// one tridiagonal solve in y per wavenumber pair, inverse transform and the
+// velocity correction.  Restates compute_projection_step
+// (projection.f90:20-214) and, for the actual pressure, the solver of
+// compute_pressure (pressure.f90:42-172).
+//
+// The reference transforms each y-plane with FFTW-MPI and calls LAPACK
+// zgtsv per mode.  Here:
+//  * x: two real rows are packed as one complex row, transformed by a
+//    shared-memory Stockham FFT (radix 4/3/2) and split into two
+//    half-spectra (kx = 0..Nx/2) - fused with the divergence that produces
+//    the rows;
+//  * z: complex columns of the half-spectrum, staged 16 kx-columns at a time
+//    in shared memory;
+//  * y: one thread per mode runs the Thomas elimination with factors
+//    precomputed once per grid (the matrix of a mode never changes between
+//    steps), into which the 1/(Nx*Nz) of the inverse transform and the 2 of
+//    the real-row packing are folded;
+//  * the inverse runs the same way back and the x pass writes the pressure.
+#include "chl_common.cuh"
+
+// ------------------------------------------------------------ Stockham passes
+// Data of `nrows` transforms of length N; element e of row r is at
+// r*rs + e*es.  One pass of radix R with sub-transform size Ns.
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+
+template <int R>
+__device__ __forceinline__ void dft_small(double2* v, bool inv) {
+  if (R == 2) {
+    const double2 a = v[0], b = v[1];
+    v[0] = cadd(a, b); v[1] = csub(a, b);
+  } else if (R == 4) {
+    const double2 a = cadd(v[0], v[2]), b = csub(v[0], v[2]);
+    const double2 c = cadd(v[1], v[3]), e = csub(v[1], v[3]);
+    // d = e * (-i) forward, e * (+i) inverse
+    const double2 d = inv ? make_double2(-e.y, e.x) : make_double2(e.y, -e.x);
+    v[0] = cadd(a, c); v[2] = csub(a, c);
+    v[1] = cadd(b, d); v[3] = csub(b, d);
+  } else if (R == 3) {
+    const double s3 = 0.86602540378443864676;   // sin(2 pi/3)
+    const double2 s = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+    const double2 t = make_double2(fma(-0.5, s.x, v[0].x), fma(-0.5, s.y, v[0].y));
+    // forward: out1 = t - i s3 d, out2 = t + i s3 d (inverse swaps)
+    const double2 m = inv ? make_double2(-s3 * d.y, s3 * d.x) : make_double2(s3 * d.y, -s3 * d.x);
+    v[0] = cadd(v[0], s);
+    v[1] = cadd(t, m);
+    v[2] = csub(t, m);
+  }
+}
+
+template <int R>
+__device__ void stockham_pass(const double2* __restrict__ x, double2* __restrict__ y, int nrows, int rs, int es,
+                              int N, int Ns, const double2* __restrict__ tw, bool inv) {
+  const int nb = N / R;
+  const int tstep = N / (Ns * R);
+  for (int w = threadIdx.x; w < nrows * nb; w += blockDim.x) {
+    const int row = w / nb, j = w - row * nb;
+    const double2* xr = x + (size_t)row * rs;
+    double2* yr = y + (size_t)row * rs;
+    const int jm = j % Ns;
+    double2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) v[r] = xr[(j + r * nb) * es];
+    if (Ns > 1) {
+#pragma unroll
+      for (int r = 1; r < R; ++r) {
+        double2 t = LDG(tw + jm * r * tstep);
+        if (inv) t.y = -t.y;
+        v[r] = cmul(v[r], t);
+      }
+    }
+    dft_small<R>(v, inv);
+    const int idxD = (j / Ns) * Ns * R + jm;
+#pragma unroll
+    for (int r = 0; r < R; ++r) yr[(idxD + r * Ns) * es] = v[r];
+  }
+}
+
+// Full transform; returns the buffer holding the result (a or b).
+__device__ double2* fft_smem(double2* a, double2* b, int nrows, int rs, int es, int N,
+                             const double2* tw, bool inv) {
+  int Ns = 1, rem = N;
+  double2 *src = a, *dst = b;
+  while (rem > 1) {
+    __syncthreads();
+    if (rem % 4 == 0) { stockham_pass<4>(src, dst, nrows, rs, es, N, Ns, tw, inv); Ns *= 4; rem /= 4; }
+    else if (rem % 3 == 0) { stockham_pass<3>(src, dst, nrows, rs, es, N, Ns, tw, inv); Ns *= 3; rem /= 3; }
+    else { stockham_pass<2>(src, dst, nrows, rs, es, N, Ns, tw, inv); Ns *= 2; rem /= 2; }
+    double2* t = src; src = dst; dst = t;
+  }
+  __syncthreads();
+  return src;
+}
+
+__device__ __forceinline__ int rows_per_block_x(int Nx) { int cr = 1024 / Nx; return cr < 1 ? 1 : cr; }
+
+// ------------------------------------------------------------ divergence + forward x
+// mode 0: div of velocity set s_in (compute_pseudo_pressure_rhs, projection.f90:40-55)
+// mode 1: div of the actual-pressure RHS Fp with the wall rows of Fv set to
+//         the pressure BC planes and the BC source terms of pressure.f90:138-139.
+__global__ void __launch_bounds__(256)
+k_div_fftx(ChlMap map, int s_in, int mode) {
+  extern __shared__ double2 sm[];
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
+  const int CR = rows_per_block_x(Nx);
+  const int nrow = Ny * (Nz / 2);
+  const int g0 = lb * CR;
+  const int cr_n = min(CR, nrow - g0);
+  double2* A = sm;
+  double2* B = sm + CR * Nx;
+  const double *U, *V, *W;
+  if (mode == 0) { U = I.U[s_in]; V = I.V[s_in]; W = I.W[s_in]; }
+  else { U = I.Fp[0]; V = I.Fp[1]; W = I.Fp[2]; }
+  for (int w = threadIdx.x; w < cr_n * Nx; w += blockDim.x) {
+    const int cr = w / Nx, i = w - cr * Nx;
+    const int g = g0 + cr;
+    const int jc = 1 + g / (Nz / 2), k0 = 2 * (g % (Nz / 2));
+    const int im = wrap(i - 1, Nx);
+    double dv[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int k = k0 + h, km = wrap(k - 1, Nz);
+      double vlo = LDG(V + vidx(I, i, jc - 1, k)), vhi = LDG(V + vidx(I, i, jc, k));
+      if (mode == 1) {
+        if (jc == 1) vlo = I.bc[(size_t)k * Nx + i];
+        if (jc == Ny) vhi = I.bc[(size_t)Nx * Nz + (size_t)k * Nx + i];
+      }
+      double d = (LDG(U + cidx(I, i, jc, k)) - LDG(U + cidx(I, im, jc, k))) * LDG(I.rdxc + i)
+               + (vhi - vlo) * LDG(I.rdyc + jc)
+               + (LDG(W + cidx(I, i, jc, k)) - LDG(W + cidx(I, i, jc, km))) * LDG(I.rdzc + k);
+      if (mode == 1) {
+        if (jc == 1) d += I.cbc1 * I.bc[(size_t)k * Nx + i];
+        if (jc == Ny) d -= I.cbc2 * I.bc[(size_t)Nx * Nz + (size_t)k * Nx + i];
+      }
+      dv[h] = d;
+    }
+    A[cr * Nx + i] = make_double2(dv[0], dv[1]);
+  }
+  double2* res = fft_smem(A, B, cr_n, Nx, 1, Nx, I.twx, false);
+  // split the packed spectrum into the two half-spectra (each times 2)
+  for (int w = threadIdx.x; w < cr_n * Nxh; w += blockDim.x) {
+    const int cr = w / Nxh, kx = w - cr * Nxh;
+    const int g = g0 + cr;
+    const int jc = 1 + g / (Nz / 2), k0 = 2 * (g % (Nz / 2));
+    const double2 z = res[cr * Nx + kx];
+    const double2 zc = res[cr * Nx + (kx == 0 ? 0 : Nx - kx)];   // conj taken below
+    const double2 Aa = make_double2(z.x + zc.x, z.y - zc.y);
+    const double2 Bb = make_double2(z.y + zc.y, zc.x - z.x);
+    I.spec[((size_t)jc * Nz + k0) * Nxh + kx] = Aa;
+    I.spec[((size_t)jc * Nz + k0 + 1) * Nxh + kx] = Bb;
+  }
+}
+
+// ------------------------------------------------------------ z transform of the half spectrum
+#define ZCW 16
+__global__ void __launch_bounds__(256)
+k_fftz(ChlMap map, int inv) {
+  extern __shared__ double2 sm[];
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
+  const int ncb = (Nxh + ZCW - 1) / ZCW;
+  const int jc = 1 + lb / ncb, c0 = (lb % ncb) * ZCW;
+  const int cw = min(ZCW, Nxh - c0);
+  double2* A = sm;
+  double2* B = sm + Nz * ZCW;
+  double2* base = I.spec + (size_t)jc * Nz * Nxh + c0;
+  for (int w = threadIdx.x; w < Nz * ZCW; w += blockDim.x) {
+    const int k = w / ZCW, c = w - k * ZCW;
+    A[k * ZCW + c] = c < cw ? base[(size_t)k * Nxh + c] : make_double2(0.0, 0.0);
+  }
+  double2* res = fft_smem(A, B, ZCW, 1, ZCW, Nz, I.twz, inv != 0);
+  for (int w = threadIdx.x; w < Nz * ZCW; w += blockDim.x) {
+    const int k = w / ZCW, c = w - k * ZCW;
+    if (c < cw) base[(size_t)k * Nxh + c] = res[k * ZCW + c];
+  }
+  (void)Ny;
+}
+
+// ------------------------------------------------------------ tridiagonal per mode
+__global__ void __launch_bounds__(128)
+k_tri(ChlMap map) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
+  const int mode = lb * blockDim.x + threadIdx.x;
+  if (mode >= Nz * Nxh) return;
+  const size_t ps = (size_t)Nz * Nxh;           // row pitch of spec and factors
+  double2* s = I.spec + ps + mode;               // row jc = 1
+  const double* fi = I.tri_inv + mode;
+  const double* fm = I.tri_m + mode;
+  const double* fc = I.tri_c + mode;
+  double2 prev = s[0];
+  const double i0 = LDG(fi);
+  prev.x *= i0; prev.y *= i0;
+  s[0] = prev;
+  for (int j = 1; j < Ny; ++j) {
+    double2 d = s[(size_t)j * ps];
+    const double iv = LDG(fi + (size_t)j * ps), m = LDG(fm + (size_t)j * ps);
+    d.x = fma(d.x, iv, -m * prev.x);
+    d.y = fma(d.y, iv, -m * prev.y);
+    s[(size_t)j * ps] = d;
+    prev = d;
+  }
+  for (int j = Ny - 2; j >= 0; --j) {
+    double2 d = s[(size_t)j * ps];
+    const double c = LDG(fc + (size_t)j * ps);
+    d.x = fma(-c, prev.x, d.x);
+    d.y = fma(-c, prev.y, d.y);
+    s[(size_t)j * ps] = d;
+    prev = d;
+  }
+}
+
+// ------------------------------------------------------------ inverse x -> pressure field
+__global__ void __launch_bounds__(256)
+k_fftx_inv(ChlMap map, int dst) {
+  extern __shared__ double2 sm[];
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
+  const int CR = rows_per_block_x(Nx);
+  const int nrow = Ny * (Nz / 2);
+  const int g0 = lb * CR;
+  const int cr_n = min(CR, nrow - g0);
+  double2* A = sm;
+  double2* B = sm + CR * Nx;
+  for (int w = threadIdx.x; w < cr_n * Nx; w += blockDim.x) {
+    const int cr = w / Nx, kx = w - cr * Nx;
+    const int g = g0 + cr;
+    const int jc = 1 + g / (Nz / 2), k0 = 2 * (g % (Nz / 2));
+    const bool lo = kx <= Nx / 2;
+    const int kk = lo ? kx : Nx - kx;
+    const double2 pa = I.spec[((size_t)jc * Nz + k0) * Nxh + kk];
+    const double2 pb = I.spec[((size_t)jc * Nz + k0 + 1) * Nxh + kk];
+    A[cr * Nx + kx] = lo ? make_double2(pa.x - pb.y, pa.y + pb.x)
+                         : make_double2(pa.x + pb.y, pb.x - pa.y);
+  }
+  double2* res = fft_smem(A, B, cr_n, Nx, 1, Nx, I.twx, true);
+  double* out = dst == 0 ? I.p : I.P;
+  for (int w = threadIdx.x; w < cr_n * Nx; w += blockDim.x) {
+    const int cr = w / Nx, i = w - cr * Nx;
+    const int g = g0 + cr;
+    const int jc = 1 + g / (Nz / 2), k0 = 2 * (g % (Nz / 2));
+    const double2 z = res[cr * Nx + i];
+    out[cidx(I, i, jc, k0)] = z.x;
+    out[cidx(I, i, jc, k0 + 1)] = z.y;
+  }
+}
+
+// ------------------------------------------------------------ velocity correction
+// project_velocity (projection.f90:192-214) + Dirichlet ghost rows.
+__global__ void __launch_bounds__(256)
+k_project(ChlMap map, int s) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t >= (long)Nx * Ny * Nz) return;
+  const int i = (int)(t % Nx);
+  const int jc = 1 + (int)((t / Nx) % Ny);
+  const int k = (int)(t / ((long)Nx * Ny));
+  const double* p = I.p;
+  const size_t c = cidx(I, i, jc, k);
+  const double p0 = LDG(p + c);
+  double* U = I.U[s]; double* V = I.V[s]; double* W = I.W[s];
+  const double un = U[c] - (LDG(p + cidx(I, wrap(i + 1, Nx), jc, k)) - p0) * LDG(I.rdxf + i);
+  const double wn = W[c] - (LDG(p + cidx(I, i, jc, wrap(k + 1, Nz))) - p0) * LDG(I.rdzf + k);
+  U[c] = un; W[c] = wn;
+  if (jc <= Ny - 1) {
+    const size_t v = vidx(I, i, jc, k);
+    V[v] = V[v] - (LDG(p + cidx(I, i, jc + 1, k)) - p0) * LDG(I.rdyf + jc);
+  }
+  if (jc == 1) { U[cidx(I, i, 0, k)] = -un; W[cidx(I, i, 0, k)] = -wn; }
+  if (jc == Ny) { U[cidx(I, i, Ny + 1, k)] = -un; W[cidx(I, i, Ny + 1, k)] = -wn; }
+}
+
+// ------------------------------------------------------------ actual pressure: wall BC planes
+// compute_pressure_BC (pressure.f90:269-340): bc = d/dy(nu dV/dy) at both walls.
+__global__ void k_pbc(ChlMap map, int s) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t >= 2L * Nx * Nz) return;
+  const int i = (int)(t % Nx), k = (int)((t / Nx) % Nz), wall = (int)(t / ((long)Nx * Nz));
+  const double* V = I.V[s];
+  const double* nt = I.nut;
+  double bcv;
+  if (wall == 0) {
+    const double g = I.gb1, g2 = I.gb2;
+    const double nui = I.nu + 0.5 * (nt[cidx(I, i, 0, k)] + nt[cidx(I, i, 1, k)]);
+    const double dnu = (nt[cidx(I, i, 1, k)] - nt[cidx(I, i, 0, k)]) / I.dygb;
+    const double v1 = V[vidx(I, i, 0, k)], v2 = V[vidx(I, i, 1, k)], v3 = V[vidx(I, i, 2, k)], v4 = V[vidx(I, i, 3, k)];
+    const double dV = (-3.0 * v1 + 4.0 * v2 - v3) / 2.0 * (1.0 / g);
+    double ddV = 2.0 * v1 - 5.0 * v2 + 4.0 * v3 - 1.0 * v4;
+    ddV = (ddV - dV * g2) / (g * g);
+    bcv = dnu * dV + nui * ddV;
+  } else {
+    const double g = I.gt1, g2 = I.gt2;
+    const double nui = I.nu + 0.5 * (nt[cidx(I, i, Ny + 1, k)] + nt[cidx(I, i, Ny, k)]);
+    const double dnu = (nt[cidx(I, i, Ny + 1, k)] - nt[cidx(I, i, Ny, k)]) / I.dygt;
+    const double v1 = V[vidx(I, i, Ny, k)], v2 = V[vidx(I, i, Ny - 1, k)], v3 = V[vidx(I, i, Ny - 2, k)], v4 = V[vidx(I, i, Ny - 3, k)];
+    const double dV = (3.0 * v1 - 4.0 * v2 + v3) / 2.0 * (1.0 / g);
+    double ddV = 2.0 * v1 - 5.0 * v2 + 4.0 * v3 - 1.0 * v4;
+    ddV = (ddV - dV * g2) / (g * g);
+    bcv = dnu * dV + nui * ddV;
+  }
+  I.bc[t] = bcv;
+}
+
+// P ghost rows (pressure.f90:158-159)
+__global__ void k_pghost(ChlMap map) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t >= (long)Nx * Nz) return;
+  const int i = (int)(t % Nx), k = (int)(t / Nx);
+  double* P = I.P;
+  P[cidx(I, i, 0, k)] = P[cidx(I, i, 1, k)] - I.dygb * I.bc[t];
+  P[cidx(I, i, Ny + 1, k)] = P[cidx(I, i, Ny, k)] + I.dygt * I.bc[(size_t)Nx * Nz + t];
+}
+
+extern "C" {
+size_t chl_smem_fftx(int maxNx) { int cr = 1024 / maxNx; if (cr < 1) cr = 1; return (size_t)2 * cr * maxNx * sizeof(double2); }
+size_t chl_smem_fftz(int maxNz) { return (size_t)2 * maxNz * ZCW * sizeof(double2); }
+int chl_fft_setup(size_t smx, size_t smz) {
+  cudaError_t e1 = cudaFuncSetAttribute(k_div_fftx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+  cudaError_t e2 = cudaFuncSetAttribute(k_fftx_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
+  cudaError_t e3 = cudaFuncSetAttribute(k_fftz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
+  return (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) ? 1 : 0;
+}
+void chl_launch_div_fftx(const ChlMap& m, int nb, size_t smem, int s_in, int mode, cudaStream_t st) { k_div_fftx<<<nb, 256, smem, st>>>(m, s_in, mode); }
+void chl_launch_fftz(const ChlMap& m, int nb, size_t smem, int inv, cudaStream_t st) { k_fftz<<<nb, 256, smem, st>>>(m, inv); }
+void chl_launch_tri(const ChlMap& m, int nb, cudaStream_t st) { k_tri<<<nb, 128, 0, st>>>(m); }
+void chl_launch_fftx_inv(const ChlMap& m, int nb, size_t smem, int dst, cudaStream_t st) { k_fftx_inv<<<nb, 256, smem, st>>>(m, dst); }
+void chl_launch_project(const ChlMap& m, int nb, int s, cudaStream_t st) { k_project<<<nb, 256, 0, st>>>(m, s); }
+void chl_launch_pbc(const ChlMap& m, int nb, int s, cudaStream_t st) { k_pbc<<<nb, 256, 0, st>>>(m, s); }
+void chl_launch_pghost(const ChlMap& m, int nb, cudaStream_t st) { k_pghost<<<nb, 256, 0, st>>>(m); }
+}

@@ -1,0 +1,784 @@
+// C ABI (include/chl.h): instance setup, device memory, the step schedule and
+// its CUDA graph.  The grid constants follow initialize
+// (initialization.f90:187-427); the step schedule follows
+// compute_time_step_RK3 (time_integration.f90:24-96) and the app_main loop
+// (app_main.f90:114-117).
+#include "../../include/chl.h"
+#include "chl_common.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+// ------------------------------------------------------------ launchers (other TUs)
+extern "C" {
+void chl_launch_rhs(const ChlMap&, int, int, int, int, double, double, int, cudaStream_t);
+void chl_launch_edges(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_centre(const ChlMap&, int, int, int, cudaStream_t);
+void chl_launch_filter_y(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_filter_x(const ChlMap&, int, cudaStream_t);
+void chl_launch_filter_z(const ChlMap&, int, cudaStream_t);
+void chl_launch_dsm_final(const ChlMap&, int, cudaStream_t);
+void chl_launch_coef(const ChlMap&, cudaStream_t);
+void chl_launch_eqwm(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_nut(const ChlMap&, int, int, int, cudaStream_t);
+size_t chl_smem_fftx(int);
+size_t chl_smem_fftz(int);
+int chl_fft_setup(size_t, size_t);
+void chl_launch_div_fftx(const ChlMap&, int, size_t, int, int, cudaStream_t);
+void chl_launch_fftz(const ChlMap&, int, size_t, int, cudaStream_t);
+void chl_launch_tri(const ChlMap&, int, cudaStream_t);
+void chl_launch_fftx_inv(const ChlMap&, int, size_t, int, cudaStream_t);
+void chl_launch_project(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_pbc(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_pghost(const ChlMap&, int, cudaStream_t);
+void chl_launch_unpack(double*, const double*, int, int, int, int, int, int, cudaStream_t);
+void chl_launch_pack(double*, const double*, int, int, int, int, int, int, cudaStream_t);
+void chl_launch_pack_unique(double*, const double*, int, int, int, int, int, cudaStream_t);
+void chl_launch_minabs(const ChlMap&, int, size_t, int, cudaStream_t);
+void chl_launch_dt(const ChlMap&, cudaStream_t);
+void chl_launch_massflow(const ChlMap&, cudaStream_t, int);
+void chl_launch_shift(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_tadvance(const ChlMap&, cudaStream_t);
+void chl_launch_divmax(const ChlMap&, int, double*, cudaStream_t);
+void chl_launch_qflow(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_stats(const ChlMap&, int, double*, int, int, cudaStream_t);
+}
+
+namespace {
+
+constexpr double RK_T[3] = {8.0 / 15.0, 2.0 / 3.0, 1.0};
+constexpr double RK_C[3][3] = {{8.0 / 15.0, 0.0, 0.0}, {1.0 / 4.0, 5.0 / 12.0, 0.0}, {1.0 / 4.0, 0.0, 3.0 / 4.0}};
+
+enum { M_PT, M_EDGE, M_FULL, M_DSMF, M_WALL, M_PLANE, M_FFTX, M_FFTZ, M_TRI, M_MINABS, M_ROWS, NMAP };
+
+// Grid constants of one instance (host, FP64), in the device index
+// convention of chl_common.cuh.  Arrays along x and z carry one slot of
+// offset so that index -1 is addressable; undefined entries are NaN.
+struct Consts {
+  int nx, ny, nz, nxg, nyg, nzg, Nx, Ny, Nz, Nxh;
+  std::vector<double> xf, yf, zf, xg, yg, zg;   // 1-based Fortran copies (index 0 unused)
+  std::vector<double> rdxc, rdxf, dxf, rdzc, rdzf, dzf;   // offset 1, length N+3
+  std::vector<double> rdyc, rdyf, dyf, w0, w1;            // length Ny+2
+  std::vector<double> csdelta, dwall;                     // length Ny+2
+  std::vector<double> kxx, kzz;
+  std::vector<double> Dd, Du, Dl;                          // 1-based by j_f
+  double dxmin, dymin, dzmin, coef_bc_1, coef_bc_2;
+};
+
+const double NaN = std::nan("");
+
+void centres(const std::vector<double>& f, int n, std::vector<double>& g) {
+  // initialization.f90:194-220: g(2:n) = midpoints, g(1), g(n+1) mirrored
+  std::vector<double> m(n);   // m[i] i=1..n-1
+  for (int i = 1; i <= n - 1; ++i) m[i] = 0.5 * (f[i] + f[i + 1]);
+  g.assign(n + 2, 0.0);
+  for (int i = 2; i <= n; ++i) g[i] = m[i - 1];
+  g[1] = m[1] - 2.0 * (m[1] - f[1]);
+  g[n + 1] = m[n - 1] + 2.0 * (f[n] - m[n - 1]);
+}
+
+std::vector<double> kmod(int N, double d) {
+  // initialization.f90:296-308
+  std::vector<double> k(N, 0.0);
+  const double pi = 4.0 * std::atan(1.0);
+  const int half = (int)std::ceil((double)N / 2.0);
+  for (int i = 0; i <= half && i < N; ++i) k[i] = 2.0 * (std::cos(2.0 * pi * (double)i / (double)N) - 1.0) / std::pow(d, 2.0);
+  for (int i = half + 1; i < N; ++i) k[i] = 2.0 * (std::cos(2.0 * pi * (double)(-N + i) / (double)N) - 1.0) / std::pow(d, 2.0);
+  return k;
+}
+
+int make_consts(const chl_grid_desc& d, Consts& c, std::string& err) {
+  if (d.nx < 6 || d.nz < 6 || d.ny < 6 || (d.nx % 2) || (d.nz % 2)) {
+    err = "grid: nx, nz must be even and >= 6, ny >= 6";
+    return CHL_E_ARG;
+  }
+  if (!d.x || !d.y || !d.z) { err = "grid: null coordinate array"; return CHL_E_ARG; }
+  c.nx = d.nx; c.ny = d.ny; c.nz = d.nz;
+  c.nxg = d.nx + 1; c.nyg = d.ny + 1; c.nzg = d.nz + 1;
+  c.Nx = d.nx - 2; c.Ny = d.ny - 1; c.Nz = d.nz - 2; c.Nxh = c.Nx / 2 + 1;
+  auto rem = [](int n) { while (n % 4 == 0) n /= 4; while (n % 3 == 0) n /= 3; while (n % 2 == 0) n /= 2; return n; };
+  if (rem(c.Nx) != 1 || rem(c.Nz) != 1) { err = "grid: Nx = nx-2 and Nz = nz-2 must be of the form 2^a 3^b"; return CHL_E_ARG; }
+  c.xf.assign(c.nx + 1, 0.0); c.yf.assign(c.ny + 1, 0.0); c.zf.assign(c.nz + 1, 0.0);
+  for (int i = 1; i <= c.nx; ++i) c.xf[i] = d.x[i - 1];
+  for (int j = 1; j <= c.ny; ++j) c.yf[j] = d.y[j - 1];
+  for (int k = 1; k <= c.nz; ++k) c.zf[k] = d.z[k - 1];
+  for (int i = 2; i <= c.nx; ++i) if (!(c.xf[i] > c.xf[i - 1])) { err = "grid: x not increasing"; return CHL_E_ARG; }
+  for (int i = 2; i <= c.ny; ++i) if (!(c.yf[i] > c.yf[i - 1])) { err = "grid: y not increasing"; return CHL_E_ARG; }
+  for (int i = 2; i <= c.nz; ++i) if (!(c.zf[i] > c.zf[i - 1])) { err = "grid: z not increasing"; return CHL_E_ARG; }
+  centres(c.xf, c.nx, c.xg); centres(c.yf, c.ny, c.yg); centres(c.zf, c.nz, c.zg);
+  auto dmin = [](const std::vector<double>& g, int n) {
+    double m = INFINITY; for (int i = 2; i <= n; ++i) m = std::min(m, g[i] - g[i - 1]); return m; };
+  c.dxmin = dmin(c.xg, c.nxg); c.dymin = dmin(c.yg, c.nyg); c.dzmin = dmin(c.zg, c.nzg);
+  // x/z spacings (device index i <-> Fortran i+2), stored with offset 1
+  auto periodic = [&](const std::vector<double>& f, const std::vector<double>& g, int N,
+                      std::vector<double>& rc, std::vector<double>& rf, std::vector<double>& df) {
+    rc.assign(N + 3, NaN); rf.assign(N + 3, NaN); df.assign(N + 3, NaN);
+    for (int i = 0; i <= N; ++i) rc[i + 1] = 1.0 / (f[i + 2] - f[i + 1]);
+    for (int i = -1; i <= N; ++i) { df[i + 1] = g[i + 3] - g[i + 2]; rf[i + 1] = 1.0 / df[i + 1]; }
+  };
+  periodic(c.xf, c.xg, c.Nx, c.rdxc, c.rdxf, c.dxf);
+  periodic(c.zf, c.zg, c.Nz, c.rdzc, c.rdzf, c.dzf);
+  const int Ny = c.Ny;
+  c.rdyc.assign(Ny + 2, NaN); c.rdyf.assign(Ny + 2, NaN); c.dyf.assign(Ny + 2, NaN);
+  c.w0.assign(Ny + 2, NaN); c.w1.assign(Ny + 2, NaN);
+  for (int jc = 1; jc <= Ny; ++jc) c.rdyc[jc] = 1.0 / (c.yf[jc + 1] - c.yf[jc]);
+  for (int jv = 0; jv <= Ny; ++jv) {
+    c.dyf[jv] = c.yg[jv + 2] - c.yg[jv + 1];
+    c.rdyf[jv] = 1.0 / c.dyf[jv];
+    // weight_y_0(j) = (yg(j+1)-y(j))/(yg(j+1)-yg(j)), j = jv+1 (initialization.f90:399-400)
+    c.w0[jv] = (c.yg[jv + 2] - c.yf[jv + 1]) / (c.yg[jv + 2] - c.yg[jv + 1]);
+    c.w1[jv] = 1.0 - c.w0[jv];
+  }
+  // static Smagorinsky: Cs*Delta_j and the van Driest wall distance (subgrid.f90:589-599)
+  c.csdelta.assign(Ny + 2, 0.0); c.dwall.assign(Ny + 2, 0.0);
+  for (int jc = 1; jc <= Ny; ++jc) {
+    const int jf = jc + 1;
+    const double Delta = std::pow(c.dxmin * c.dzmin * (c.yf[jf] - c.yf[jf - 1]), 1.0 / 3.0);
+    c.csdelta[jc] = d.Cs * Delta;
+    c.dwall[jc] = (jf < c.nyg / 2) ? (c.yg[jf] - c.yf[1]) : (c.yf[c.ny] - c.yg[jf]);
+  }
+  c.kxx = kmod(c.Nx, c.dxmin);
+  c.kzz = kmod(c.Nz, c.dzmin);
+  // Dyy (initialization.f90:355-385)
+  c.Dd.assign(c.nyg + 1, 0.0); c.Du.assign(c.nyg + 1, 0.0); c.Dl.assign(c.nyg + 1, 0.0);
+  auto abc = [&](int j, double& a, double& b, double& cc) {
+    const std::vector<double>& y = c.yf; const std::vector<double>& yg = c.yg;
+    a = 1.0 / (y[j] - y[j - 1]) / (yg[j + 1] - yg[j]);
+    b = 1.0 / (y[j] - y[j - 1]) * (-1.0 / (yg[j + 1] - yg[j]) - 1.0 / (yg[j] - yg[j - 1]));
+    cc = 1.0 / (y[j] - y[j - 1]) / (yg[j] - yg[j - 1]);
+  };
+  double a, b, cc;
+  for (int j = 3; j <= c.nyg - 2; ++j) { abc(j, a, b, cc); c.Du[j] = a; c.Dl[j] = cc; c.Dd[j] = b; }
+  abc(2, a, b, cc); c.Dd[2] = b + cc; c.Du[2] = a; c.coef_bc_1 = cc;
+  abc(c.nyg - 1, a, b, cc); c.Dd[c.nyg - 1] = a + b; c.Dl[c.nyg - 1] = cc; c.coef_bc_2 = a;
+  return CHL_OK;
+}
+
+struct Inst {
+  Consts c;
+  chl_grid_desc d;
+  ChlInst dev{};
+  void* arena = nullptr;
+  bool uploaded = false;
+  double* staging = nullptr;   // Fortran-layout staging (largest field)
+  size_t nstage = 0;
+};
+
+struct Arena {
+  size_t off = 0;
+  std::vector<std::pair<size_t, size_t>> plan;   // (offset, bytes)
+  size_t take(size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; }
+};
+
+int dsm_npart(int Nx, int Nz) { return (Nx * Nz + 256 * 4 - 1) / (256 * 4); }
+int fftx_rows(int Nx) { int cr = 1024 / Nx; return cr < 1 ? 1 : cr; }
+
+}  // namespace
+
+struct chl_handle {
+  std::vector<Inst> in;
+  ChlInst* d_inst = nullptr;
+  cudaStream_t st = nullptr;
+  std::string err;
+  int* d_off[NMAP] = {};
+  int nblk[NMAP] = {};
+  size_t smem_x = 0, smem_z = 0, smem_min = 0;
+  int LES_model = 0, wall_model = 0, any_mass = 0;
+  double* d_divout = nullptr;
+  double* d_stats = nullptr;
+  int stats_pitch = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  ChlMap map(int which) const { return ChlMap{d_inst, d_off[which], (int)in.size()}; }
+};
+
+#define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { \
+  h->err = std::string("CUDA: ") + cudaGetErrorString(e_) + " at " #call; return CHL_E_CUDA; } } while (0)
+#define LAUNCHED() do { cudaError_t e_ = cudaGetLastError(); if (e_ != cudaSuccess) { \
+  h->err = std::string("CUDA launch: ") + cudaGetErrorString(e_); return CHL_E_CUDA; } } while (0)
+
+static int upload_consts(chl_handle* h, Inst& I) {
+  Consts& c = I.c;
+  const int Nx = c.Nx, Ny = c.Ny, Nz = c.Nz, Nxh = c.Nxh;
+  const size_t nc = (size_t)Nx * (Ny + 2) * Nz, nv = (size_t)Nx * (Ny + 1) * Nz;
+  const size_t nspec = (size_t)(Ny + 2) * Nz * Nxh, ntri = (size_t)Ny * Nz * Nxh;
+  const bool dsm = I.d.LES_model == CHL_LES_DYNAMIC;
+  const int npart = dsm_npart(Nx, Nz);
+  Arena A;
+  // constants
+  size_t o_rdxc = A.take(8 * (Nx + 3)), o_rdxf = A.take(8 * (Nx + 3)), o_dxf = A.take(8 * (Nx + 3));
+  size_t o_rdzc = A.take(8 * (Nz + 3)), o_rdzf = A.take(8 * (Nz + 3)), o_dzf = A.take(8 * (Nz + 3));
+  size_t o_rdyc = A.take(8 * (Ny + 2)), o_rdyf = A.take(8 * (Ny + 2)), o_dyf = A.take(8 * (Ny + 2));
+  size_t o_w0 = A.take(8 * (Ny + 2)), o_w1 = A.take(8 * (Ny + 2));
+  size_t o_csd = A.take(8 * (Ny + 2)), o_dw = A.take(8 * (Ny + 2));
+  size_t o_twx = A.take(16 * Nx), o_twz = A.take(16 * Nz);
+  size_t o_ti = A.take(8 * ntri), o_tm = A.take(8 * ntri), o_tc = A.take(8 * ntri);
+  // state
+  size_t o_U[3], o_V[3], o_W[3], o_F1[3], o_Fp[3];
+  for (int s = 0; s < 3; ++s) { o_U[s] = A.take(8 * nc); o_V[s] = A.take(8 * nv); o_W[s] = A.take(8 * nc); }
+  for (int s = 0; s < 3; ++s) o_F1[s] = A.take(8 * (s == 1 ? nv : nc));
+  for (int s = 0; s < 3; ++s) o_Fp[s] = A.take(8 * (s == 1 ? nv : nc));
+  size_t o_nut = A.take(8 * nc), o_S = A.take(8 * nc);
+  size_t o_q[CHL_NQ] = {}, o_r[CHL_NQ] = {};
+  if (dsm) for (int m = 0; m < CHL_NQ; ++m) { o_q[m] = A.take(8 * nc); o_r[m] = A.take(8 * nc); }
+  size_t o_E[3];
+  for (int m = 0; m < 3; ++m) o_E[m] = A.take(8 * nc);
+  size_t o_spec = A.take(16 * nspec), o_p = A.take(8 * nc), o_P = A.take(8 * nc);
+  size_t o_alpha = A.take(8 * 2 * (size_t)Nx * Nz), o_bc = A.take(8 * 2 * (size_t)Nx * Nz);
+  size_t o_part = A.take(8 * 2 * (size_t)(Ny + 2) * npart);
+  size_t o_coef = A.take(8 * (Ny + 2)), o_scal = A.take(8 * CHL_S_NSCAL);
+  size_t o_min = A.take(8 * (size_t)(Nx + Ny + 1 + Nz)), o_status = A.take(64);
+  I.nstage = (size_t)c.nxg * c.nyg * c.nzg;
+  size_t o_stage = A.take(8 * I.nstage);
+  cudaError_t e = cudaMalloc(&I.arena, A.off);
+  if (e != cudaSuccess) { h->err = "device allocation failed (" + std::to_string(A.off) + " bytes)"; return CHL_E_NOMEM; }
+  CK(cudaMemsetAsync(I.arena, 0, A.off, h->st));
+  char* base = (char*)I.arena;
+  auto P = [&](size_t o) { return (double*)(base + o); };
+  ChlInst& D = I.dev;
+  D.Nx = Nx; D.Ny = Ny; D.Nz = Nz; D.Nxh = Nxh;
+  D.LES_model = I.d.LES_model; D.Dirichlet_nu_t = I.d.Dirichlet_nu_t;
+  D.wall_model = I.d.wall_model; D.x_mass_cte = I.d.x_mass_cte;
+  D.nu = I.d.nu; D.CFL = I.d.CFL; D.Cs = I.d.Cs;
+  D.dxmin = c.dxmin; D.dymin = c.dymin; D.dzmin = c.dzmin;
+  D.dyw = c.yg[2] - c.yg[1];
+  D.hb = c.yg[4] - c.yf[1];
+  D.ht = c.yf[c.ny] - c.yg[c.nyg - 3];
+  D.cbc1 = c.coef_bc_1 * (c.yg[2] - c.yg[1]);
+  D.cbc2 = c.coef_bc_2 * (c.yg[c.nyg] - c.yg[c.nyg - 1]);
+  D.ybot = c.yf[1]; D.ytop = c.yf[c.ny];
+  const std::vector<double>& y = c.yf;
+  D.gb1 = (-3.0 * y[1] + 4.0 * y[2] - y[3]) / 2.0;
+  D.gb2 = 2.0 * y[1] - 5.0 * y[2] + 4.0 * y[3] - 1.0 * y[4];
+  D.gt1 = (3.0 * y[c.ny] - 4.0 * y[c.ny - 1] + y[c.ny - 2]) / 2.0;
+  D.gt2 = 2.0 * y[c.ny] - 5.0 * y[c.ny - 1] + 4.0 * y[c.ny - 2] - 1.0 * y[c.ny - 3];
+  D.dygb = c.yg[2] - c.yg[1]; D.dygt = c.yg[c.nyg] - c.yg[c.nyg - 1];
+  D.mass_norm = 1.0 / ((double)Nx * Nz);
+  D.rdxc = P(o_rdxc) + 1; D.rdxf = P(o_rdxf) + 1; D.dxf = P(o_dxf) + 1;
+  D.rdzc = P(o_rdzc) + 1; D.rdzf = P(o_rdzf) + 1; D.dzf = P(o_dzf) + 1;
+  D.rdyc = P(o_rdyc); D.rdyf = P(o_rdyf); D.dyf = P(o_dyf); D.w0 = P(o_w0); D.w1 = P(o_w1);
+  D.smag_csdelta = P(o_csd); D.smag_dwall = P(o_dw);
+  D.twx = (const double2*)(base + o_twx); D.twz = (const double2*)(base + o_twz);
+  D.tri_inv = P(o_ti); D.tri_m = P(o_tm); D.tri_c = P(o_tc);
+  for (int s = 0; s < 3; ++s) { D.U[s] = P(o_U[s]); D.V[s] = P(o_V[s]); D.W[s] = P(o_W[s]); D.F1[s] = P(o_F1[s]); D.Fp[s] = P(o_Fp[s]); }
+  D.nut = P(o_nut); D.S = P(o_S);
+  for (int m = 0; m < CHL_NQ; ++m) { D.q[m] = dsm ? P(o_q[m]) : nullptr; D.r[m] = dsm ? P(o_r[m]) : nullptr; }
+  for (int m = 0; m < 3; ++m) D.E[m] = P(o_E[m]);
+  D.spec = (double2*)(base + o_spec); D.p = P(o_p); D.P = P(o_P);
+  D.alpha = P(o_alpha); D.bc = P(o_bc); D.part = P(o_part); D.npart = npart;
+  D.coef = P(o_coef); D.scal = P(o_scal);
+  D.minabs = (unsigned long long*)(base + o_min); D.red = nullptr; D.status = (int*)(base + o_status);
+  I.staging = P(o_stage);
+  // host constant arrays -> device
+  auto put = [&](size_t o, const std::vector<double>& v) { return cudaMemcpyAsync(base + o, v.data(), 8 * v.size(), cudaMemcpyHostToDevice, h->st); };
+  CK(put(o_rdxc, c.rdxc)); CK(put(o_rdxf, c.rdxf)); CK(put(o_dxf, c.dxf));
+  CK(put(o_rdzc, c.rdzc)); CK(put(o_rdzf, c.rdzf)); CK(put(o_dzf, c.dzf));
+  CK(put(o_rdyc, c.rdyc)); CK(put(o_rdyf, c.rdyf)); CK(put(o_dyf, c.dyf));
+  CK(put(o_w0, c.w0)); CK(put(o_w1, c.w1)); CK(put(o_csd, c.csdelta)); CK(put(o_dw, c.dwall));
+  const double pi = 4.0 * std::atan(1.0);
+  std::vector<double> tw(2 * (size_t)std::max(Nx, Nz));
+  for (int m = 0; m < Nx; ++m) { tw[2 * m] = std::cos(2.0 * pi * m / Nx); tw[2 * m + 1] = -std::sin(2.0 * pi * m / Nx); }
+  CK(cudaMemcpy(base + o_twx, tw.data(), 16 * Nx, cudaMemcpyHostToDevice));
+  for (int m = 0; m < Nz; ++m) { tw[2 * m] = std::cos(2.0 * pi * m / Nz); tw[2 * m + 1] = -std::sin(2.0 * pi * m / Nz); }
+  CK(cudaMemcpy(base + o_twz, tw.data(), 16 * Nz, cudaMemcpyHostToDevice));
+  // Thomas factors per mode: denominators of the elimination of
+  // Dyy + kxx + kzz (the zgtsv system of projection.f90:97-110), with the
+  // 1/(2 Nx Nz) of the packed inverse transform folded into inv.
+  {
+    std::vector<double> fi(ntri), fm(ntri), fc(ntri);
+    const double scale = 1.0 / (2.0 * (double)Nx * (double)Nz);
+    for (int kz = 0; kz < Nz; ++kz)
+      for (int kx = 0; kx < Nxh; ++kx) {
+        const double lam = c.kxx[kx] + c.kzz[kz];
+        double cprev = 0.0;
+        for (int r = 0; r < Ny; ++r) {
+          const int jf = r + 2;
+          double D_ = c.Dd[jf] + lam;
+          if (kx == 0 && kz == 0 && r == 0) D_ = 3.0 / 2.0 * D_;
+          const double L = r > 0 ? c.Dl[jf] : 0.0;
+          const double Uu = r < Ny - 1 ? c.Du[jf] : 0.0;
+          const double den = D_ - L * cprev;
+          const size_t o = ((size_t)r * Nz + kz) * Nxh + kx;
+          fi[o] = scale / den;
+          fm[o] = L / den;
+          fc[o] = Uu / den;
+          cprev = Uu / den;
+        }
+      }
+    CK(cudaMemcpy(base + o_ti, fi.data(), 8 * ntri, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(base + o_tm, fm.data(), 8 * ntri, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(base + o_tc, fc.data(), 8 * ntri, cudaMemcpyHostToDevice));
+  }
+  std::vector<double> scal(CHL_S_NSCAL, 0.0);
+  scal[CHL_S_DPDX] = I.d.dPdx;
+  CK(cudaMemcpy(base + o_scal, scal.data(), 8 * CHL_S_NSCAL, cudaMemcpyHostToDevice));
+  return CHL_OK;
+}
+
+static int build_maps(chl_handle* h) {
+  const int n = (int)h->in.size();
+  auto cdiv = [](long a, long b) { return (int)((a + b - 1) / b); };
+  for (int m = 0; m < NMAP; ++m) {
+    std::vector<int> off(n + 1, 0);
+    for (int q = 0; q < n; ++q) {
+      const Consts& c = h->in[q].c;
+      const int Nx = c.Nx, Ny = c.Ny, Nz = c.Nz, Nxh = c.Nxh;
+      int b = 0;
+      switch (m) {
+        case M_PT: b = cdiv((long)Nx * Ny * Nz, 256); break;
+        case M_EDGE: b = cdiv((long)Nx * (Ny + 1) * Nz, 256); break;
+        case M_FULL: b = cdiv((long)Nx * (Ny + 2) * Nz, 256); break;
+        case M_DSMF: b = Ny * dsm_npart(Nx, Nz); break;
+        case M_WALL: b = cdiv(2L * Nx * Nz, 256); break;
+        case M_PLANE: b = cdiv((long)Nx * Nz, 256); break;
+        case M_FFTX: b = cdiv((long)Ny * (Nz / 2), fftx_rows(Nx)); break;
+        case M_FFTZ: b = Ny * cdiv(Nxh, 16); break;
+        case M_TRI: b = cdiv((long)Nz * Nxh, 128); break;
+        case M_MINABS: b = Nz; break;
+        case M_ROWS: b = Ny + 1; break;
+      }
+      off[q + 1] = off[q] + b;
+    }
+    h->nblk[m] = off[n];
+    CK(cudaMalloc(&h->d_off[m], sizeof(int) * (n + 1)));
+    CK(cudaMemcpy(h->d_off[m], off.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+  }
+  int mx = 0, mz = 0, mmin = 0;
+  for (auto& I : h->in) { mx = std::max(mx, I.c.Nx); mz = std::max(mz, I.c.Nz); mmin = std::max(mmin, I.c.Nx + I.c.Ny + 1); }
+  h->smem_x = chl_smem_fftx(mx);
+  h->smem_z = chl_smem_fftz(mz);
+  h->smem_min = 8 * (size_t)mmin;
+  if (chl_fft_setup(h->smem_x, h->smem_z)) { h->err = "FFT shared-memory size not supported"; return CHL_E_ARG; }
+  return CHL_OK;
+}
+
+// ------------------------------------------------------------ schedules
+static int enqueue_sgs(chl_handle* h, int s, bool with_wm) {
+  cudaStream_t st = h->st;
+  if (h->LES_model == CHL_LES_DYNAMIC) {
+    chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st);
+    chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 1, st);
+    chl_launch_filter_y(h->map(M_FULL), h->nblk[M_FULL], s, st);
+    chl_launch_filter_x(h->map(M_FULL), h->nblk[M_FULL], st);
+    chl_launch_filter_z(h->map(M_FULL), h->nblk[M_FULL], st);
+    chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], 3, st);
+    chl_launch_dsm_final(h->map(M_DSMF), h->nblk[M_DSMF], st);
+  } else if (h->LES_model == CHL_LES_SMAGORINSKY) {
+    chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st);
+    chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 0, st);
+  }
+  chl_launch_coef(h->map(M_PT), st);
+  if (with_wm && h->wall_model == CHL_WM_EQLOG) chl_launch_eqwm(h->map(M_WALL), h->nblk[M_WALL], s, st);
+  chl_launch_nut(h->map(M_FULL), h->nblk[M_FULL], s, with_wm ? 1 : 0, st);
+  LAUNCHED();
+  return CHL_OK;
+}
+
+static int enqueue_projection(chl_handle* h, int s, int mode) {
+  cudaStream_t st = h->st;
+  chl_launch_div_fftx(h->map(M_FFTX), h->nblk[M_FFTX], h->smem_x, s, mode, st);
+  chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 0, st);
+  chl_launch_tri(h->map(M_TRI), h->nblk[M_TRI], st);
+  chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 1, st);
+  chl_launch_fftx_inv(h->map(M_FFTX), h->nblk[M_FFTX], h->smem_x, mode == 0 ? 0 : 1, st);
+  if (mode == 0) chl_launch_project(h->map(M_PT), h->nblk[M_PT], s, st);
+  LAUNCHED();
+  return CHL_OK;
+}
+
+static int enqueue_dt(chl_handle* h) {
+  chl_launch_minabs(h->map(M_MINABS), h->nblk[M_MINABS], h->smem_min, 0, h->st);
+  chl_launch_dt(h->map(M_PT), h->st);
+  LAUNCHED();
+  return CHL_OK;
+}
+
+static int enqueue_rk3(chl_handle* h) {
+  // set in -> out per stage: 0 -> 1, 1 -> 2, 2 -> 0 (base is always set 0)
+  const int sin[3] = {0, 1, 2}, sout[3] = {1, 2, 0};
+  for (int s = 0; s < 3; ++s) {
+    int rc = enqueue_sgs(h, sin[s], h->wall_model != CHL_WM_NONE);
+    if (rc) return rc;
+    const double c1 = s == 0 ? 0.0 : RK_C[s][0];
+    const double c2 = RK_C[s][s];
+    chl_launch_rhs(h->map(M_PT), h->nblk[M_PT], sin[s], 0, sout[s], c1, c2, s == 0 ? 0 : 1, h->st);
+    LAUNCHED();
+    rc = enqueue_projection(h, sout[s], 0);
+    if (rc) return rc;
+  }
+  if (h->any_mass) {
+    chl_launch_massflow(h->map(M_PT), h->st, 0);
+    chl_launch_shift(h->map(M_PT), h->nblk[M_PT], 0, h->st);
+  }
+  chl_launch_tadvance(h->map(M_PT), h->st);
+  LAUNCHED();
+  (void)RK_T;
+  return CHL_OK;
+}
+
+static int check_ready(chl_handle* h) {
+  if (!h) return CHL_E_ARG;
+  for (auto& I : h->in) if (!I.uploaded) { h->err = "fields not uploaded"; return CHL_E_STATE; }
+  return CHL_OK;
+}
+
+static int finish(chl_handle* h) {
+  cudaError_t e = cudaStreamSynchronize(h->st);
+  if (e != cudaSuccess) { h->err = std::string("CUDA: ") + cudaGetErrorString(e); return CHL_E_CUDA; }
+  return CHL_OK;
+}
+
+// ------------------------------------------------------------ C ABI
+extern "C" {
+
+int chl_grid_constants_size(const chl_grid_desc* d) {
+  if (!d) return -1;
+  const int Nx = d->nx - 2, Nz = d->nz - 2, nyg = d->ny + 1;
+  return Nx + Nz + 3 * (nyg - 2) + d->ny + 5;
+}
+
+int chl_grid_constants(const chl_grid_desc* d, double* out) {
+  if (!d || !out) return CHL_E_ARG;
+  Consts c; std::string err;
+  int rc = make_consts(*d, c, err);
+  if (rc) return rc;
+  size_t o = 0;
+  for (int i = 0; i < c.Nx; ++i) out[o++] = c.kxx[i];
+  for (int i = 0; i < c.Nz; ++i) out[o++] = c.kzz[i];
+  for (int j = 2; j <= c.nyg - 1; ++j) out[o++] = c.Dd[j];
+  for (int j = 2; j <= c.nyg - 1; ++j) out[o++] = c.Du[j];
+  for (int j = 2; j <= c.nyg - 1; ++j) out[o++] = c.Dl[j];
+  for (int jv = 0; jv <= c.Ny; ++jv) out[o++] = c.w0[jv];
+  out[o++] = c.dxmin; out[o++] = c.dymin; out[o++] = c.dzmin; out[o++] = c.coef_bc_1; out[o++] = c.coef_bc_2;
+  return CHL_OK;
+}
+
+int chl_batch_create(int n, const chl_grid_desc* descs, chl_handle** out) {
+  if (!out || n <= 0 || !descs) return CHL_E_ARG;
+  *out = nullptr;
+  chl_handle* h = new chl_handle();
+  h->in.resize(n);
+  for (int q = 0; q < n; ++q) {
+    Inst& I = h->in[q];
+    I.d = descs[q];
+    int rc = make_consts(I.d, I.c, h->err);
+    if (rc) { *out = h; return rc; }
+    if (I.d.LES_model < 0 || I.d.LES_model > 2 || I.d.wall_model < 0 || I.d.wall_model > 2) {
+      h->err = "unsupported LES_model / wall_model"; *out = h; return CHL_E_ARG;
+    }
+    if (q > 0 && (I.d.LES_model != h->in[0].d.LES_model || I.d.wall_model != h->in[0].d.wall_model)) {
+      h->err = "instances of one batch must share LES_model and wall_model"; *out = h; return CHL_E_ARG;
+    }
+    if (I.d.wall_model == CHL_WM_EQLOG && I.c.Ny < 8) { h->err = "equilibrium wall model needs Ny >= 8"; *out = h; return CHL_E_ARG; }
+    if (I.d.x_mass_cte) h->any_mass = 1;
+  }
+  h->LES_model = h->in[0].d.LES_model;
+  h->wall_model = h->in[0].d.wall_model;
+  cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { h->err = std::string("CUDA: ") + cudaGetErrorString(e); *out = h; return CHL_E_CUDA; }
+  for (auto& I : h->in) { int rc = upload_consts(h, I); if (rc) { *out = h; return rc; } }
+  std::vector<ChlInst> hv(n);
+  for (int q = 0; q < n; ++q) hv[q] = h->in[q].dev;
+  e = cudaMalloc(&h->d_inst, sizeof(ChlInst) * n);
+  if (e != cudaSuccess) { h->err = "device allocation failed"; *out = h; return CHL_E_NOMEM; }
+  e = cudaMemcpy(h->d_inst, hv.data(), sizeof(ChlInst) * n, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) { h->err = std::string("CUDA: ") + cudaGetErrorString(e); *out = h; return CHL_E_CUDA; }
+  e = cudaMalloc(&h->d_divout, sizeof(double) * 2 * n);
+  if (e != cudaSuccess) { h->err = "device allocation failed"; *out = h; return CHL_E_NOMEM; }
+  for (auto& I : h->in) h->stats_pitch = std::max(h->stats_pitch, 7 * (I.c.Ny + 1) + 4);
+  e = cudaMalloc(&h->d_stats, sizeof(double) * (size_t)h->stats_pitch * n);
+  if (e != cudaSuccess) { h->err = "device allocation failed"; *out = h; return CHL_E_NOMEM; }
+  int rc = build_maps(h);
+  if (rc) { *out = h; return rc; }
+  *out = h;
+  return finish(h);
+}
+
+int chl_create(const chl_grid_desc* desc, chl_handle** out) { return chl_batch_create(1, desc, out); }
+
+int chl_destroy(chl_handle* h) {
+  if (!h) return CHL_OK;
+  if (h->st) cudaStreamSynchronize(h->st);
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  for (auto& I : h->in) if (I.arena) cudaFree(I.arena);
+  for (int m = 0; m < NMAP; ++m) if (h->d_off[m]) cudaFree(h->d_off[m]);
+  if (h->d_inst) cudaFree(h->d_inst);
+  if (h->d_divout) cudaFree(h->d_divout);
+  if (h->d_stats) cudaFree(h->d_stats);
+  if (h->st) cudaStreamDestroy(h->st);
+  delete h;
+  return CHL_OK;
+}
+
+const char* chl_last_error(const chl_handle* h) { return h ? h->err.c_str() : "null handle"; }
+int chl_num_instances(const chl_handle* h) { return h ? (int)h->in.size() : 0; }
+
+static Inst* get_inst(chl_handle* h, int inst) {
+  if (!h || inst < 0 || inst >= (int)h->in.size()) { if (h) h->err = "instance index out of range"; return nullptr; }
+  return &h->in[inst];
+}
+
+int chl_upload(chl_handle* h, int inst, const double* U, const double* V, const double* W) {
+  Inst* I = get_inst(h, inst);
+  if (!I) return CHL_E_ARG;
+  if (!U || !V || !W) { h->err = "null field"; return CHL_E_ARG; }
+  const Consts& c = I->c;
+  const int Nx = c.Nx, Ny = c.Ny, Nz = c.Nz;
+  struct { const double* src; double* dst; int n1, n2, n3, nrow, kind; } f[3] = {
+      {U, I->dev.U[0], c.nx, c.nyg, c.nzg, Ny + 2, 0},
+      {V, I->dev.V[0], c.nxg, c.ny, c.nzg, Ny + 1, 1},
+      {W, I->dev.W[0], c.nxg, c.nyg, c.nz, Ny + 2, 0}};
+  for (auto& q : f) {
+    CK(cudaMemcpyAsync(I->staging, q.src, 8 * (size_t)q.n1 * q.n2 * q.n3, cudaMemcpyHostToDevice, h->st));
+    chl_launch_unpack(q.dst, I->staging, Nx, q.nrow, Nz, q.n1, q.n2, q.kind, h->st);
+    LAUNCHED();
+  }
+  // Qflow_x_0 of this instance (mass_flow.f90:271-309); the kernel runs per instance
+  ChlMap m{h->d_inst + inst, h->d_off[M_PT], 1};
+  chl_launch_qflow(m, 0, CHL_S_Q0, h->st);
+  LAUNCHED();
+  I->uploaded = true;
+  return finish(h);
+}
+
+static int download_field(chl_handle* h, Inst* I, double* dst, const double* src, int n1, int n2, int n3, int nrow) {
+  chl_launch_pack(I->staging, src, I->c.Nx, nrow, I->c.Nz, n1, n2, n3, h->st);
+  LAUNCHED();
+  CK(cudaMemcpyAsync(dst, I->staging, 8 * (size_t)n1 * n2 * n3, cudaMemcpyDeviceToHost, h->st));
+  return finish(h);
+}
+
+int chl_download(chl_handle* h, int inst, double* U, double* V, double* W, double* P, double* nu_t) {
+  Inst* I = get_inst(h, inst);
+  if (!I) return CHL_E_ARG;
+  const Consts& c = I->c;
+  const int Ny = c.Ny;
+  int rc = 0;
+  if (U && (rc = download_field(h, I, U, I->dev.U[0], c.nx, c.nyg, c.nzg, Ny + 2))) return rc;
+  if (V && (rc = download_field(h, I, V, I->dev.V[0], c.nxg, c.ny, c.nzg, Ny + 1))) return rc;
+  if (W && (rc = download_field(h, I, W, I->dev.W[0], c.nxg, c.nyg, c.nz, Ny + 2))) return rc;
+  if (P && (rc = download_field(h, I, P, I->dev.P, c.nxg, c.nyg, c.nzg, Ny + 2))) return rc;
+  if (nu_t && (rc = download_field(h, I, nu_t, I->dev.nut, c.nxg, c.nyg, c.nzg, Ny + 2))) return rc;
+  return CHL_OK;
+}
+
+int chl_download_pseudo_pressure(chl_handle* h, int inst, double* p) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !p) return CHL_E_ARG;
+  const Consts& c = I->c;
+  return download_field(h, I, p, I->dev.p, c.nxg, c.nyg, c.nzg, c.Ny + 2);
+}
+
+int chl_set_wall_stress(chl_handle* h, int inst, const double* a) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !a) return CHL_E_ARG;
+  const Consts& c = I->c;
+  std::vector<double> al(2 * (size_t)c.Nx * c.Nz);
+  for (int w = 0; w < 2; ++w)
+    for (int k = 0; k < c.Nz; ++k)
+      for (int i = 0; i < c.Nx; ++i)   // alpha_x(i+2, w+1, k+2)
+        al[((size_t)w * c.Nz + k) * c.Nx + i] = a[(size_t)(i + 1) + (size_t)c.nx * ((size_t)w + 2 * (size_t)(k + 1))];
+  CK(cudaMemcpyAsync(I->dev.alpha, al.data(), 8 * al.size(), cudaMemcpyHostToDevice, h->st));
+  return finish(h);
+}
+
+int chl_get_wall_stress(chl_handle* h, int inst, double* a) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !a) return CHL_E_ARG;
+  const Consts& c = I->c;
+  std::vector<double> al(2 * (size_t)c.Nx * c.Nz);
+  CK(cudaMemcpyAsync(al.data(), I->dev.alpha, 8 * al.size(), cudaMemcpyDeviceToHost, h->st));
+  int rc = finish(h);
+  if (rc) return rc;
+  for (int k1 = 0; k1 < c.nzg; ++k1)
+    for (int w = 0; w < 2; ++w)
+      for (int i1 = 0; i1 < c.nx; ++i1) {
+        int i = (i1 - 1) % c.Nx; if (i < 0) i += c.Nx;
+        int k = (k1 - 1) % c.Nz; if (k < 0) k += c.Nz;
+        a[(size_t)i1 + (size_t)c.nx * ((size_t)w + 2 * (size_t)k1)] = al[((size_t)w * c.Nz + k) * c.Nx + i];
+      }
+  return CHL_OK;
+}
+
+int chl_get_scalars(chl_handle* h, int inst, double* out4) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !out4) return CHL_E_ARG;
+  double s[CHL_S_NSCAL];
+  CK(cudaMemcpyAsync(s, I->dev.scal, sizeof(s), cudaMemcpyDeviceToHost, h->st));
+  int rc = finish(h);
+  if (rc) return rc;
+  out4[0] = s[CHL_S_DT]; out4[1] = s[CHL_S_T]; out4[2] = s[CHL_S_DPDX]; out4[3] = s[CHL_S_Q0];
+  return CHL_OK;
+}
+
+int chl_set_scalars(chl_handle* h, int inst, const double* in4) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !in4) return CHL_E_ARG;
+  double s[CHL_S_NSCAL];
+  CK(cudaMemcpyAsync(s, I->dev.scal, sizeof(s), cudaMemcpyDeviceToHost, h->st));
+  int rc = finish(h);
+  if (rc) return rc;
+  s[CHL_S_DT] = in4[0]; s[CHL_S_T] = in4[1]; s[CHL_S_DPDX] = in4[2]; s[CHL_S_Q0] = in4[3];
+  CK(cudaMemcpyAsync(I->dev.scal, s, sizeof(s), cudaMemcpyHostToDevice, h->st));
+  return finish(h);
+}
+
+int chl_compute_dt(chl_handle* h) {
+  int rc = check_ready(h); if (rc) return rc;
+  rc = enqueue_dt(h); if (rc) return rc;
+  return finish(h);
+}
+
+int chl_compute_time_step_RK3(chl_handle* h) {
+  int rc = check_ready(h); if (rc) return rc;
+  rc = enqueue_rk3(h); if (rc) return rc;
+  return finish(h);
+}
+
+int chl_rk3_step(chl_handle* h, int nsteps) {
+  int rc = check_ready(h); if (rc) return rc;
+  if (nsteps < 0) { h->err = "nsteps < 0"; return CHL_E_ARG; }
+  if (!h->gexec) {
+    CK(cudaStreamBeginCapture(h->st, cudaStreamCaptureModeThreadLocal));
+    rc = enqueue_dt(h);
+    if (!rc) rc = enqueue_rk3(h);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(h->st, &g);
+    if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+    if (e != cudaSuccess) { h->err = std::string("graph capture: ") + cudaGetErrorString(e); return CHL_E_CUDA; }
+    h->graph = g;
+    CK(cudaGraphInstantiate(&h->gexec, g, 0));
+  }
+  for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(h->gexec, h->st));
+  return CHL_OK;
+}
+
+int chl_synchronize(chl_handle* h) { if (!h) return CHL_E_ARG; return finish(h); }
+
+int chl_compute_eddy_viscosity(chl_handle* h) {
+  int rc = check_ready(h); if (rc) return rc;
+  rc = enqueue_sgs(h, 0, false); if (rc) return rc;
+  return finish(h);
+}
+
+int chl_compute_wall_model(chl_handle* h) {
+  int rc = check_ready(h); if (rc) return rc;
+  if (h->wall_model == CHL_WM_EQLOG) chl_launch_eqwm(h->map(M_WALL), h->nblk[M_WALL], 0, h->st);
+  chl_launch_nut(h->map(M_FULL), h->nblk[M_FULL], 0, h->wall_model != CHL_WM_NONE ? 1 : 0, h->st);
+  LAUNCHED();
+  return finish(h);
+}
+
+int chl_compute_rhs(chl_handle* h, int inst, double* Fu, double* Fv, double* Fw) {
+  int rc = check_ready(h); if (rc) return rc;
+  Inst* I = get_inst(h, inst);
+  if (!I) return CHL_E_ARG;
+  chl_launch_rhs(h->map(M_PT), h->nblk[M_PT], 0, 0, 0, 0.0, 0.0, 2, h->st);
+  LAUNCHED();
+  const Consts& c = I->c;
+  const int Nx = c.Nx, Ny = c.Ny, Nz = c.Nz;
+  struct { double* dst; const double* src; int nrow, jlo, nj; } f[3] = {
+      {Fu, I->dev.Fp[0], Ny + 2, 1, Ny}, {Fv, I->dev.Fp[1], Ny + 1, 1, Ny - 1}, {Fw, I->dev.Fp[2], Ny + 2, 1, Ny}};
+  for (auto& q : f) {
+    if (!q.dst) continue;
+    chl_launch_pack_unique(I->staging, q.src, Nx, q.nrow, Nz, q.jlo, q.nj, h->st);
+    LAUNCHED();
+    CK(cudaMemcpyAsync(q.dst, I->staging, 8 * (size_t)Nx * q.nj * Nz, cudaMemcpyDeviceToHost, h->st));
+  }
+  return finish(h);
+}
+
+int chl_compute_projection_step(chl_handle* h) {
+  int rc = check_ready(h); if (rc) return rc;
+  rc = enqueue_projection(h, 0, 0); if (rc) return rc;
+  return finish(h);
+}
+
+int chl_compute_dPx_for_constant_mass_flow(chl_handle* h, int inst, double* dPdx) {
+  int rc = check_ready(h); if (rc) return rc;
+  Inst* I = get_inst(h, inst);
+  if (!I || !dPdx) return CHL_E_ARG;
+  double s[CHL_S_NSCAL];
+  CK(cudaMemcpyAsync(s, I->dev.scal, sizeof(s), cudaMemcpyDeviceToHost, h->st));
+  if ((rc = finish(h))) return rc;
+  chl_launch_massflow(h->map(M_PT), h->st, 0);
+  LAUNCHED();
+  double s2[CHL_S_NSCAL];
+  CK(cudaMemcpyAsync(s2, I->dev.scal, sizeof(s2), cudaMemcpyDeviceToHost, h->st));
+  if ((rc = finish(h))) return rc;
+  *dPdx = s2[CHL_S_SHIFT];
+  // this entry point only reports dPdx: restore the imposed gradient
+  CK(cudaMemcpyAsync(I->dev.scal, s, sizeof(s), cudaMemcpyHostToDevice, h->st));
+  return finish(h);
+}
+
+int chl_compute_pressure(chl_handle* h) {
+  int rc = check_ready(h); if (rc) return rc;
+  chl_launch_pbc(h->map(M_WALL), h->nblk[M_WALL], 0, h->st);
+  chl_launch_rhs(h->map(M_PT), h->nblk[M_PT], 0, 0, 0, 0.0, 0.0, 2, h->st);
+  LAUNCHED();
+  rc = enqueue_projection(h, 0, 1); if (rc) return rc;
+  chl_launch_pghost(h->map(M_PLANE), h->nblk[M_PLANE], h->st);
+  LAUNCHED();
+  return finish(h);
+}
+
+int chl_check_divergence(chl_handle* h, int inst, double* max_div, double* max_abs_div) {
+  int rc = check_ready(h); if (rc) return rc;
+  if (!get_inst(h, inst)) return CHL_E_ARG;
+  chl_launch_divmax(h->map(M_PT), 0, h->d_divout, h->st);
+  LAUNCHED();
+  double r[2];
+  CK(cudaMemcpyAsync(r, h->d_divout + 2 * inst, sizeof(r), cudaMemcpyDeviceToHost, h->st));
+  if ((rc = finish(h))) return rc;
+  if (max_div) *max_div = r[0];
+  if (max_abs_div) *max_abs_div = r[1];
+  return CHL_OK;
+}
+
+static int run_stats(chl_handle* h, int inst, std::vector<double>& buf) {
+  int rc = check_ready(h); if (rc) return rc;
+  if (!get_inst(h, inst)) return CHL_E_ARG;
+  chl_launch_stats(h->map(M_ROWS), h->nblk[M_ROWS], h->d_stats, h->stats_pitch, 0, h->st);
+  LAUNCHED();
+  buf.resize(h->stats_pitch);
+  CK(cudaMemcpyAsync(buf.data(), h->d_stats + (size_t)inst * h->stats_pitch, 8 * (size_t)h->stats_pitch,
+                     cudaMemcpyDeviceToHost, h->st));
+  return finish(h);
+}
+
+int chl_stats(chl_handle* h, int inst, chl_stats_out* out) {
+  if (!out) return CHL_E_ARG;
+  std::vector<double> buf;
+  int rc = run_stats(h, inst, buf); if (rc) return rc;
+  const Inst& I = h->in[inst];
+  const double* w = buf.data() + 7 * (I.c.Ny + 1);
+  const double Ly = I.c.yf[I.c.ny] - I.c.yf[1];
+  out->tau_wall = w[0];
+  out->utau = std::pow((w[0] + w[0]) / Ly, 0.5);
+  out->Retau = out->utau * (I.c.yf[I.c.ny] - I.c.yf[1]) / 2.0 / I.d.nu;
+  out->Qflow_x = w[1];
+  out->Qflow_y = w[2];
+  double sc[4];
+  if ((rc = chl_get_scalars(h, inst, sc))) return rc;
+  out->dt = sc[0]; out->t = sc[1]; out->dPdx = sc[2];
+  return chl_check_divergence(h, inst, &out->max_div, &out->max_abs_div);
+}
+
+int chl_stats_profiles(chl_handle* h, int inst, double* Um, double* Vm, double* Wm, double* U2, double* V2,
+                       double* W2, double* UV) {
+  std::vector<double> buf;
+  int rc = run_stats(h, inst, buf); if (rc) return rc;
+  const int ny = h->in[inst].c.ny;
+  double* dst[7] = {Um, Vm, Wm, U2, V2, W2, UV};
+  for (int m = 0; m < 7; ++m)
+    if (dst[m]) std::memcpy(dst[m], buf.data() + (size_t)m * ny, 8 * (size_t)ny);
+  return CHL_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,251 @@
+// Layout conversion, time step, constant mass flow, reductions.
+#include "chl_common.cuh"
+
+// ------------------------------------------------------------ Fortran <-> device layout
+// Fortran array F(n1,n2,n3) (column-major, full ghosted extents of the
+// reference) -> device field: x/z unique points, all y rows.
+// kind 0: U/W-like (ghost rows 0 and Ny+1 = minus the first interior row),
+// kind 1: V-like (wall rows 0 and Ny set to zero).
+__global__ void k_unpack(double* dst, const double* __restrict__ F, int Nx, int nrow, int Nz,
+                         int n1, int n2, int kind) {
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)Nx * nrow * Nz) return;
+  const int i = (int)(t % Nx), j = (int)((t / Nx) % nrow), k = (int)(t / ((long)Nx * nrow));
+  const size_t d = (size_t)i + (size_t)Nx * ((size_t)j + (size_t)nrow * k);
+  const int last = nrow - 1;
+  if (kind == 1 && (j == 0 || j == last)) { dst[d] = 0.0; return; }
+  int js = j; double sg = 1.0;
+  if (kind == 0 && j == 0) { js = 1; sg = -1.0; }
+  if (kind == 0 && j == last) { js = last - 1; sg = -1.0; }
+  const size_t f = (size_t)(i + 1) + (size_t)n1 * ((size_t)js + (size_t)n2 * (size_t)(k + 1));
+  dst[d] = sg * F[f];
+}
+
+// device field -> Fortran array with every ghost filled (periodic copies in
+// x and z, stored ghost/wall rows in y)
+__global__ void k_pack(double* __restrict__ F, const double* __restrict__ src, int Nx, int nrow, int Nz,
+                       int n1, int n2, int n3) {
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)n1 * n2 * n3) return;
+  const int i1 = (int)(t % n1), j1 = (int)((t / n1) % n2), k1 = (int)(t / ((long)n1 * n2));
+  int i = (i1 - 1) % Nx; if (i < 0) i += Nx;
+  int k = (k1 - 1) % Nz; if (k < 0) k += Nz;
+  const int j = j1 < nrow ? j1 : nrow - 1;
+  F[t] = src[(size_t)i + (size_t)Nx * ((size_t)j + (size_t)nrow * k)];
+}
+
+// device field (rows jlo..jhi) -> dense unique-point array (Nx, jhi-jlo+1, Nz)
+__global__ void k_pack_unique(double* __restrict__ F, const double* __restrict__ src, int Nx, int nrow,
+                              int Nz, int jlo, int nj) {
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (long)Nx * nj * Nz) return;
+  const int i = (int)(t % Nx), j = (int)((t / Nx) % nj), k = (int)(t / ((long)Nx * nj));
+  F[t] = src[(size_t)i + (size_t)Nx * ((size_t)(j + jlo) + (size_t)nrow * k)];
+}
+
+extern "C" {
+void chl_launch_unpack(double* dst, const double* F, int Nx, int nrow, int Nz, int n1, int n2, int kind, cudaStream_t st) {
+  long n = (long)Nx * nrow * Nz;
+  k_unpack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dst, F, Nx, nrow, Nz, n1, n2, kind);
+}
+void chl_launch_pack(double* F, const double* src, int Nx, int nrow, int Nz, int n1, int n2, int n3, cudaStream_t st) {
+  long n = (long)n1 * n2 * n3;
+  k_pack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, src, Nx, nrow, Nz, n1, n2, n3);
+}
+void chl_launch_pack_unique(double* F, const double* src, int Nx, int nrow, int Nz, int jlo, int nj, cudaStream_t st) {
+  long n = (long)Nx * nj * Nz;
+  k_pack_unique<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, src, Nx, nrow, Nz, jlo, nj);
+}
+}
+
+// ------------------------------------------------------------ compute_dt (time_integration.f90:102-150)
+// max(dx/|u|) over points = max over the index with its own spacing of
+// dx/min|u|, so only min |u| per x face (U), per y face row (V) and per z
+// face (W) is reduced; |u| is reduced on its bit pattern (integer pipe).
+#define CHL_BIG_BITS 0x7FF0000000000000ULL
+__device__ __forceinline__ unsigned long long absbits(double v) {
+  return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
+}
+
+// one block per z plane of each instance
+__global__ void __launch_bounds__(256)
+k_minabs(ChlMap map, int s) {
+  extern __shared__ unsigned long long smin[];   // [Nx] U, [Ny+1] V
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const int k = lb;
+  unsigned long long* su = smin;
+  unsigned long long* sv = smin + Nx;
+  for (int w = threadIdx.x; w < Nx + Ny + 1; w += blockDim.x) smin[w] = CHL_BIG_BITS;
+  __syncthreads();
+  const double* U = I.U[s]; const double* V = I.V[s]; const double* W = I.W[s];
+  unsigned long long mw = CHL_BIG_BITS;
+  for (int w = threadIdx.x; w < Nx * Ny; w += blockDim.x) {
+    const int i = w % Nx, jc = 1 + w / Nx;
+    atomicMin(su + i, absbits(U[cidx(I, i, jc, k)]));
+    atomicMin(sv + jc, absbits(V[vidx(I, i, jc, k)]));
+    const unsigned long long b = absbits(W[cidx(I, i, jc, k)]);
+    mw = b < mw ? b : mw;
+  }
+  __shared__ unsigned long long red[256];
+  red[threadIdx.x] = mw;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] = min(red[threadIdx.x], red[threadIdx.x + h]);
+    __syncthreads();
+  }
+  unsigned long long* g = I.minabs;      // [Nx] U, [Ny+1] V, [Nz] W
+  for (int w = threadIdx.x; w < Nx; w += blockDim.x) atomicMin(g + w, su[w]);
+  for (int w = threadIdx.x + 1; w <= Ny; w += blockDim.x) atomicMin(g + Nx + w, sv[w]);
+  if (threadIdx.x == 0) g[Nx + Ny + 1 + k] = red[0];
+}
+
+__global__ void k_minabs_init(ChlMap map) {
+  const ChlInst& I = map.inst[blockIdx.x];
+  const int n = I.Nx + I.Ny + 1 + I.Nz;
+  for (int w = threadIdx.x; w < n; w += blockDim.x) I.minabs[w] = CHL_BIG_BITS;
+}
+
+// one block per instance
+__global__ void k_dt(ChlMap map) {
+  const ChlInst& I = map.inst[blockIdx.x];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const unsigned long long* g = I.minabs;
+  __shared__ double r[3][128];
+  double lu = 0.0, lv = 0.0, lw = 0.0;
+  // U: faces i_f = 2..nxg-1 (my 0..Nx, face Nx is the copy of face 0)
+  for (int i = threadIdx.x; i <= Nx; i += blockDim.x)
+    lu = fmax(lu, I.dxf[i] / __longlong_as_double((long long)g[i == Nx ? 0 : i]));
+  // V: face rows j_f = 2..nyg-1 (my 1..Ny; row Ny is the wall, |V| = 0)
+  for (int j = 1 + threadIdx.x; j <= Ny; j += blockDim.x)
+    lv = fmax(lv, I.dyf[j] / __longlong_as_double((long long)g[Nx + j]));
+  // W: faces k_f = 2..nzg-1 (my 0..Nz)
+  for (int k = threadIdx.x; k <= Nz; k += blockDim.x)
+    lw = fmax(lw, I.dzf[k] / __longlong_as_double((long long)g[Nx + Ny + 1 + (k == Nz ? 0 : k)]));
+  r[0][threadIdx.x] = lu; r[1][threadIdx.x] = lv; r[2][threadIdx.x] = lw;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < blockDim.x; ++w) {
+      lu = fmax(lu, r[0][w]); lv = fmax(lv, r[1][w]); lw = fmax(lw, r[2][w]);
+    }
+    const double C = I.CFL, nu = I.nu;
+    const double dt_conv = fmin(fmin(C * lu, C * lv), C * lw);
+    const double dt_vis = fmin(fmin(C * I.dxmin * I.dxmin / nu, C * I.dymin * I.dymin / nu), C * I.dzmin * I.dzmin / nu);
+    double dt = fmin(dt_conv, dt_vis);
+    dt = fmin(dt, 1e-3);
+    if (C < 0.0) dt = -C;
+    I.scal[CHL_S_DT] = dt;
+  }
+}
+
+// ------------------------------------------------------------ constant mass flow
+// compute_dPx_for_constant_mass_flow (mass_flow.f90:360-413) over the unique
+// x-z points of rows j_f = 3 and nyg-2, then U += dPdx on the interior
+// (time_integration.f90:89-94); one block per instance for the sum.
+__global__ void k_massflow(ChlMap map, int s) {
+  const ChlInst& I = map.inst[blockIdx.x];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const double* U = I.U[s];
+  double acc = 0.0;
+  for (int w = threadIdx.x; w < Nx * Nz; w += blockDim.x) {
+    const int i = w % Nx, k = w / Nx;
+    acc += 0.5 * (U[cidx(I, i, 2, k)] + U[cidx(I, i, Ny - 1, k)]);
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if (threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    const double d = I.scal[CHL_S_Q0] - red[0] / (double)(Nx * Nz);
+    I.scal[CHL_S_SHIFT] = d;
+    I.scal[CHL_S_DPDX] = 0.0;
+  }
+}
+
+__global__ void __launch_bounds__(256)
+k_shift(ChlMap map, int s) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t >= (long)Nx * Ny * Nz) return;
+  const int i = (int)(t % Nx), jc = 1 + (int)((t / Nx) % Ny), k = (int)(t / ((long)Nx * Ny));
+  double* U = I.U[s];
+  const double d = I.scal[CHL_S_SHIFT];
+  const double un = U[cidx(I, i, jc, k)] + d;
+  U[cidx(I, i, jc, k)] = un;
+  if (jc == 1) U[cidx(I, i, 0, k)] = -un;
+  if (jc == Ny) U[cidx(I, i, Ny + 1, k)] = -un;
+}
+
+// time advance t += dt (compute_time_step_RK3 leaves t = to + rk_t(3)*dt)
+__global__ void k_tadvance(ChlMap map) {
+  const ChlInst& I = map.inst[blockIdx.x];
+  if (threadIdx.x == 0) I.scal[CHL_S_T] = I.scal[CHL_S_T] + 1.0 * I.scal[CHL_S_DT];
+}
+
+// ------------------------------------------------------------ divergence check
+// check_divergence (projection.f90:223-245): signed max and max |div| over
+// the unique centres; one block per instance, results in scal.
+__global__ void k_divmax(ChlMap map, int s, double* out) {
+  const ChlInst& I = map.inst[blockIdx.x];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const double *U = I.U[s], *V = I.V[s], *W = I.W[s];
+  double mx = 0.0, ma = 0.0;
+  for (long w = threadIdx.x; w < (long)Nx * Ny * Nz; w += blockDim.x) {
+    const int i = (int)(w % Nx), jc = 1 + (int)((w / Nx) % Ny), k = (int)(w / ((long)Nx * Ny));
+    const double d = (U[cidx(I, i, jc, k)] - U[cidx(I, wrap(i - 1, Nx), jc, k)]) * I.rdxc[i]
+                   + (V[vidx(I, i, jc, k)] - V[vidx(I, i, jc - 1, k)]) * I.rdyc[jc]
+                   + (W[cidx(I, i, jc, k)] - W[cidx(I, i, jc, wrap(k - 1, Nz))]) * I.rdzc[k];
+    mx = fmax(mx, d); ma = fmax(ma, fabs(d));
+  }
+  __shared__ double r0[256], r1[256];
+  r0[threadIdx.x] = mx; r1[threadIdx.x] = ma;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if (threadIdx.x < h) { r0[threadIdx.x] = fmax(r0[threadIdx.x], r0[threadIdx.x + h]); r1[threadIdx.x] = fmax(r1[threadIdx.x], r1[threadIdx.x + h]); }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) { out[2 * blockIdx.x] = r0[0]; out[2 * blockIdx.x + 1] = r1[0]; }
+}
+
+// ------------------------------------------------------------ initial bulk flow Qflow_x_0
+// compute_mean_mass_flow_U (mass_flow.f90:271-309), trapezoid over rows
+// j_f = 3..nyg-1 of the unique x-z points; one block per instance.
+__global__ void k_qflow(ChlMap map, int s, int slot) {
+  const ChlInst& I = map.inst[blockIdx.x];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const double* U = I.U[s];
+  double q = 0.0, n = 0.0;
+  for (long w = threadIdx.x; w < (long)Nx * (Ny - 1) * Nz; w += blockDim.x) {
+    const int i = (int)(w % Nx), jc = 2 + (int)((w / Nx) % (Ny - 1)), k = (int)(w / ((long)Nx * (Ny - 1)));
+    const double dyg = I.dyf[jc - 1];          // yg(j)-yg(j-1), j_f = jc+1
+    q += (U[cidx(I, i, jc, k)] + U[cidx(I, i, jc - 1, k)]) * 0.5 * dyg;
+    n += (1.0 + 1.0) * 0.5 * dyg;
+  }
+  __shared__ double r0[256], r1[256];
+  r0[threadIdx.x] = q; r1[threadIdx.x] = n;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if (threadIdx.x < h) { r0[threadIdx.x] += r0[threadIdx.x + h]; r1[threadIdx.x] += r1[threadIdx.x + h]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) I.scal[slot] = r0[0] / r1[0];
+}
+
+extern "C" {
+void chl_launch_minabs(const ChlMap& m, int nb, size_t smem, int s, cudaStream_t st) {
+  k_minabs_init<<<m.n, 128, 0, st>>>(m);
+  k_minabs<<<nb, 256, smem, st>>>(m, s);
+}
+void chl_launch_dt(const ChlMap& m, cudaStream_t st) { k_dt<<<m.n, 128, 0, st>>>(m); }
+void chl_launch_massflow(const ChlMap& m, cudaStream_t st, int s) { k_massflow<<<m.n, 256, 0, st>>>(m, s); }
+void chl_launch_shift(const ChlMap& m, int nb, int s, cudaStream_t st) { k_shift<<<nb, 256, 0, st>>>(m, s); }
+void chl_launch_tadvance(const ChlMap& m, cudaStream_t st) { k_tadvance<<<m.n, 32, 0, st>>>(m); }
+void chl_launch_divmax(const ChlMap& m, int s, double* out, cudaStream_t st) { k_divmax<<<m.n, 256, 0, st>>>(m, s, out); }
+void chl_launch_qflow(const ChlMap& m, int s, int slot, cudaStream_t st) { k_qflow<<<m.n, 256, 0, st>>>(m, s, slot); }
+}

@@ -1,0 +1,342 @@
+// Subgrid-scale eddy viscosity and wall models.
+//
+// Dynamic Smagorinsky (Lilly) as sgs_dynamic_Smagorinsky does it
+// (subgrid.f90:379-537): test filter filter_xzy (subgrid.f90:140-190, the
+// 1/6-2/3-1/6 rule in x, z and y, one-sided 2/3-1/3 at the first and last
+// row), strain rates of compute_Sij (subgrid.f90:1014-1072), plane sums of
+// L:M and M:M over i=2..nxg-1, k=2..nzg-1 (the duplicated periodic column
+// and plane counted twice, subgrid.f90:492-509), nu_t = max(0,-1/2 <LM>/<MM>|S|)
+// and the ghost-row rule of Dirichlet_nu_t.
+//
+// The filter is applied as three separable passes with unnormalised weights
+// (1,4,1) and (4,2); the 6^3 = 216 scale, the 1/2 of the centre averages
+// and the 1/8 of the edge averages are folded into the final L:M and M:M
+// dot products, which only enter as the ratio <LM>/<MM>.  This keeps the
+// FP64 instruction count per point at its minimum (the GB300 FP64 pipe, not
+// HBM, bounds this code).
+//
+// Static Smagorinsky with van Driest damping (subgrid.f90:563-612, which
+// aborts in the reference) is written from its formula.  The stress wall
+// model is compute_wall_model (wallmodel.f90:23-46); the equilibrium log-law
+// wall stress that feeds it is new.
+#include "chl_common.cuh"
+
+// ---------------------------------------------------------------- edges
+// E12 at (x-face a, y-face jv, z-centre k), E13 at (x-face a, centre row jc,
+// z-face b), E23 at (x-centre i, y-face jv, z-face b): 2 x the edge strain
+// rates of compute_Sij, stored V-like (E12, E23: Ny+1 rows) and centre-like
+// (E13, rows 1..Ny).
+__global__ void __launch_bounds__(256)
+k_edges(ChlMap map, int src) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t >= (long)Nx * (Ny + 1) * Nz) return;
+  const int a = (int)(t % Nx);
+  const int j = (int)((t / Nx) % (Ny + 1));
+  const int k = (int)(t / ((long)Nx * (Ny + 1)));
+  const double *U, *V, *W;
+  if (src < 3) { U = I.U[src]; V = I.V[src]; W = I.W[src]; }
+  else { U = I.r[15]; V = I.r[16]; W = I.r[17]; }
+  const int ap = wrap(a + 1, Nx), kp = wrap(k + 1, Nz);
+  const double rxf = LDG(I.rdxf + a), rzf = LDG(I.rdzf + k), ryf = LDG(I.rdyf + j);
+  // E12 (jv = j): dU/dy + dV/dx
+  const double e12 = (LDG(U + cidx(I, a, j + 1, k)) - LDG(U + cidx(I, a, j, k))) * ryf
+                   + (LDG(V + vidx(I, ap, j, k)) - LDG(V + vidx(I, a, j, k))) * rxf;
+  // E23 (jv = j, b = k): dV/dz + dW/dy
+  const double e23 = (LDG(V + vidx(I, a, j, kp)) - LDG(V + vidx(I, a, j, k))) * rzf
+                   + (LDG(W + cidx(I, a, j + 1, k)) - LDG(W + cidx(I, a, j, k))) * ryf;
+  I.E[0][vidx(I, a, j, k)] = e12;
+  I.E[2][vidx(I, a, j, k)] = e23;
+  if (j >= 1 && j <= Ny) {
+    // E13 (jc = j, b = k): dU/dz + dW/dx
+    const double e13 = (LDG(U + cidx(I, a, j, kp)) - LDG(U + cidx(I, a, j, k))) * rzf
+                     + (LDG(W + cidx(I, ap, j, k)) - LDG(W + cidx(I, a, j, k))) * rxf;
+    I.E[1][cidx(I, a, j, k)] = e13;
+  }
+}
+
+// Centre strain: diagonal D, 8*S_offdiag O (sum of four edges), |S|.
+struct Strain { double d1, d2, d3, o12, o13, o23, s; };
+
+__device__ __forceinline__ Strain centre_strain(const ChlInst& I, const double* U, const double* V,
+                                                const double* W, int i, int jc, int k) {
+  const int im = wrap(i - 1, I.Nx), km = wrap(k - 1, I.Nz);
+  Strain s;
+  s.d1 = (LDG(U + cidx(I, i, jc, k)) - LDG(U + cidx(I, im, jc, k))) * LDG(I.rdxc + i);
+  s.d2 = (LDG(V + vidx(I, i, jc, k)) - LDG(V + vidx(I, i, jc - 1, k))) * LDG(I.rdyc + jc);
+  s.d3 = (LDG(W + cidx(I, i, jc, k)) - LDG(W + cidx(I, i, jc, km))) * LDG(I.rdzc + k);
+  const double* E12 = I.E[0]; const double* E13 = I.E[1]; const double* E23 = I.E[2];
+  s.o12 = (LDG(E12 + vidx(I, im, jc - 1, k)) + LDG(E12 + vidx(I, i, jc - 1, k)))
+        + (LDG(E12 + vidx(I, im, jc, k)) + LDG(E12 + vidx(I, i, jc, k)));
+  s.o13 = (LDG(E13 + cidx(I, im, jc, km)) + LDG(E13 + cidx(I, i, jc, km)))
+        + (LDG(E13 + cidx(I, im, jc, k)) + LDG(E13 + cidx(I, i, jc, k)));
+  s.o23 = (LDG(E23 + vidx(I, i, jc - 1, km)) + LDG(E23 + vidx(I, i, jc, km)))
+        + (LDG(E23 + vidx(I, i, jc - 1, k)) + LDG(E23 + vidx(I, i, jc, k)));
+  // |S|^2 = 2 (d.d) + 4 (S12^2+S13^2+S23^2) = 2 (d.d + (o.o)/32)
+  double dd = s.d1 * s.d1; dd = fma(s.d2, s.d2, dd); dd = fma(s.d3, s.d3, dd);
+  double oo = s.o12 * s.o12; oo = fma(s.o13, s.o13, oo); oo = fma(s.o23, s.o23, oo);
+  s.s = sqrt(2.0 * fma(oo, 0.03125, dd));
+  return s;
+}
+
+// Raw strain and the DSM filter inputs at centres (rows 1..Ny):
+// q0..2 = 2*(centre velocities), q3..8 = their products, q9..14 = |S|*(d, o).
+__global__ void __launch_bounds__(256)
+k_centre(ChlMap map, int s_in, int dsm) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t >= (long)Nx * Ny * Nz) return;
+  const int i = (int)(t % Nx);
+  const int jc = 1 + (int)((t / Nx) % Ny);
+  const int k = (int)(t / ((long)Nx * Ny));
+  const double *U = I.U[s_in], *V = I.V[s_in], *W = I.W[s_in];
+  const Strain s = centre_strain(I, U, V, W, i, jc, k);
+  const size_t c = cidx(I, i, jc, k);
+  I.S[c] = s.s;
+  if (!dsm) return;
+  const int im = wrap(i - 1, Nx), km = wrap(k - 1, Nz);
+  const double uc = LDG(U + cidx(I, im, jc, k)) + LDG(U + c);
+  const double vc = LDG(V + vidx(I, i, jc - 1, k)) + LDG(V + vidx(I, i, jc, k));
+  const double wc = LDG(W + cidx(I, i, jc, km)) + LDG(W + c);
+  I.q[0][c] = uc; I.q[1][c] = vc; I.q[2][c] = wc;
+  I.q[3][c] = uc * uc; I.q[4][c] = vc * vc; I.q[5][c] = wc * wc;
+  I.q[6][c] = uc * vc; I.q[7][c] = uc * wc; I.q[8][c] = vc * wc;
+  I.q[9][c] = s.s * s.d1; I.q[10][c] = s.s * s.d2; I.q[11][c] = s.s * s.d3;
+  I.q[12][c] = s.s * s.o12; I.q[13][c] = s.s * s.o13; I.q[14][c] = s.s * s.o23;
+}
+
+// ------------------------------------------------------------ filter passes
+// y pass: q (and the velocity set s_in for the three face components) -> r.
+// Centre components use rows 1..Ny, U and W rows 0..Ny+1, V rows 0..Ny, each
+// with the one-sided rule at its first and last row.
+__device__ __forceinline__ double fy(const double* f, size_t c, size_t pitch, int j, int j0, int j1) {
+  const double q = LDG(f + c);
+  if (j == j0) return fma(4.0, q, 2.0 * LDG(f + c + pitch));
+  if (j == j1) return fma(4.0, q, 2.0 * LDG(f + c - pitch));
+  return fma(4.0, q, LDG(f + c - pitch) + LDG(f + c + pitch));
+}
+
+__global__ void __launch_bounds__(256)
+k_filter_y(ChlMap map, int s_in) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t >= (long)Nx * (Ny + 2) * Nz) return;
+  const int i = (int)(t % Nx);
+  const int j = (int)((t / Nx) % (Ny + 2));
+  const int k = (int)(t / ((long)Nx * (Ny + 2)));
+  const size_t c = cidx(I, i, j, k);
+  const size_t pc = (size_t)Nx;
+  if (j >= 1 && j <= Ny) {
+#pragma unroll
+    for (int m = 0; m < 15; ++m) I.r[m][c] = fy(I.q[m], c, pc, j, 1, Ny);
+  }
+  I.r[15][c] = fy(I.U[s_in], c, pc, j, 0, Ny + 1);
+  I.r[17][c] = fy(I.W[s_in], c, pc, j, 0, Ny + 1);
+  if (j <= Ny) {
+    const size_t v = vidx(I, i, j, k);
+    I.r[16][v] = fy(I.V[s_in], v, pc, j, 0, Ny);
+  }
+}
+
+// x or z pass (periodic, weights 1-4-1) over all stored rows of each component.
+template <int DIR>
+__global__ void __launch_bounds__(256)
+k_filter_xz(ChlMap map, int from_r) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t >= (long)Nx * (Ny + 2) * Nz) return;
+  const int i = (int)(t % Nx);
+  const int j = (int)((t / Nx) % (Ny + 2));
+  const int k = (int)(t / ((long)Nx * (Ny + 2)));
+  double* const* in = from_r ? I.r : I.q;
+  double* const* out = from_r ? I.q : I.r;
+  const int im = DIR == 0 ? wrap(i - 1, Nx) : i, ip = DIR == 0 ? wrap(i + 1, Nx) : i;
+  const int km = DIR == 1 ? wrap(k - 1, Nz) : k, kp = DIR == 1 ? wrap(k + 1, Nz) : k;
+  const size_t c = cidx(I, i, j, k), cm = cidx(I, im, j, km), cp = cidx(I, ip, j, kp);
+  if (j >= 1 && j <= Ny) {
+#pragma unroll
+    for (int m = 0; m < 15; ++m)
+      out[m][c] = fma(4.0, LDG(in[m] + c), LDG(in[m] + cm) + LDG(in[m] + cp));
+  }
+  out[15][c] = fma(4.0, LDG(in[15] + c), LDG(in[15] + cm) + LDG(in[15] + cp));
+  out[17][c] = fma(4.0, LDG(in[17] + c), LDG(in[17] + cm) + LDG(in[17] + cp));
+  if (j <= Ny) {
+    const size_t v = vidx(I, i, j, k), vm = vidx(I, im, j, km), vp = vidx(I, ip, j, kp);
+    out[16][v] = fma(4.0, LDG(in[16] + v), LDG(in[16] + vm) + LDG(in[16] + vp));
+  }
+}
+
+// ------------------------------------------------------------ L:M, M:M
+// One block per (centre row jc, chunk of the x-z plane); each thread sums its
+// points in a fixed order, then a fixed-order block reduction writes
+// part[0|1][jc][chunk].  Filtered fields live in r after the three passes.
+#define DSM_PPT 4
+__global__ void __launch_bounds__(256)
+k_dsm_final(ChlMap map) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const int np = I.npart;
+  const int jc = 1 + lb / np, chunk = lb % np;
+  const int plane = Nx * Nz;
+  double lm = 0.0, mm = 0.0;
+  const double* const* R = I.r;
+  for (int m = 0; m < DSM_PPT; ++m) {
+    const int pidx = chunk * (256 * DSM_PPT) + m * 256 + threadIdx.x;
+    if (pidx >= plane) break;
+    const int i = pidx % Nx, k = pidx / Nx;
+    const size_t c = cidx(I, i, jc, k);
+    const Strain h = centre_strain(I, R[15], R[16], R[17], i, jc, k);  // 216 x filtered strain
+    const double s4 = 4.0 * h.s;
+    const double M1 = fma(s4, h.d1, -216.0 * LDG(R[9] + c));
+    const double M2 = fma(s4, h.d2, -216.0 * LDG(R[10] + c));
+    const double M3 = fma(s4, h.d3, -216.0 * LDG(R[11] + c));
+    const double M4 = fma(s4, h.o12, -216.0 * LDG(R[12] + c));
+    const double M5 = fma(s4, h.o13, -216.0 * LDG(R[13] + c));
+    const double M6 = fma(s4, h.o23, -216.0 * LDG(R[14] + c));
+    const double fu = LDG(R[0] + c), fv = LDG(R[1] + c), fw = LDG(R[2] + c);
+    const double L1 = fma(216.0, LDG(R[3] + c), -fu * fu);
+    const double L2 = fma(216.0, LDG(R[4] + c), -fv * fv);
+    const double L3 = fma(216.0, LDG(R[5] + c), -fw * fw);
+    const double L4 = fma(216.0, LDG(R[6] + c), -fu * fv);
+    const double L5 = fma(216.0, LDG(R[7] + c), -fu * fw);
+    const double L6 = fma(216.0, LDG(R[8] + c), -fv * fw);
+    double ld = L1 * M1; ld = fma(L2, M2, ld); ld = fma(L3, M3, ld);
+    double lo = L4 * M4; lo = fma(L5, M5, lo); lo = fma(L6, M6, lo);
+    double md = M1 * M1; md = fma(M2, M2, md); md = fma(M3, M3, md);
+    double mo = M4 * M4; mo = fma(M5, M5, mo); mo = fma(M6, M6, mo);
+    double lmp = fma(0.25, lo, ld), mmp = fma(0.03125, mo, md);
+    // duplicated periodic column i=2 and plane k=2 of the reference's sums
+    const double wgt = (i == 0 ? 2.0 : 1.0) * (k == 0 ? 2.0 : 1.0);
+    lm = fma(wgt, lmp, lm);
+    mm = fma(wgt, mmp, mm);
+  }
+  __shared__ double sl[256], sm[256];
+  sl[threadIdx.x] = lm; sm[threadIdx.x] = mm;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) { sl[threadIdx.x] += sl[threadIdx.x + w]; sm[threadIdx.x] += sm[threadIdx.x + w]; }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    I.part[(size_t)jc * np + chunk] = sl[0];
+    I.part[(size_t)(Ny + 2) * np + (size_t)jc * np + chunk] = sm[0];
+  }
+}
+
+// ------------------------------------------------------------ nu_t coefficient per row
+__global__ void k_coef(ChlMap map) {
+  const ChlInst& I = map.inst[blockIdx.x];
+  const int Ny = I.Ny, np = I.npart;
+  for (int jc = threadIdx.x; jc < Ny + 2; jc += blockDim.x) {
+    double c = 0.0;
+    if (jc >= 1 && jc <= Ny) {
+      if (I.LES_model == 2) {
+        double lm = 0.0, mm = 0.0;
+        for (int q = 0; q < np; ++q) {
+          lm += I.part[(size_t)jc * np + q];
+          mm += I.part[(size_t)(Ny + 2) * np + (size_t)jc * np + q];
+        }
+        c = -0.125 * (lm / mm);          // -1/2 * <LM>/<MM>, see the scaling note above
+      } else if (I.LES_model == 1) {
+        // van Driest: f = 1 - exp(-d/25/(nu/utau)), utau = dPdx^0.5 (subgrid.f90:581-599)
+        const double ut = sqrt(I.scal[CHL_S_DPDX]);
+        double f = 1.0 - exp(-I.smag_dwall[jc] / 25.0 / (I.nu / ut));
+        if (I.Dirichlet_nu_t == 0) f = 1.0;
+        const double cd = I.smag_csdelta[jc] * f;   // Cs*Delta_j*f
+        c = cd * cd;
+      }
+    }
+    I.coef[jc] = c;
+  }
+}
+
+// ------------------------------------------------------------ equilibrium log-law wall stress
+#define EQWM_KAPPA 0.41
+#define EQWM_B 5.2
+#define EQWM_ITERS 12
+__device__ double eqlog_tau(double u, double h, double nu) {
+  const double au = fabs(u);
+  const double ut_lam = sqrt(nu * au / h);
+  const double f0 = ut_lam * (log(h * ut_lam / nu) / EQWM_KAPPA + EQWM_B) - au;
+  double ut = ut_lam;
+  if (f0 < 0.0) {
+    for (int it = 0; it < EQWM_ITERS; ++it) {
+      const double lg = log(h * ut / nu);
+      const double f = ut * (lg / EQWM_KAPPA + EQWM_B) - au;
+      const double fp = lg / EQWM_KAPPA + EQWM_B + 1.0 / EQWM_KAPPA;
+      const double d = f / fp;
+      ut = ut - d;
+      if (fabs(d) <= 1e-17 * ut) break;
+    }
+  }
+  const double tau = ut * ut;
+  return u < 0.0 ? -tau : (u > 0.0 ? tau : 0.0);
+}
+
+__global__ void k_eqwm(ChlMap map, int s_in) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t >= 2L * Nx * Nz) return;
+  const int a = (int)(t % Nx), k = (int)((t / Nx) % Nz), wall = (int)(t / ((long)Nx * Nz));
+  const double* U = I.U[s_in];
+  const double u = wall == 0 ? U[cidx(I, a, 3, k)] : U[cidx(I, a, Ny - 2, k)];
+  I.alpha[t] = eqlog_tau(u, wall == 0 ? I.hb : I.ht, I.nu);
+}
+
+// ------------------------------------------------------------ nu_t (+ wall model rows)
+__device__ __forceinline__ double wm_face(const ChlInst& I, const double* U, int a, int k, int wall) {
+  const double al = I.alpha[(size_t)wall * I.Nx * I.Nz + (size_t)k * I.Nx + a];
+  const double du = wall == 0 ? U[cidx(I, a, 1, k)] - U[cidx(I, a, 0, k)]
+                              : U[cidx(I, a, I.Ny, k)] - U[cidx(I, a, I.Ny + 1, k)];
+  return al / (du / I.dyw) - I.nu;
+}
+
+__global__ void __launch_bounds__(256)
+k_nut(ChlMap map, int s_in, int use_wm) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t >= (long)Nx * (Ny + 2) * Nz) return;
+  const int i = (int)(t % Nx);
+  const int jc = (int)((t / Nx) % (Ny + 2));
+  const int k = (int)(t / ((long)Nx * (Ny + 2)));
+  double v = 0.0;
+  if (I.LES_model != 0) {
+    int js = jc, sgn = 1;
+    if (jc == 0) { js = 1; sgn = I.Dirichlet_nu_t == 1 ? -1 : 1; }
+    if (jc == Ny + 1) { js = Ny; sgn = I.Dirichlet_nu_t == 1 ? -1 : 1; }
+    v = fmax(I.coef[js] * I.S[cidx(I, i, js, k)], 0.0);
+    if (sgn < 0) v = -v;
+  }
+  if (use_wm && I.wall_model != 0 && (jc <= 1 || jc >= Ny)) {
+    const int wall = jc <= 1 ? 0 : 1;
+    const double* U = I.U[s_in];
+    v = 0.5 * (wm_face(I, U, wrap(i - 1, Nx), k, wall) + wm_face(I, U, i, k, wall));
+  }
+  I.nut[cidx(I, i, jc, k)] = v;
+}
+
+// ------------------------------------------------------------ launchers
+extern "C" {
+void chl_launch_edges(const ChlMap& m, int nb, int src, cudaStream_t st) { k_edges<<<nb, 256, 0, st>>>(m, src); }
+void chl_launch_centre(const ChlMap& m, int nb, int s_in, int dsm, cudaStream_t st) { k_centre<<<nb, 256, 0, st>>>(m, s_in, dsm); }
+void chl_launch_filter_y(const ChlMap& m, int nb, int s_in, cudaStream_t st) { k_filter_y<<<nb, 256, 0, st>>>(m, s_in); }
+void chl_launch_filter_x(const ChlMap& m, int nb, cudaStream_t st) { k_filter_xz<0><<<nb, 256, 0, st>>>(m, 1); }
+void chl_launch_filter_z(const ChlMap& m, int nb, cudaStream_t st) { k_filter_xz<1><<<nb, 256, 0, st>>>(m, 0); }
+void chl_launch_dsm_final(const ChlMap& m, int nb, cudaStream_t st) { k_dsm_final<<<nb, 256, 0, st>>>(m); }
+void chl_launch_coef(const ChlMap& m, cudaStream_t st) { k_coef<<<m.n, 128, 0, st>>>(m); }
+void chl_launch_eqwm(const ChlMap& m, int nb, int s_in, cudaStream_t st) { k_eqwm<<<nb, 256, 0, st>>>(m, s_in); }
+void chl_launch_nut(const ChlMap& m, int nb, int s_in, int use_wm, cudaStream_t st) { k_nut<<<nb, 256, 0, st>>>(m, s_in, use_wm); }
+}

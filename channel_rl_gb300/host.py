@@ -1,0 +1,291 @@
+"""Python mirror of the reference's hot-path interface over the C ABI.
+
+``Channel`` exposes the Fortran subroutines of wadaniel/channel_RL that the
+library replaces, under their own names (compute_dt, compute_time_step_RK3,
+compute_eddy_viscosity, compute_wall_model, compute_rhs_u/v/w,
+compute_projection_step, compute_dPx_for_constant_mass_flow,
+compute_pressure, check_divergence, compute_statistics), operating on the
+GPU-resident state of one or more channel instances.  Arrays crossing the
+boundary are Fortran-ordered float64 with the reference's ghosted extents.
+
+There is no CPU path: if ``libchl.so`` cannot be loaded or CUDA reports an
+error, the call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import build as _build
+from .cases import Case, faces
+
+_LIB = None
+_F64P = C.POINTER(C.c_double)
+
+
+class ChlError(RuntimeError):
+    pass
+
+
+class GridDesc(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("x", _F64P), ("y", _F64P), ("z", _F64P),
+                ("nu", C.c_double), ("CFL", C.c_double), ("dPdx", C.c_double),
+                ("x_mass_cte", C.c_int), ("LES_model", C.c_int), ("Dirichlet_nu_t", C.c_int),
+                ("wall_model", C.c_int), ("Cs", C.c_double)]
+
+
+class StatsOut(C.Structure):
+    _fields_ = [(n, C.c_double) for n in
+                ("utau", "Retau", "tau_wall", "Qflow_x", "Qflow_y", "dt", "t", "dPdx",
+                 "max_div", "max_abs_div")]
+
+
+# every symbol declared in include/chl.h
+EXPORTS = (
+    "chl_create", "chl_batch_create", "chl_destroy", "chl_last_error", "chl_num_instances",
+    "chl_upload", "chl_download", "chl_download_pseudo_pressure", "chl_set_wall_stress",
+    "chl_get_wall_stress", "chl_get_scalars", "chl_set_scalars", "chl_compute_dt",
+    "chl_compute_time_step_RK3", "chl_rk3_step", "chl_compute_eddy_viscosity",
+    "chl_compute_wall_model", "chl_compute_rhs", "chl_compute_projection_step",
+    "chl_compute_dPx_for_constant_mass_flow", "chl_compute_pressure", "chl_check_divergence",
+    "chl_stats", "chl_stats_profiles", "chl_synchronize", "chl_grid_constants_size",
+    "chl_grid_constants",
+)
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libchl.so (building it in-tree if asked and absent)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise ChlError(f"{path} missing: run channel_rl_gb300.build.build()")
+        _build.build()
+    lib = C.CDLL(path)
+    H = C.c_void_p
+    lib.chl_create.argtypes = [C.POINTER(GridDesc), C.POINTER(H)]
+    lib.chl_batch_create.argtypes = [C.c_int, C.POINTER(GridDesc), C.POINTER(H)]
+    lib.chl_destroy.argtypes = [H]
+    lib.chl_last_error.argtypes = [H]
+    lib.chl_last_error.restype = C.c_char_p
+    lib.chl_num_instances.argtypes = [H]
+    lib.chl_upload.argtypes = [H, C.c_int, _F64P, _F64P, _F64P]
+    lib.chl_download.argtypes = [H, C.c_int, _F64P, _F64P, _F64P, _F64P, _F64P]
+    lib.chl_download_pseudo_pressure.argtypes = [H, C.c_int, _F64P]
+    lib.chl_set_wall_stress.argtypes = [H, C.c_int, _F64P]
+    lib.chl_get_wall_stress.argtypes = [H, C.c_int, _F64P]
+    lib.chl_get_scalars.argtypes = [H, C.c_int, _F64P]
+    lib.chl_set_scalars.argtypes = [H, C.c_int, _F64P]
+    for n in ("chl_compute_dt", "chl_compute_time_step_RK3", "chl_compute_eddy_viscosity",
+              "chl_compute_wall_model", "chl_compute_projection_step", "chl_compute_pressure",
+              "chl_synchronize"):
+        getattr(lib, n).argtypes = [H]
+    lib.chl_rk3_step.argtypes = [H, C.c_int]
+    lib.chl_compute_rhs.argtypes = [H, C.c_int, _F64P, _F64P, _F64P]
+    lib.chl_compute_dPx_for_constant_mass_flow.argtypes = [H, C.c_int, _F64P]
+    lib.chl_check_divergence.argtypes = [H, C.c_int, _F64P, _F64P]
+    lib.chl_stats.argtypes = [H, C.c_int, C.POINTER(StatsOut)]
+    lib.chl_stats_profiles.argtypes = [H, C.c_int] + [_F64P] * 7
+    lib.chl_grid_constants_size.argtypes = [C.POINTER(GridDesc)]
+    lib.chl_grid_constants.argtypes = [C.POINTER(GridDesc), _F64P]
+    _LIB = lib
+    return lib
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    assert a.dtype == np.float64
+    return a.ctypes.data_as(_F64P)
+
+
+@dataclass
+class _Keep:
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+
+
+def grid_desc(case: Case, keep: list):
+    x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in faces(case))
+    keep.append(_Keep(x, y, z))
+    wm = case.wall_model if case.wall_model in (0, 1, 2) else 1
+    return GridDesc(case.nx, case.ny, case.nz, _ptr(x), _ptr(y), _ptr(z), case.nu, case.CFL,
+                    case.dPdx, case.x_mass_cte, case.LES_model, case.Dirichlet_nu_t, wm, case.Cs)
+
+
+def grid_constants(case: Case):
+    """Host-side grid constants from the library (no GPU needed)."""
+    lib = load()
+    keep = []
+    d = grid_desc(case, keep)
+    n = lib.chl_grid_constants_size(C.byref(d))
+    out = np.zeros(n)
+    rc = lib.chl_grid_constants(C.byref(d), _ptr(out))
+    if rc:
+        raise ChlError(f"chl_grid_constants failed ({rc})")
+    Nx, Nz, nyg, ny = case.Nx, case.Nz, case.Ny + 2, case.ny
+    o = 0
+    res = {}
+    for name, m in (("kxx", Nx), ("kzz", Nz), ("Dd", nyg - 2), ("Du", nyg - 2), ("Dl", nyg - 2), ("w0", ny)):
+        res[name] = out[o:o + m].copy()
+        o += m
+    res["dxmin"], res["dymin"], res["dzmin"], res["coef_bc_1"], res["coef_bc_2"] = out[o:o + 5]
+    return res
+
+
+class Channel:
+    """One or more channel instances resident on the GPU."""
+
+    def __init__(self, cases):
+        if isinstance(cases, Case):
+            cases = [cases]
+        self.cases = list(cases)
+        self.lib = load()
+        self._keep = []
+        descs = (GridDesc * len(self.cases))(*[grid_desc(c, self._keep) for c in self.cases])
+        self.h = C.c_void_p()
+        rc = self.lib.chl_batch_create(len(self.cases), descs, C.byref(self.h))
+        self._check(rc, "chl_batch_create")
+
+    # -- plumbing ------------------------------------------------------------
+    def _check(self, rc, what):
+        if rc:
+            msg = self.lib.chl_last_error(self.h).decode() if self.h else ""
+            raise ChlError(f"{what} failed ({rc}): {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.chl_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _shape(self, q, field):
+        c = self.cases[q]
+        nx, ny, nz = c.nx, c.ny, c.nz
+        return {"U": (nx, ny + 1, nz + 1), "V": (nx + 1, ny, nz + 1), "W": (nx + 1, ny + 1, nz),
+                "P": (nx + 1, ny + 1, nz + 1)}[field]
+
+    # -- state ---------------------------------------------------------------
+    def upload(self, U, V, W, inst=0):
+        arrs = [np.asfortranarray(a, dtype=np.float64) for a in (U, V, W)]
+        for a, f in zip(arrs, "UVW"):
+            if a.shape != self._shape(inst, f):
+                raise ValueError(f"{f} has shape {a.shape}, expected {self._shape(inst, f)}")
+        rc = self.lib.chl_upload(self.h, inst, *[_ptr(a) for a in arrs])
+        self._check(rc, "chl_upload")
+
+    def download(self, inst=0, fields=("U", "V", "W")):
+        out = {}
+        args = []
+        for f in ("U", "V", "W", "P", "nu_t"):
+            if f in fields:
+                a = np.zeros(self._shape(inst, "P" if f == "nu_t" else f), order="F")
+                out[f] = a
+                args.append(_ptr(a))
+            else:
+                args.append(None)
+        rc = self.lib.chl_download(self.h, inst, *args)
+        self._check(rc, "chl_download")
+        return out
+
+    def pseudo_pressure(self, inst=0):
+        a = np.zeros(self._shape(inst, "P"), order="F")
+        self._check(self.lib.chl_download_pseudo_pressure(self.h, inst, _ptr(a)), "download p")
+        return a
+
+    def set_wall_stress(self, alpha_x, inst=0):
+        a = np.asfortranarray(alpha_x, dtype=np.float64)
+        c = self.cases[inst]
+        if a.shape != (c.nx, 2, c.nz + 1):
+            raise ValueError("alpha_x must be (nx, 2, nzg)")
+        self._check(self.lib.chl_set_wall_stress(self.h, inst, _ptr(a)), "chl_set_wall_stress")
+
+    def wall_stress(self, inst=0):
+        c = self.cases[inst]
+        a = np.zeros((c.nx, 2, c.nz + 1), order="F")
+        self._check(self.lib.chl_get_wall_stress(self.h, inst, _ptr(a)), "chl_get_wall_stress")
+        return a
+
+    def scalars(self, inst=0):
+        s = np.zeros(4)
+        self._check(self.lib.chl_get_scalars(self.h, inst, _ptr(s)), "chl_get_scalars")
+        return dict(dt=s[0], t=s[1], dPdx=s[2], Qflow_x_0=s[3])
+
+    def set_scalars(self, inst=0, **kw):
+        cur = self.scalars(inst)
+        cur.update(kw)
+        s = np.array([cur["dt"], cur["t"], cur["dPdx"], cur["Qflow_x_0"]])
+        self._check(self.lib.chl_set_scalars(self.h, inst, _ptr(s)), "chl_set_scalars")
+
+    # -- reference subroutines -------------------------------------------------
+    def compute_dt(self):
+        self._check(self.lib.chl_compute_dt(self.h), "compute_dt")
+
+    def compute_time_step_RK3(self):
+        self._check(self.lib.chl_compute_time_step_RK3(self.h), "compute_time_step_RK3")
+
+    def step(self, nsteps=1):
+        """nsteps x (compute_dt; compute_time_step_RK3), graph-replayed, async."""
+        self._check(self.lib.chl_rk3_step(self.h, nsteps), "chl_rk3_step")
+
+    def synchronize(self):
+        self._check(self.lib.chl_synchronize(self.h), "synchronize")
+
+    def compute_eddy_viscosity(self):
+        self._check(self.lib.chl_compute_eddy_viscosity(self.h), "compute_eddy_viscosity")
+
+    def compute_wall_model(self):
+        self._check(self.lib.chl_compute_wall_model(self.h), "compute_wall_model")
+
+    def compute_rhs(self, inst=0):
+        """(Fu, Fv, Fw) on the unique points: (Nx,Ny,Nz), (Nx,Ny-1,Nz), (Nx,Ny,Nz)."""
+        c = self.cases[inst]
+        Fu = np.zeros((c.Nx, c.Ny, c.Nz), order="F")
+        Fv = np.zeros((c.Nx, c.Ny - 1, c.Nz), order="F")
+        Fw = np.zeros((c.Nx, c.Ny, c.Nz), order="F")
+        self._check(self.lib.chl_compute_rhs(self.h, inst, _ptr(Fu), _ptr(Fv), _ptr(Fw)), "compute_rhs")
+        return Fu, Fv, Fw
+
+    def compute_projection_step(self):
+        self._check(self.lib.chl_compute_projection_step(self.h), "compute_projection_step")
+
+    def compute_dPx_for_constant_mass_flow(self, inst=0):
+        d = C.c_double()
+        self._check(self.lib.chl_compute_dPx_for_constant_mass_flow(self.h, inst, C.byref(d)),
+                    "compute_dPx_for_constant_mass_flow")
+        return d.value
+
+    def compute_pressure(self):
+        self._check(self.lib.chl_compute_pressure(self.h), "compute_pressure")
+
+    def check_divergence(self, inst=0):
+        a, b = C.c_double(), C.c_double()
+        self._check(self.lib.chl_check_divergence(self.h, inst, C.byref(a), C.byref(b)), "check_divergence")
+        return a.value, b.value
+
+    def compute_statistics(self, inst=0):
+        s = StatsOut()
+        self._check(self.lib.chl_stats(self.h, inst, C.byref(s)), "chl_stats")
+        out = {n: getattr(s, n) for n, _ in StatsOut._fields_}
+        ny = self.cases[inst].ny
+        prof = [np.zeros(ny) for _ in range(7)]
+        self._check(self.lib.chl_stats_profiles(self.h, inst, *[_ptr(p) for p in prof]), "chl_stats_profiles")
+        for n, p in zip(("Umean", "Vmean", "Wmean", "U2mean", "V2mean", "W2mean", "UVmean"), prof):
+            out[n] = p
+        return out

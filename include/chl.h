@@ -1,0 +1,137 @@
+/*
+ * chl.h - C ABI of the GB300 channel-LES time step.
+ *
+ * Drop-in for the hot path of wadaniel/channel_RL: the Fortran subroutines
+ * that advance the resident channel state one RK3 step.  Each entry point
+ * names the reference routine it replaces (file:line in the reference's
+ * code/ directory).  Plain pointers and sizes only; arrays are Fortran
+ * column-major with the reference's full ghosted extents unless stated.
+ *
+ * Grid convention: nx, ny, nz are the reference's global FACE counts
+ * (nx_global, ny_global, nz_global, global.f90:46); Nx = nx-2 and Nz = nz-2
+ * are the FFT lengths (initialization.f90:258-259), Ny = ny-1 wall-normal
+ * cells; nxg = nx+1, nyg = ny+1, nzg = nz+1.  Field extents:
+ *   U(nx,nyg,nzg)  V(nxg,ny,nzg)  W(nxg,nyg,nz)  P, nu_t(nxg,nyg,nzg)
+ *
+ * Return values: 0 on success, >0 an error code (CHL_E_*); chl_last_error()
+ * gives the message.  No entry point aborts the process.
+ *
+ * Threading: a handle belongs to one host thread at a time.  All device work
+ * is ordered on the handle's CUDA stream; calls that return host data
+ * synchronise that stream.
+ */
+#ifndef CHL_H
+#define CHL_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CHL_OK 0
+#define CHL_E_ARG 1      /* invalid argument / size */
+#define CHL_E_CUDA 2     /* CUDA runtime error */
+#define CHL_E_NOMEM 3    /* device allocation failed */
+#define CHL_E_STATE 4    /* call out of order (e.g. step before upload) */
+#define CHL_E_NAN 5      /* non-finite values detected in the fields */
+
+/* LES_model (subgrid.f90:30-45) */
+#define CHL_LES_NONE 0
+#define CHL_LES_SMAGORINSKY 1
+#define CHL_LES_DYNAMIC 2
+/* wall_model */
+#define CHL_WM_NONE 0     /* no-slip: compute_wall_model skipped */
+#define CHL_WM_STRESS 1   /* compute_wall_model with a caller-set alpha_x (wallmodel.f90:23-46) */
+#define CHL_WM_EQLOG 2    /* equilibrium log law at the third cell computes alpha_x each stage */
+
+typedef struct chl_handle chl_handle;
+
+/* Grid and input parameters of one channel instance: the reference's
+ * parameter file (input_output.f90:20-91) plus the face coordinates it reads
+ * from the snapshot (global.f90:63-67). */
+typedef struct {
+  int nx, ny, nz;              /* face counts; nx, nz even; ny >= 5 */
+  const double* x;             /* x(1:nx) */
+  const double* y;             /* y(1:ny), y(1) and y(ny) are the walls */
+  const double* z;             /* z(1:nz) */
+  double nu;                   /* kinematic viscosity */
+  double CFL;                  /* CFL number, or -dt for a fixed step */
+  double dPdx;                 /* imposed pressure gradient (x_mass_cte = 0) */
+  int x_mass_cte;              /* 1: constant mass flow (mass_flow.f90:360-413) */
+  int LES_model;               /* CHL_LES_* */
+  int Dirichlet_nu_t;          /* 1: nu_t ghost = -nu_t (Dirichlet), 0: Neumann */
+  int wall_model;              /* CHL_WM_* */
+  double Cs;                   /* static Smagorinsky constant */
+} chl_grid_desc;
+
+/* Statistics of compute_statistics (statistics.f90:22-145). */
+typedef struct {
+  double utau, Retau, tau_wall, Qflow_x, Qflow_y, dt, t, dPdx, max_div, max_abs_div;
+} chl_stats_out;
+
+/* initialize (initialization.f90:23-497) for one instance / n instances
+ * advanced together.  Allocates every device buffer once. */
+int chl_create(const chl_grid_desc* desc, chl_handle** out);
+int chl_batch_create(int n, const chl_grid_desc* descs, chl_handle** out);
+/* finalize (finalization.f90:19-121). */
+int chl_destroy(chl_handle* h);
+const char* chl_last_error(const chl_handle* h);
+int chl_num_instances(const chl_handle* h);
+
+/* Load U, V, W (full Fortran extents; ghosts are re-derived by the
+ * boundary conditions, as the snapshot reader does, input_output.f90:514-540)
+ * and set the initial bulk flow Qflow_x_0 (initialization.f90:442). */
+int chl_upload(chl_handle* h, int inst, const double* U, const double* V, const double* W);
+/* Fields with every ghost filled; any pointer may be NULL.  P is the actual
+ * pressure of the last chl_compute_pressure call. */
+int chl_download(chl_handle* h, int inst, double* U, double* V, double* W, double* P, double* nu_t);
+/* Pseudo-pressure of the last projection (rhs_p, projection.f90:119-126), P layout. */
+int chl_download_pseudo_pressure(chl_handle* h, int inst, double* p);
+
+/* Wall stress alpha_x(nx,2,nzg) of the stress wall model (set by the RL
+ * driver in the reference, smarties_stat.f90:180-258).  Only the unique
+ * points i=2..nx-1, k=2..nzg-2 are read. */
+int chl_set_wall_stress(chl_handle* h, int inst, const double* alpha_x);
+int chl_get_wall_stress(chl_handle* h, int inst, double* alpha_x);
+
+/* scalars: [0] dt, [1] t, [2] dPdx, [3] Qflow_x_0 */
+int chl_get_scalars(chl_handle* h, int inst, double* out4);
+int chl_set_scalars(chl_handle* h, int inst, const double* in4);
+
+/* compute_dt (time_integration.f90:102-150), all instances. */
+int chl_compute_dt(chl_handle* h);
+/* compute_time_step_RK3 (time_integration.f90:24-96) with the current dt. */
+int chl_compute_time_step_RK3(chl_handle* h);
+/* nsteps x { compute_dt; compute_time_step_RK3 } (app_main.f90:114-117),
+ * replayed from one captured CUDA graph; asynchronous. */
+int chl_rk3_step(chl_handle* h, int nsteps);
+
+/* Per-subroutine entry points on the current fields (for parity bisection). */
+int chl_compute_eddy_viscosity(chl_handle* h);       /* subgrid.f90:23-47 */
+int chl_compute_wall_model(chl_handle* h);           /* wallmodel.f90:23-46 (eq. log law first if CHL_WM_EQLOG) */
+/* compute_rhs_u/v/w (equations.f90:24-468) of the current fields and nu_t;
+ * outputs on the unique points: Fu(Nx,Ny,Nz), Fv(Nx,Ny-1,Nz), Fw(Nx,Ny,Nz). */
+int chl_compute_rhs(chl_handle* h, int inst, double* Fu, double* Fv, double* Fw);
+int chl_compute_projection_step(chl_handle* h);      /* projection.f90:20-28 */
+int chl_compute_dPx_for_constant_mass_flow(chl_handle* h, int inst, double* dPdx); /* mass_flow.f90:360-413 */
+int chl_compute_pressure(chl_handle* h);             /* pressure.f90:21-29 */
+int chl_check_divergence(chl_handle* h, int inst, double* max_div, double* max_abs_div); /* projection.f90:223-245 */
+int chl_stats(chl_handle* h, int inst, chl_stats_out* out);  /* statistics.f90:22-145 */
+
+/* Profiles of compute_statistics, each of length ny: Umean, Vmean, Wmean,
+ * U2mean, V2mean, W2mean, UVmean (any may be NULL). */
+int chl_stats_profiles(chl_handle* h, int inst, double* Umean, double* Vmean, double* Wmean,
+                       double* U2mean, double* V2mean, double* W2mean, double* UVmean);
+
+int chl_synchronize(chl_handle* h);
+
+/* Host-only: the grid constants chl_create derives (initialization.f90:
+ * 187-427), for checking without a GPU.  out must hold chl_grid_constants_size
+ * doubles: [kxx(0:Nx-1), kzz(0:Nz-1), Dd(2:nyg-1), Du(2:nyg-1), Dl(2:nyg-1),
+ * w0(1:ny), dxmin, dymin, dzmin, coef_bc_1, coef_bc_2]. */
+int chl_grid_constants_size(const chl_grid_desc* desc);
+int chl_grid_constants(const chl_grid_desc* desc, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
