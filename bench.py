@@ -1,0 +1,393 @@
+#!/usr/bin/env python
+"""LES grid-point RK3 steps/s on GB300 (one JSON line on stdout).
+
+Default workload: the roofline-sizing channel, 8pi x 2 x 3pi, 256x96x192
+cells, Re_tau 5200, equilibrium log-law wall model, dynamic Smagorinsky
+(``--workload c3_smag`` for the static-Smagorinsky variant).  A step is one
+iteration of the reference's solver loop: compute_dt + compute_time_step_RK3
+(app_main.f90:114-117), replayed from one CUDA graph.
+
+  value   grid points x steps / device seconds (CUDA events on the library's
+          stream), fields resident in HBM; per-step working set >> L2.
+  e2e     same metric through the C ABI with host buffers: every step uploads
+          U, V, W from pinned host memory (chl_set_fields), steps, and reads
+          U, V, W back (chl_download_async), timed on the host clock.
+  --impl reference
+          the reference algorithm on the host cores: the oracle restatement
+          (the Fortran reference cannot be built: no gfortran/MPI/FFTW here or
+          on the GPU host), each step a bounded sample of the same workload.
+
+Multi-GPU (torchrun): independent replicas (one channel per rank, weak
+scaling); value = all ranks' grid-point steps / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+import numpy as np
+
+from channel_rl_gb300 import cases as C
+
+METRIC = "LES grid-point RK3 steps/s"
+UNIT = "grid-point-steps/s"
+
+# Algorithmic HBM bytes per grid point per launch of each kernel (compulsory
+# 8-byte streams; spectral arrays count their half-spectrum share).
+KERNEL_BYTES = {
+    "rhs_flux": 8 * 13.0,        # U, V, W, nu+nu_t in; 9 face fluxes out
+    "rhs_update": 8 * 18.0,      # 9 fluxes + 3 base (+3 F1) in; 3 (+3 F1) out
+    "filter_y": 8 * 36.0, "filter_x": 8 * 36.0, "filter_z": 8 * 36.0,   # 18 components in + out
+    "centre_strain": 8 * 22.0,   # U,V,W + 3 edge fields in, |S| + 15 filter inputs out
+    "edges": 8 * 6.0,
+    "dsm_LM_MM": 8 * 21.0,
+    "nut": 8 * 2.0,
+    "div_fft_x": 8 * 4.0,        # U,V,W in, half spectrum out
+    "fft_z": 8 * 2.0,
+    "tridiag": 8 * 5.5,
+    "ifft_x": 8 * 2.0,
+    "project": 8 * 7.0,
+    "massflow_shift": 8 * 2.0,
+    "dt_minabs": 8 * 3.0,
+}
+# Compulsory traffic of an ideally fused step (8-byte streams per point):
+# 107 with the dynamic model, 101 with static Smagorinsky.
+STEP_STREAMS = {"dsm": 107, "smag": 101}
+
+
+def workload(name):
+    if name == "c3_dsm":
+        return [C.c3_roofline(les=C.LES_DSM)]
+    if name == "c3_smag":
+        return [C.c3_roofline(les=C.LES_SMAG)]
+    if name == "c3_dsm_small":
+        return [C.smaller(C.c3_roofline(les=C.LES_DSM), 128, 96, 96)]
+    if name == "c1":
+        return [C.c1_small()]
+    if name == "c2":
+        return [C.c2_wm64()]
+    if name == "c4":
+        return C.c4_ensemble()
+    raise SystemExit(f"unknown workload {name}")
+
+
+def load_json(path, default=None):
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except Exception:
+        return default
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clocks/throttle reasons sampled during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[3:7]):
+                if v.lower() in ("active", "1"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- distributed plumbing
+def dist_setup(n):
+    if n <= 1 or "RANK" not in os.environ:
+        return 0, 1, None
+    import torch
+    import torch.distributed as dist
+    rank, world = int(os.environ["RANK"]), int(os.environ["WORLD_SIZE"])
+    backend = "nccl" if torch.cuda.is_available() else "gloo"
+    if backend == "nccl":
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    dist.init_process_group(backend=backend)
+    return rank, world, dist
+
+
+def reduce_max_sum(dist, tmax, work):
+    """Max of the per-rank time, sum of the per-rank work (grid-point steps)."""
+    if dist is None:
+        return tmax, work
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([tmax], dtype=torch.float64, device=dev)
+    w = torch.tensor([work], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(w, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(w.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- CPU (oracle) timing
+SAMPLE_POINTS = 600_000
+
+
+def cpu_sample(cases_):
+    """Bounded sample of a workload for the host-core timing: instances in
+    order up to ~SAMPLE_POINTS cells; an instance larger than that keeps its
+    x-y plane and physics and is cut to fewer z planes (a slab), so the
+    per-point work is that of the full workload."""
+    out, pts = [], 0
+    for c in cases_:
+        if pts >= SAMPLE_POINTS:
+            break
+        if c.points > SAMPLE_POINTS:
+            nz = c.Nz
+            while c.Nx * c.Ny * nz > SAMPLE_POINTS and nz % 2 == 0 and nz > 8:
+                nz //= 2
+            c = C.smaller(c, c.Nx, c.Ny, nz)
+        out.append(c)
+        pts += c.points
+    return out
+
+
+def describe(cases_):
+    if len(cases_) == 1:
+        c = cases_[0]
+        return f"{c.Nx}x{c.Ny}x{c.Nz}"
+    return f"{len(cases_)} instances, {sum(c.points for c in cases_)} cells"
+
+
+def oracle_step_rate(cases_, budget_s, max_steps):
+    """Grid-point steps/s of the oracle restatement on this host, timing
+    whole steps of the given workload until budget_s (at least one)."""
+    from oracle.channel_ref import ChannelOracle, Grid, Params
+    total_pts, total_t, nsteps = 0, 0.0, 0
+    for case in cases_:
+        o = ChannelOracle(Grid(*C.faces(case)),
+                          Params(nu=case.nu, CFL=case.CFL, dPdx=case.dPdx, x_mass_cte=case.x_mass_cte,
+                                 LES_model=case.LES_model, Dirichlet_nu_t=case.Dirichlet_nu_t,
+                                 wall_model=min(case.wall_model, 2), Cs=case.Cs))
+        o.set_fields(*C.initial_fields(case))
+        t0 = time.perf_counter()
+        n = 0
+        while n < max_steps:
+            o.step()
+            n += 1
+            if time.perf_counter() - t0 > budget_s / len(cases_):
+                break
+        total_t += time.perf_counter() - t0
+        total_pts += case.points * n
+        nsteps += n
+    return total_pts / total_t, nsteps, total_t
+
+
+def run_reference(args):
+    rank, world, dist = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    cases_ = workload(args.workload)
+    samp = cpu_sample(cases_)
+    rate, nsteps, secs = oracle_step_rate(samp, args.ref_budget, max(1, args.steps))
+    sample = (f"{nsteps} RK3 step(s) (compute_dt + compute_time_step_RK3) of {describe(samp)} cut from "
+              f"{args.workload} ({describe(cases_)}): same physics, NumPy restatement of the reference, "
+              f"{secs:.1f} s on 1 host core")
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": nsteps, "warmup": 0, "ms_per_step": 1e3 * secs / nsteps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_of(args, cases_),
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def config_of(args, cases_):
+    c0 = cases_[0]
+    les = {0: "none", 1: "static-smagorinsky", 2: "dynamic-smagorinsky"}[c0.LES_model]
+    wm = {0: "none", 1: "stress", 2: "equilibrium-loglaw", 3: "mlp"}[c0.wall_model]
+    return {"workload": args.workload, "instances": len(cases_),
+            "grid": f"{c0.Nx}x{c0.Ny}x{c0.Nz}" if len(cases_) == 1 else "mixed",
+            "points": sum(c.points for c in cases_), "Re_tau": c0.Retau, "sgs": les, "wall_model": wm,
+            "parallelism": f"replicas{args.gpus}", "l2": "inputs larger than L2 (per-step working set > 1 GB)"}
+
+
+# ---------------------------------------------------------------- our arm
+def run_ours(args):
+    rank, world, dist = dist_setup(args.gpus)
+    import torch
+    from channel_rl_gb300.host import Channel, load
+    torch.cuda.init()
+    dev_index = int(os.environ.get("LOCAL_RANK", 0))
+    cases_ = workload(args.workload)
+    ch = Channel(cases_)
+    for q, case in enumerate(cases_):
+        ch.upload(*C.initial_fields(case), inst=q)
+    points = sum(c.points for c in cases_)
+    # warm-up (builds the graph on the first call)
+    ch.step(max(args.warmup, 1))
+    ch.synchronize()
+    nker = ch.graph_kernel_count()
+    # timed region: barrier + sync on both sides, device time by CUDA events
+    barrier(dist)
+    torch.cuda.synchronize()
+    with ClockSampler(dev_index) as clk:
+        t0 = time.perf_counter()
+        ms = ch.time_steps(args.steps)
+        wall = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    barrier(dist)
+    tmax_ms, work = reduce_max_sum(dist, ms, points * args.steps)
+    value = work / (tmax_ms * 1e-3)
+    # per-kernel breakdown (event-bracketed, un-graphed steps)
+    prof = ch.profile_step(reps=args.prof_reps)
+    tot_prof = sum(v[0] for v in prof.values())
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    per_launch_s = dom_ms / dom_n * 1e-3
+    peaks = load_json(os.path.join(HERE, "MEASURED_PEAKS.json"), {})
+    hbm_peak = float(peaks.get("hbm_gbs", 6789.6))
+    fp64 = load_json(os.path.join(HERE, "profiles", "fp64_peak.json"), {})
+    fp64_peak = fp64.get("dfma_gflops")
+    traffic = load_json(os.path.join(HERE, "profiles", "kernel_traffic.json"), {})
+    byt = KERNEL_BYTES.get(dom, 0.0) * points
+    achieved = byt / per_launch_s / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+            "frac": achieved / hbm_peak, "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": (traffic.get(args.workload, {}).get(dom) if traffic else None),
+            "algorithmic_bytes_per_launch": byt, "launch_ms": per_launch_s * 1e3}
+    sgs = "dsm" if cases_[0].LES_model == 2 else "smag"
+    step_bytes = 8 * STEP_STREAMS[sgs] * points
+    roof["step_hbm_gbs_vs_fused_minimum"] = step_bytes / (tmax_ms / args.steps * 1e-3) / 1e9
+    fl = traffic.get("fp64_ops_per_point", {}).get(args.workload, {}) if traffic else {}
+    if fp64_peak and dom in fl:
+        fp = fl[dom] * 2.0 * points / per_launch_s / 1e9   # DFMA counted as 2 flops
+        roof["fp64"] = {"bound": "fp64", "achieved": fp, "peak": fp64_peak, "unit": "GFLOP/s",
+                        "frac": fp / fp64_peak, "peak_source": "measured (profiles/fp64_peak.json)"}
+    # e2e through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e and len(cases_) == 1:
+        e2e = e2e_rate(ch, cases_[0], args)
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tmax_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_of(args, cases_), "e2e": e2e, "roofline": roof,
+            "gpu_launches": nker * args.steps, "clocks": clk.summary(),
+            "host_wall_s": wall,
+            "kernels_ms_per_step": {k: round(v[0], 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
+            "profiled_step_ms": tot_prof}
+    if rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
+        samp = cpu_sample(cases_)
+        rate, nsteps, secs = oracle_step_rate(samp, args.cpu_budget, 50)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"{nsteps} RK3 step(s) of {describe(samp)} cut from {args.workload} "
+                                          f"({describe(cases_)}), same physics, NumPy restatement of the "
+                                          f"reference, {secs:.1f} s on 1 host core"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    ch.close()
+
+
+def e2e_rate(ch, case, args):
+    import torch
+    U, V, W = C.initial_fields(case)
+    pin = []
+    for a in (U, V, W):
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        v = t.numpy().reshape(a.shape, order="F")
+        v[...] = a
+        pin.append((t, v))
+    out = []
+    for a in (U, V, W):
+        t = torch.empty(a.size, dtype=torch.float64, pin_memory=True)
+        out.append((t, t.numpy().reshape(a.shape, order="F")))
+    hb = sum(a.size * 8 for a in (U, V, W))
+    for _ in range(2):
+        ch.set_fields_ptr(pin[0][1], pin[1][1], pin[2][1])
+        ch.step(1)
+        ch.download_async(out[0][1], out[1][1], out[2][1])
+    ch.synchronize()
+    n = max(1, args.e2e_steps)
+    t0 = time.perf_counter()
+    for _ in range(n):
+        ch.set_fields_ptr(pin[0][1], pin[1][1], pin[2][1])
+        ch.step(1)
+        ch.download_async(out[0][1], out[1][1], out[2][1])
+        ch.synchronize()
+    secs = time.perf_counter() - t0
+    return {"value": case.points * n / secs, "unit": UNIT, "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb,
+            "steps": n, "path": "chl_set_fields + chl_rk3_step + chl_download_async, pinned host U,V,W"}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=60)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--workload", default="c3_dsm")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--prof-reps", type=int, default=3)
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--ref-budget", type=float, default=120.0)
+    args = ap.parse_args()
+    if args.warmup < 3 and args.impl == "ours":
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

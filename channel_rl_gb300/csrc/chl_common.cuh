@@ -44,7 +44,8 @@ struct ChlInst {
   double *U[3], *V[3], *W[3];
   double *F1[3];                  // stage-1 RHS (kept for stages 2 and 3)
   double *Fp[3];                  // RHS for the actual pressure
-  double *nut, *S;                // eddy viscosity (Ny+2 rows), |S| (Ny+2 rows)
+  double *nut, *S;                // nu + nu_t (Ny+2 rows), |S| (Ny+2 rows)
+  double *G[9];                   // momentum face fluxes (chl_rhs.cu)
   double *q[CHL_NQ], *r[CHL_NQ];  // DSM filter ping-pong
   double *E[3];                   // edge fields (S12, S13, S23 numerators)
   double2 *spec;                  // [Ny+2][Nz][Nxh] spectra (rows 1..Ny used)

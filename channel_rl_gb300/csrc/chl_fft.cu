@@ -192,29 +192,50 @@ k_tri(ChlMap map) {
   const int mode = lb * blockDim.x + threadIdx.x;
   if (mode >= Nz * Nxh) return;
   const size_t ps = (size_t)Nz * Nxh;           // row pitch of spec and factors
-  double2* s = I.spec + ps + mode;               // row jc = 1
-  const double* fi = I.tri_inv + mode;
-  const double* fm = I.tri_m + mode;
-  const double* fc = I.tri_c + mode;
-  double2 prev = s[0];
-  const double i0 = LDG(fi);
-  prev.x *= i0; prev.y *= i0;
-  s[0] = prev;
-  for (int j = 1; j < Ny; ++j) {
-    double2 d = s[(size_t)j * ps];
-    const double iv = LDG(fi + (size_t)j * ps), m = LDG(fm + (size_t)j * ps);
-    d.x = fma(d.x, iv, -m * prev.x);
-    d.y = fma(d.y, iv, -m * prev.y);
-    s[(size_t)j * ps] = d;
-    prev = d;
+  double2* __restrict__ s = I.spec + ps + mode;  // row jc = 1
+  const double* __restrict__ fi = I.tri_inv + mode;
+  const double* __restrict__ fm = I.tri_m + mode;
+  const double* __restrict__ fc = I.tri_c + mode;
+  // The recurrence is serial in j; the loads are not.  Rows are fetched
+  // TB at a time ahead of the chain so their latency overlaps.
+  constexpr int TB = 8;
+  double2 prev = make_double2(0.0, 0.0);
+  for (int j0 = 0; j0 < Ny; j0 += TB) {
+    double2 d[TB]; double iv[TB], m[TB];
+#pragma unroll
+    for (int q = 0; q < TB; ++q) {
+      const int j = j0 + q;
+      if (j < Ny) { d[q] = s[(size_t)j * ps]; iv[q] = LDG(fi + (size_t)j * ps); m[q] = LDG(fm + (size_t)j * ps); }
+    }
+#pragma unroll
+    for (int q = 0; q < TB; ++q) {
+      const int j = j0 + q;
+      if (j < Ny) {
+        d[q].x = fma(d[q].x, iv[q], -m[q] * prev.x);   // m = 0 on the first row
+        d[q].y = fma(d[q].y, iv[q], -m[q] * prev.y);
+        prev = d[q];
+        s[(size_t)j * ps] = d[q];
+      }
+    }
   }
-  for (int j = Ny - 2; j >= 0; --j) {
-    double2 d = s[(size_t)j * ps];
-    const double c = LDG(fc + (size_t)j * ps);
-    d.x = fma(-c, prev.x, d.x);
-    d.y = fma(-c, prev.y, d.y);
-    s[(size_t)j * ps] = d;
-    prev = d;
+  // back substitution from the last row (prev holds it)
+  for (int j1 = Ny - 2; j1 >= 0; j1 -= TB) {
+    double2 d[TB]; double c[TB];
+#pragma unroll
+    for (int q = 0; q < TB; ++q) {
+      const int j = j1 - q;
+      if (j >= 0) { d[q] = s[(size_t)j * ps]; c[q] = LDG(fc + (size_t)j * ps); }
+    }
+#pragma unroll
+    for (int q = 0; q < TB; ++q) {
+      const int j = j1 - q;
+      if (j >= 0) {
+        d[q].x = fma(-c[q], prev.x, d[q].x);
+        d[q].y = fma(-c[q], prev.y, d[q].y);
+        prev = d[q];
+        s[(size_t)j * ps] = d[q];
+      }
+    }
   }
 }
 
@@ -291,11 +312,11 @@ __global__ void k_pbc(ChlMap map, int s) {
   if (t >= 2L * Nx * Nz) return;
   const int i = (int)(t % Nx), k = (int)((t / Nx) % Nz), wall = (int)(t / ((long)Nx * Nz));
   const double* V = I.V[s];
-  const double* nt = I.nut;
+  const double* nt = I.nut;      // nu + nu_t
   double bcv;
   if (wall == 0) {
     const double g = I.gb1, g2 = I.gb2;
-    const double nui = I.nu + 0.5 * (nt[cidx(I, i, 0, k)] + nt[cidx(I, i, 1, k)]);
+    const double nui = 0.5 * (nt[cidx(I, i, 0, k)] + nt[cidx(I, i, 1, k)]);
     const double dnu = (nt[cidx(I, i, 1, k)] - nt[cidx(I, i, 0, k)]) / I.dygb;
     const double v1 = V[vidx(I, i, 0, k)], v2 = V[vidx(I, i, 1, k)], v3 = V[vidx(I, i, 2, k)], v4 = V[vidx(I, i, 3, k)];
     const double dV = (-3.0 * v1 + 4.0 * v2 - v3) / 2.0 * (1.0 / g);
@@ -304,7 +325,7 @@ __global__ void k_pbc(ChlMap map, int s) {
     bcv = dnu * dV + nui * ddV;
   } else {
     const double g = I.gt1, g2 = I.gt2;
-    const double nui = I.nu + 0.5 * (nt[cidx(I, i, Ny + 1, k)] + nt[cidx(I, i, Ny, k)]);
+    const double nui = 0.5 * (nt[cidx(I, i, Ny + 1, k)] + nt[cidx(I, i, Ny, k)]);
     const double dnu = (nt[cidx(I, i, Ny + 1, k)] - nt[cidx(I, i, Ny, k)]) / I.dygt;
     const double v1 = V[vidx(I, i, Ny, k)], v2 = V[vidx(I, i, Ny - 1, k)], v3 = V[vidx(I, i, Ny - 2, k)], v4 = V[vidx(I, i, Ny - 3, k)];
     const double dV = (3.0 * v1 - 4.0 * v2 + v3) / 2.0 * (1.0 / g);

@@ -15,7 +15,8 @@
 
 // ------------------------------------------------------------ launchers (other TUs)
 extern "C" {
-void chl_launch_rhs(const ChlMap&, int, int, int, int, double, double, int, cudaStream_t);
+void chl_launch_flux(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_update(const ChlMap&, int, int, int, double, double, int, cudaStream_t);
 void chl_launch_edges(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_centre(const ChlMap&, int, int, int, cudaStream_t);
 void chl_launch_filter_y(const ChlMap&, int, int, cudaStream_t);
@@ -36,11 +37,11 @@ void chl_launch_project(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_pbc(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_pghost(const ChlMap&, int, cudaStream_t);
 void chl_launch_unpack(double*, const double*, int, int, int, int, int, int, cudaStream_t);
-void chl_launch_pack(double*, const double*, int, int, int, int, int, int, cudaStream_t);
+void chl_launch_pack(double*, const double*, int, int, int, int, int, int, double, cudaStream_t);
 void chl_launch_pack_unique(double*, const double*, int, int, int, int, int, cudaStream_t);
 void chl_launch_minabs(const ChlMap&, int, size_t, int, cudaStream_t);
 void chl_launch_dt(const ChlMap&, cudaStream_t);
-void chl_launch_massflow(const ChlMap&, cudaStream_t, int);
+void chl_launch_massflow(const ChlMap&, cudaStream_t, int, int);
 void chl_launch_shift(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_tadvance(const ChlMap&, cudaStream_t);
 void chl_launch_divmax(const ChlMap&, int, double*, cudaStream_t);
@@ -179,8 +180,14 @@ int fftx_rows(int Nx) { int cr = 1024 / Nx; return cr < 1 ? 1 : cr; }
 
 }  // namespace
 
+struct ProfRec { const char* name; int ev; };
+
 struct chl_handle {
   std::vector<Inst> in;
+  // per-launch event profiling (chl_profile_step)
+  bool prof = false;
+  std::vector<cudaEvent_t> ev;
+  std::vector<ProfRec> rec;
   ChlInst* d_inst = nullptr;
   cudaStream_t st = nullptr;
   std::string err;
@@ -198,6 +205,12 @@ struct chl_handle {
 
 #define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { \
   h->err = std::string("CUDA: ") + cudaGetErrorString(e_) + " at " #call; return CHL_E_CUDA; } } while (0)
+// Wraps one kernel launch: with profiling on, brackets it by two events.
+#define KL(name, call) do { \
+  if (h->prof && h->rec.size() * 2 + 2 <= h->ev.size()) { \
+    int e0_ = (int)h->rec.size() * 2; cudaEventRecord(h->ev[e0_], h->st); call; \
+    cudaEventRecord(h->ev[e0_ + 1], h->st); h->rec.push_back(ProfRec{name, e0_}); \
+  } else { call; } } while (0)
 #define LAUNCHED() do { cudaError_t e_ = cudaGetLastError(); if (e_ != cudaSuccess) { \
   h->err = std::string("CUDA launch: ") + cudaGetErrorString(e_); return CHL_E_CUDA; } } while (0)
 
@@ -223,6 +236,8 @@ static int upload_consts(chl_handle* h, Inst& I) {
   for (int s = 0; s < 3; ++s) o_F1[s] = A.take(8 * (s == 1 ? nv : nc));
   for (int s = 0; s < 3; ++s) o_Fp[s] = A.take(8 * (s == 1 ? nv : nc));
   size_t o_nut = A.take(8 * nc), o_S = A.take(8 * nc);
+  size_t o_G[9];
+  for (int m = 0; m < 9; ++m) o_G[m] = A.take(8 * nc);
   size_t o_q[CHL_NQ] = {}, o_r[CHL_NQ] = {};
   if (dsm) for (int m = 0; m < CHL_NQ; ++m) { o_q[m] = A.take(8 * nc); o_r[m] = A.take(8 * nc); }
   size_t o_E[3];
@@ -266,6 +281,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.tri_inv = P(o_ti); D.tri_m = P(o_tm); D.tri_c = P(o_tc);
   for (int s = 0; s < 3; ++s) { D.U[s] = P(o_U[s]); D.V[s] = P(o_V[s]); D.W[s] = P(o_W[s]); D.F1[s] = P(o_F1[s]); D.Fp[s] = P(o_Fp[s]); }
   D.nut = P(o_nut); D.S = P(o_S);
+  for (int m = 0; m < 9; ++m) D.G[m] = P(o_G[m]);
   for (int m = 0; m < CHL_NQ; ++m) { D.q[m] = dsm ? P(o_q[m]) : nullptr; D.r[m] = dsm ? P(o_r[m]) : nullptr; }
   for (int m = 0; m < 3; ++m) D.E[m] = P(o_E[m]);
   D.spec = (double2*)(base + o_spec); D.p = P(o_p); D.P = P(o_P);
@@ -347,9 +363,17 @@ static int build_maps(chl_handle* h) {
     CK(cudaMalloc(&h->d_off[m], sizeof(int) * (n + 1)));
     CK(cudaMemcpy(h->d_off[m], off.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
   }
-  int mx = 0, mz = 0, mmin = 0;
-  for (auto& I : h->in) { mx = std::max(mx, I.c.Nx); mz = std::max(mz, I.c.Nz); mmin = std::max(mmin, I.c.Nx + I.c.Ny + 1); }
-  h->smem_x = chl_smem_fftx(mx);
+  // dynamic shared memory is per launch, so it must hold the largest
+  // per-instance need: the x transform of an instance stages
+  // fftx_rows(Nx) rows of Nx, which is not monotonic in Nx
+  int mz = 0, mmin = 0;
+  size_t sx = 0;
+  for (auto& I : h->in) {
+    sx = std::max(sx, chl_smem_fftx(I.c.Nx));
+    mz = std::max(mz, I.c.Nz);
+    mmin = std::max(mmin, I.c.Nx + I.c.Ny + 1);
+  }
+  h->smem_x = sx;
   h->smem_z = chl_smem_fftz(mz);
   h->smem_min = 8 * (size_t)mmin;
   if (chl_fft_setup(h->smem_x, h->smem_z)) { h->err = "FFT shared-memory size not supported"; return CHL_E_ARG; }
@@ -360,39 +384,39 @@ static int build_maps(chl_handle* h) {
 static int enqueue_sgs(chl_handle* h, int s, bool with_wm) {
   cudaStream_t st = h->st;
   if (h->LES_model == CHL_LES_DYNAMIC) {
-    chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st);
-    chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 1, st);
-    chl_launch_filter_y(h->map(M_FULL), h->nblk[M_FULL], s, st);
-    chl_launch_filter_x(h->map(M_FULL), h->nblk[M_FULL], st);
-    chl_launch_filter_z(h->map(M_FULL), h->nblk[M_FULL], st);
-    chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], 3, st);
-    chl_launch_dsm_final(h->map(M_DSMF), h->nblk[M_DSMF], st);
+    KL("edges", chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st));
+    KL("centre_strain", chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 1, st));
+    KL("filter_y", chl_launch_filter_y(h->map(M_FULL), h->nblk[M_FULL], s, st));
+    KL("filter_x", chl_launch_filter_x(h->map(M_FULL), h->nblk[M_FULL], st));
+    KL("filter_z", chl_launch_filter_z(h->map(M_FULL), h->nblk[M_FULL], st));
+    KL("edges", chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], 3, st));
+    KL("dsm_LM_MM", chl_launch_dsm_final(h->map(M_DSMF), h->nblk[M_DSMF], st));
   } else if (h->LES_model == CHL_LES_SMAGORINSKY) {
-    chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st);
-    chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 0, st);
+    KL("edges", chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st));
+    KL("centre_strain", chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 0, st));
   }
-  chl_launch_coef(h->map(M_PT), st);
-  if (with_wm && h->wall_model == CHL_WM_EQLOG) chl_launch_eqwm(h->map(M_WALL), h->nblk[M_WALL], s, st);
-  chl_launch_nut(h->map(M_FULL), h->nblk[M_FULL], s, with_wm ? 1 : 0, st);
+  KL("nut_coef", chl_launch_coef(h->map(M_PT), st));
+  if (with_wm && h->wall_model == CHL_WM_EQLOG) KL("eq_wallmodel", chl_launch_eqwm(h->map(M_WALL), h->nblk[M_WALL], s, st));
+  KL("nut", chl_launch_nut(h->map(M_FULL), h->nblk[M_FULL], s, with_wm ? 1 : 0, st));
   LAUNCHED();
   return CHL_OK;
 }
 
 static int enqueue_projection(chl_handle* h, int s, int mode) {
   cudaStream_t st = h->st;
-  chl_launch_div_fftx(h->map(M_FFTX), h->nblk[M_FFTX], h->smem_x, s, mode, st);
-  chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 0, st);
-  chl_launch_tri(h->map(M_TRI), h->nblk[M_TRI], st);
-  chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 1, st);
-  chl_launch_fftx_inv(h->map(M_FFTX), h->nblk[M_FFTX], h->smem_x, mode == 0 ? 0 : 1, st);
-  if (mode == 0) chl_launch_project(h->map(M_PT), h->nblk[M_PT], s, st);
+  KL("div_fft_x", chl_launch_div_fftx(h->map(M_FFTX), h->nblk[M_FFTX], h->smem_x, s, mode, st));
+  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 0, st));
+  KL("tridiag", chl_launch_tri(h->map(M_TRI), h->nblk[M_TRI], st));
+  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 1, st));
+  KL("ifft_x", chl_launch_fftx_inv(h->map(M_FFTX), h->nblk[M_FFTX], h->smem_x, mode == 0 ? 0 : 1, st));
+  if (mode == 0) KL("project", chl_launch_project(h->map(M_PT), h->nblk[M_PT], s, st));
   LAUNCHED();
   return CHL_OK;
 }
 
 static int enqueue_dt(chl_handle* h) {
-  chl_launch_minabs(h->map(M_MINABS), h->nblk[M_MINABS], h->smem_min, 0, h->st);
-  chl_launch_dt(h->map(M_PT), h->st);
+  KL("dt_minabs", chl_launch_minabs(h->map(M_MINABS), h->nblk[M_MINABS], h->smem_min, 0, h->st));
+  KL("dt", chl_launch_dt(h->map(M_PT), h->st));
   LAUNCHED();
   return CHL_OK;
 }
@@ -405,16 +429,17 @@ static int enqueue_rk3(chl_handle* h) {
     if (rc) return rc;
     const double c1 = s == 0 ? 0.0 : RK_C[s][0];
     const double c2 = RK_C[s][s];
-    chl_launch_rhs(h->map(M_PT), h->nblk[M_PT], sin[s], 0, sout[s], c1, c2, s == 0 ? 0 : 1, h->st);
+    KL("rhs_flux", chl_launch_flux(h->map(M_EDGE), h->nblk[M_EDGE], sin[s], h->st));
+    KL("rhs_update", chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, sout[s], c1, c2, s == 0 ? 0 : 1, h->st));
     LAUNCHED();
     rc = enqueue_projection(h, sout[s], 0);
     if (rc) return rc;
   }
   if (h->any_mass) {
-    chl_launch_massflow(h->map(M_PT), h->st, 0);
-    chl_launch_shift(h->map(M_PT), h->nblk[M_PT], 0, h->st);
+    KL("massflow", chl_launch_massflow(h->map(M_PT), h->st, 0, 0));
+    KL("massflow_shift", chl_launch_shift(h->map(M_PT), h->nblk[M_PT], 0, h->st));
   }
-  chl_launch_tadvance(h->map(M_PT), h->st);
+  KL("t_advance", chl_launch_tadvance(h->map(M_PT), h->st));
   LAUNCHED();
   (void)RK_T;
   return CHL_OK;
@@ -510,6 +535,7 @@ int chl_destroy(chl_handle* h) {
   if (h->d_inst) cudaFree(h->d_inst);
   if (h->d_divout) cudaFree(h->d_divout);
   if (h->d_stats) cudaFree(h->d_stats);
+  for (auto& e : h->ev) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return CHL_OK;
@@ -546,8 +572,9 @@ int chl_upload(chl_handle* h, int inst, const double* U, const double* V, const 
   return finish(h);
 }
 
-static int download_field(chl_handle* h, Inst* I, double* dst, const double* src, int n1, int n2, int n3, int nrow) {
-  chl_launch_pack(I->staging, src, I->c.Nx, nrow, I->c.Nz, n1, n2, n3, h->st);
+static int download_field(chl_handle* h, Inst* I, double* dst, const double* src, int n1, int n2, int n3, int nrow,
+                          double sub = 0.0) {
+  chl_launch_pack(I->staging, src, I->c.Nx, nrow, I->c.Nz, n1, n2, n3, sub, h->st);
   LAUNCHED();
   CK(cudaMemcpyAsync(dst, I->staging, 8 * (size_t)n1 * n2 * n3, cudaMemcpyDeviceToHost, h->st));
   return finish(h);
@@ -563,7 +590,7 @@ int chl_download(chl_handle* h, int inst, double* U, double* V, double* W, doubl
   if (V && (rc = download_field(h, I, V, I->dev.V[0], c.nxg, c.ny, c.nzg, Ny + 1))) return rc;
   if (W && (rc = download_field(h, I, W, I->dev.W[0], c.nxg, c.nyg, c.nz, Ny + 2))) return rc;
   if (P && (rc = download_field(h, I, P, I->dev.P, c.nxg, c.nyg, c.nzg, Ny + 2))) return rc;
-  if (nu_t && (rc = download_field(h, I, nu_t, I->dev.nut, c.nxg, c.nyg, c.nzg, Ny + 2))) return rc;
+  if (nu_t && (rc = download_field(h, I, nu_t, I->dev.nut, c.nxg, c.nyg, c.nzg, Ny + 2, I->d.nu))) return rc;
   return CHL_OK;
 }
 
@@ -678,7 +705,8 @@ int chl_compute_rhs(chl_handle* h, int inst, double* Fu, double* Fv, double* Fw)
   int rc = check_ready(h); if (rc) return rc;
   Inst* I = get_inst(h, inst);
   if (!I) return CHL_E_ARG;
-  chl_launch_rhs(h->map(M_PT), h->nblk[M_PT], 0, 0, 0, 0.0, 0.0, 2, h->st);
+  chl_launch_flux(h->map(M_EDGE), h->nblk[M_EDGE], 0, h->st);
+  chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, 0, 0.0, 0.0, 2, h->st);
   LAUNCHED();
   const Consts& c = I->c;
   const int Nx = c.Nx, Ny = c.Ny, Nz = c.Nz;
@@ -706,7 +734,7 @@ int chl_compute_dPx_for_constant_mass_flow(chl_handle* h, int inst, double* dPdx
   double s[CHL_S_NSCAL];
   CK(cudaMemcpyAsync(s, I->dev.scal, sizeof(s), cudaMemcpyDeviceToHost, h->st));
   if ((rc = finish(h))) return rc;
-  chl_launch_massflow(h->map(M_PT), h->st, 0);
+  chl_launch_massflow(h->map(M_PT), h->st, 0, 1);
   LAUNCHED();
   double s2[CHL_S_NSCAL];
   CK(cudaMemcpyAsync(s2, I->dev.scal, sizeof(s2), cudaMemcpyDeviceToHost, h->st));
@@ -720,7 +748,8 @@ int chl_compute_dPx_for_constant_mass_flow(chl_handle* h, int inst, double* dPdx
 int chl_compute_pressure(chl_handle* h) {
   int rc = check_ready(h); if (rc) return rc;
   chl_launch_pbc(h->map(M_WALL), h->nblk[M_WALL], 0, h->st);
-  chl_launch_rhs(h->map(M_PT), h->nblk[M_PT], 0, 0, 0, 0.0, 0.0, 2, h->st);
+  chl_launch_flux(h->map(M_EDGE), h->nblk[M_EDGE], 0, h->st);
+  chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, 0, 0.0, 0.0, 2, h->st);
   LAUNCHED();
   rc = enqueue_projection(h, 0, 1); if (rc) return rc;
   chl_launch_pghost(h->map(M_PLANE), h->nblk[M_PLANE], h->st);
@@ -739,6 +768,107 @@ int chl_check_divergence(chl_handle* h, int inst, double* max_div, double* max_a
   if (max_div) *max_div = r[0];
   if (max_abs_div) *max_abs_div = r[1];
   return CHL_OK;
+}
+
+int chl_set_fields(chl_handle* h, int inst, const double* U, const double* V, const double* W) {
+  Inst* I = get_inst(h, inst);
+  if (!I) return CHL_E_ARG;
+  if (!I->uploaded) { h->err = "chl_set_fields before chl_upload"; return CHL_E_STATE; }
+  if (!U || !V || !W) { h->err = "null field"; return CHL_E_ARG; }
+  const Consts& c = I->c;
+  struct { const double* src; double* dst; int n1, n2, n3, nrow, kind; } f[3] = {
+      {U, I->dev.U[0], c.nx, c.nyg, c.nzg, c.Ny + 2, 0},
+      {V, I->dev.V[0], c.nxg, c.ny, c.nzg, c.Ny + 1, 1},
+      {W, I->dev.W[0], c.nxg, c.nyg, c.nz, c.Ny + 2, 0}};
+  for (auto& q : f) {
+    CK(cudaMemcpyAsync(I->staging, q.src, 8 * (size_t)q.n1 * q.n2 * q.n3, cudaMemcpyHostToDevice, h->st));
+    chl_launch_unpack(q.dst, I->staging, c.Nx, q.nrow, c.Nz, q.n1, q.n2, q.kind, h->st);
+    LAUNCHED();
+  }
+  return CHL_OK;   // stream-ordered; no synchronisation
+}
+
+int chl_download_async(chl_handle* h, int inst, double* U, double* V, double* W) {
+  Inst* I = get_inst(h, inst);
+  if (!I) return CHL_E_ARG;
+  const Consts& c = I->c;
+  struct { double* dst; const double* src; int n1, n2, n3, nrow; } f[3] = {
+      {U, I->dev.U[0], c.nx, c.nyg, c.nzg, c.Ny + 2}, {V, I->dev.V[0], c.nxg, c.ny, c.nzg, c.Ny + 1},
+      {W, I->dev.W[0], c.nxg, c.nyg, c.nz, c.Ny + 2}};
+  for (auto& q : f) {
+    if (!q.dst) continue;
+    // one staging buffer: each copy must leave it before the next pack
+    chl_launch_pack(I->staging, q.src, c.Nx, q.nrow, c.Nz, q.n1, q.n2, q.n3, 0.0, h->st);
+    LAUNCHED();
+    CK(cudaMemcpyAsync(q.dst, I->staging, 8 * (size_t)q.n1 * q.n2 * q.n3, cudaMemcpyDeviceToHost, h->st));
+  }
+  return CHL_OK;
+}
+
+int chl_time_steps(chl_handle* h, int nsteps, double* ms) {
+  if (!ms) return CHL_E_ARG;
+  int rc = check_ready(h); if (rc) return rc;
+  if (!h->gexec) { if ((rc = chl_rk3_step(h, 0))) return rc; }
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a)); CK(cudaEventCreate(&b));
+  CK(cudaStreamSynchronize(h->st));
+  CK(cudaEventRecord(a, h->st));
+  for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(h->gexec, h->st));
+  CK(cudaEventRecord(b, h->st));
+  CK(cudaEventSynchronize(b));
+  float f = 0.f;
+  CK(cudaEventElapsedTime(&f, a, b));
+  cudaEventDestroy(a); cudaEventDestroy(b);
+  *ms = f;
+  return CHL_OK;
+}
+
+int chl_graph_kernel_count(chl_handle* h, int* count) {
+  if (!h || !count) return CHL_E_ARG;
+  int rc = check_ready(h); if (rc) return rc;
+  if (!h->gexec) { if ((rc = chl_rk3_step(h, 0))) return rc; }
+  size_t n = 0;
+  CK(cudaGraphGetNodes(h->graph, nullptr, &n));
+  std::vector<cudaGraphNode_t> nodes(n);
+  CK(cudaGraphGetNodes(h->graph, nodes.data(), &n));
+  int k = 0;
+  for (auto& nd : nodes) { cudaGraphNodeType t; CK(cudaGraphNodeGetType(nd, &t)); if (t == cudaGraphNodeTypeKernel) ++k; }
+  *count = k;
+  return CHL_OK;
+}
+
+int chl_profile_step(chl_handle* h, int reps, int maxk, char* names, double* ms_per_step, int* launches_per_step) {
+  if (!h || reps <= 0 || maxk <= 0 || !names || !ms_per_step || !launches_per_step) return CHL_E_ARG;
+  int rc = check_ready(h); if (rc) return rc;
+  if (h->ev.empty()) {
+    h->ev.resize(512);
+    for (auto& e : h->ev) CK(cudaEventCreate(&e));
+  }
+  std::vector<std::string> keys; std::vector<double> tot; std::vector<int> cnt;
+  for (int r = 0; r < reps; ++r) {
+    h->rec.clear();
+    h->prof = true;
+    rc = enqueue_dt(h);
+    if (!rc) rc = enqueue_rk3(h);
+    h->prof = false;
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(h->st));
+    for (auto& q : h->rec) {
+      float f = 0.f;
+      CK(cudaEventElapsedTime(&f, h->ev[q.ev], h->ev[q.ev + 1]));
+      size_t i = 0;
+      for (; i < keys.size(); ++i) if (keys[i] == q.name) break;
+      if (i == keys.size()) { keys.push_back(q.name); tot.push_back(0.0); cnt.push_back(0); }
+      tot[i] += f; if (r == 0) cnt[i] += 1;
+    }
+  }
+  const int nk = std::min((int)keys.size(), maxk);
+  for (int i = 0; i < nk; ++i) {
+    std::strncpy(names + 32 * i, keys[i].c_str(), 31); names[32 * i + 31] = 0;
+    ms_per_step[i] = tot[i] / reps;
+    launches_per_step[i] = cnt[i];
+  }
+  return nk;
 }
 
 static int run_stats(chl_handle* h, int inst, std::vector<double>& buf) {

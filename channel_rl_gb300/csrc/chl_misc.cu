@@ -24,14 +24,15 @@ __global__ void k_unpack(double* dst, const double* __restrict__ F, int Nx, int 
 // device field -> Fortran array with every ghost filled (periodic copies in
 // x and z, stored ghost/wall rows in y)
 __global__ void k_pack(double* __restrict__ F, const double* __restrict__ src, int Nx, int nrow, int Nz,
-                       int n1, int n2, int n3) {
+                       int n1, int n2, int n3, double sub) {
   long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)n1 * n2 * n3) return;
   const int i1 = (int)(t % n1), j1 = (int)((t / n1) % n2), k1 = (int)(t / ((long)n1 * n2));
   int i = (i1 - 1) % Nx; if (i < 0) i += Nx;
   int k = (k1 - 1) % Nz; if (k < 0) k += Nz;
   const int j = j1 < nrow ? j1 : nrow - 1;
-  F[t] = src[(size_t)i + (size_t)Nx * ((size_t)j + (size_t)nrow * k)];
+  const double v = src[(size_t)i + (size_t)Nx * ((size_t)j + (size_t)nrow * k)];
+  F[t] = sub == 0.0 ? v : v - sub;     // nu_t is stored as nu + nu_t
 }
 
 // device field (rows jlo..jhi) -> dense unique-point array (Nx, jhi-jlo+1, Nz)
@@ -48,9 +49,10 @@ void chl_launch_unpack(double* dst, const double* F, int Nx, int nrow, int Nz, i
   long n = (long)Nx * nrow * Nz;
   k_unpack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dst, F, Nx, nrow, Nz, n1, n2, kind);
 }
-void chl_launch_pack(double* F, const double* src, int Nx, int nrow, int Nz, int n1, int n2, int n3, cudaStream_t st) {
+void chl_launch_pack(double* F, const double* src, int Nx, int nrow, int Nz, int n1, int n2, int n3, double sub,
+                     cudaStream_t st) {
   long n = (long)n1 * n2 * n3;
-  k_pack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, src, Nx, nrow, Nz, n1, n2, n3);
+  k_pack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, src, Nx, nrow, Nz, n1, n2, n3, sub);
 }
 void chl_launch_pack_unique(double* F, const double* src, int Nx, int nrow, int Nz, int jlo, int nj, cudaStream_t st) {
   long n = (long)Nx * nj * Nz;
@@ -143,9 +145,13 @@ __global__ void k_dt(ChlMap map) {
 // compute_dPx_for_constant_mass_flow (mass_flow.f90:360-413) over the unique
 // x-z points of rows j_f = 3 and nyg-2, then U += dPdx on the interior
 // (time_integration.f90:89-94); one block per instance for the sum.
-__global__ void k_massflow(ChlMap map, int s) {
+__global__ void k_massflow(ChlMap map, int s, int force) {
   const ChlInst& I = map.inst[blockIdx.x];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  if (!I.x_mass_cte && !force) {                 // pressure-gradient forcing: no shift
+    if (threadIdx.x == 0) I.scal[CHL_S_SHIFT] = 0.0;
+    return;
+  }
   const double* U = I.U[s];
   double acc = 0.0;
   for (int w = threadIdx.x; w < Nx * Nz; w += blockDim.x) {
@@ -162,7 +168,7 @@ __global__ void k_massflow(ChlMap map, int s) {
   if (threadIdx.x == 0) {
     const double d = I.scal[CHL_S_Q0] - red[0] / (double)(Nx * Nz);
     I.scal[CHL_S_SHIFT] = d;
-    I.scal[CHL_S_DPDX] = 0.0;
+    if (!force) I.scal[CHL_S_DPDX] = 0.0;   // dPdx = 0 after the shift (time_integration.f90:92)
   }
 }
 
@@ -174,6 +180,7 @@ k_shift(ChlMap map, int s) {
   long t = (long)lb * blockDim.x + threadIdx.x;
   if (t >= (long)Nx * Ny * Nz) return;
   const int i = (int)(t % Nx), jc = 1 + (int)((t / Nx) % Ny), k = (int)(t / ((long)Nx * Ny));
+  if (!I.x_mass_cte) return;
   double* U = I.U[s];
   const double d = I.scal[CHL_S_SHIFT];
   const double un = U[cidx(I, i, jc, k)] + d;
@@ -243,7 +250,7 @@ void chl_launch_minabs(const ChlMap& m, int nb, size_t smem, int s, cudaStream_t
   k_minabs<<<nb, 256, smem, st>>>(m, s);
 }
 void chl_launch_dt(const ChlMap& m, cudaStream_t st) { k_dt<<<m.n, 128, 0, st>>>(m); }
-void chl_launch_massflow(const ChlMap& m, cudaStream_t st, int s) { k_massflow<<<m.n, 256, 0, st>>>(m, s); }
+void chl_launch_massflow(const ChlMap& m, cudaStream_t st, int s, int force) { k_massflow<<<m.n, 256, 0, st>>>(m, s, force); }
 void chl_launch_shift(const ChlMap& m, int nb, int s, cudaStream_t st) { k_shift<<<nb, 256, 0, st>>>(m, s); }
 void chl_launch_tadvance(const ChlMap& m, cudaStream_t st) { k_tadvance<<<m.n, 32, 0, st>>>(m); }
 void chl_launch_divmax(const ChlMap& m, int s, double* out, cudaStream_t st) { k_divmax<<<m.n, 256, 0, st>>>(m, s, out); }

@@ -1,21 +1,111 @@
 // Momentum right-hand side and Runge-Kutta stage update.
 //
-// Restates compute_rhs_u/v/w (equations.f90:24-468) with the reference's
-// interpolations (interpolation.f90:24-105: plain averages in x,z, weighted
-// average weight_y_0/1 in y) and fuses the RK3 stage update of
-// compute_time_step_RK3 (time_integration.f90:42-44, 59-61, 76-81) and the
-// Dirichlet ghost rows of apply_Dirichlet_bc_y (boundary_conditions.f90:239-254).
-// Divisions by grid spacings are multiplications by precomputed reciprocals.
+// Restates compute_rhs_u/v/w (equations.f90:24-468) - advection by the
+// reference's interpolations (interpolation.f90:24-105: plain averages in x
+// and z, weight_y_0/1 averages in y) plus variable-viscosity diffusion - and
+// the stage update of compute_time_step_RK3 (time_integration.f90:42-81)
+// with the Dirichlet ghost rows of apply_Dirichlet_bc_y
+// (boundary_conditions.f90:239-254).
+//
+// The reference sums each derivative's advective and viscous part per
+// component; here the same terms are grouped by the face they live on
+// (flux form), so every face value is computed once:
+//   * cell centres     : the diagonal fluxes of u (x), v (y), w (z);
+//   * xy edges (x-face, y-face, z-centre): uv and the edge viscosity, shared
+//                        by the y flux of u and the x flux of v;
+//   * xz edges (x-face, y-centre, z-face): uw, shared by u (z) and w (x);
+//   * yz edges (x-centre, y-face, z-face): vw, shared by v (z) and w (y).
+// The edge viscosities are exactly the reference's averages (nu_y1/nu_y2 of
+// compute_rhs_u equal nu_x1/nu_x2 of compute_rhs_v at the same edge, etc.).
+// I.nut holds nu + nu_t, so no per-use "nu +" is needed.  The first kernel
+// writes the nine face fluxes, the second takes their divergence and
+// updates the stage: the FP64 pipe, not HBM, bounds this code, and each
+// flux is computed once instead of twice.
 #include "chl_common.cuh"
 
+// flux fields: centre-like (rows 1..Ny): 0 GUx, 1 GVy, 2 GWz, 3 GUz, 4 GWx;
+// V-like (rows 0..Ny): 5 GUy, 6 GVx, 7 GVz, 8 GWy
+enum { G_UX = 0, G_VY, G_WZ, G_UZ, G_WX, G_UY, G_VX, G_VZ, G_WY };
+
+__global__ void __launch_bounds__(256)
+k_flux(ChlMap map, int sin) {
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t >= (long)Nx * (Ny + 1) * Nz) return;
+  const int i = (int)(t % Nx);
+  const int j = (int)((t / Nx) % (Ny + 1));
+  const int k = (int)(t / ((long)Nx * (Ny + 1)));
+  const int im = wrap(i - 1, Nx), ip = wrap(i + 1, Nx);
+  const int km = wrap(k - 1, Nz), kp = wrap(k + 1, Nz);
+  const double* __restrict__ U = I.U[sin];
+  const double* __restrict__ V = I.V[sin];
+  const double* __restrict__ W = I.W[sin];
+  const double* __restrict__ nt = I.nut;   // nu + nu_t
+  double* const* G = I.G;
+#define UC(ii, jj, kk) LDG(U + cidx(I, ii, jj, kk))
+#define WC(ii, jj, kk) LDG(W + cidx(I, ii, jj, kk))
+#define VV(ii, jj, kk) LDG(V + vidx(I, ii, jj, kk))
+#define NT(ii, jj, kk) LDG(nt + cidx(I, ii, jj, kk))
+  const double rxf = LDG(I.rdxf + i), rzf = LDG(I.rdzf + k), ryf = LDG(I.rdyf + j);
+  const double hw0 = 0.5 * LDG(I.w0 + j), hw1 = 0.5 * LDG(I.w1 + j);
+  // row j and j+1 values shared by the xy and yz edges (y-face jv = j)
+  const double u_a = UC(i, j, k), u_b = UC(i, j + 1, k);
+  const double w_a = WC(i, j, k), w_b = WC(i, j + 1, k);
+  const double v_0 = VV(i, j, k);
+  const double n_a = NT(i, j, k), n_b = NT(i, j + 1, k);
+  {  // xy edge (x-face i, y-face j, z-centre k): uv, nu -> GUy, GVx
+    const double v_p = VV(ip, j, k);
+    const double uy = fma(hw0, u_a, hw1 * u_b);          // 0.5 * u on the y-face
+    const double uv = uy * (v_0 + v_p);                  // u * v (v = 0.5 (v0+vp))
+    const double nxy = fma(hw0, n_a + NT(ip, j, k), hw1 * (n_b + NT(ip, j + 1, k)));
+    const size_t e = vidx(I, i, j, k);
+    G[G_UY][e] = fma(nxy, (u_b - u_a) * ryf, -uv);
+    G[G_VX][e] = fma(nxy, (v_p - v_0) * rxf, -uv);
+  }
+  {  // yz edge (x-centre i, y-face j, z-face k): vw, nu -> GVz, GWy
+    const double v_z = VV(i, j, kp);
+    const double wy = fma(hw0, w_a, hw1 * w_b);
+    const double vw = wy * (v_0 + v_z);
+    const double nyz = fma(hw0, n_a + NT(i, j, kp), hw1 * (n_b + NT(i, j + 1, kp)));
+    const size_t e = vidx(I, i, j, k);
+    G[G_VZ][e] = fma(nyz, (v_z - v_0) * rzf, -vw);
+    G[G_WY][e] = fma(nyz, (w_b - w_a) * ryf, -vw);
+  }
+  if (j >= 1 && j <= Ny) {
+    const int jc = j;
+    const size_t c = cidx(I, i, jc, k);
+    {  // cell centre: diagonal fluxes
+      const double um = UC(im, jc, k), vm = VV(i, jc - 1, k), wm = WC(i, jc, km);
+      const double su = um + u_a, sv = vm + v_0, sw = wm + w_a;
+      G[G_UX][c] = fma(-0.25 * su, su, n_a * LDG(I.rdxc + i) * (u_a - um));
+      G[G_VY][c] = fma(-0.25 * sv, sv, n_a * LDG(I.rdyc + jc) * (v_0 - vm));
+      G[G_WZ][c] = fma(-0.25 * sw, sw, n_a * LDG(I.rdzc + k) * (w_a - wm));
+    }
+    {  // xz edge (x-face i, y-centre jc, z-face k): uw, nu -> GUz, GWx
+      const double u_z = UC(i, jc, kp), w_p = WC(ip, jc, k);
+      const double uw = 0.25 * (u_a + u_z) * (w_a + w_p);
+      const double nxz = 0.25 * ((n_a + NT(ip, jc, k)) + (NT(i, jc, kp) + NT(ip, jc, kp)));
+      G[G_UZ][c] = fma(nxz, (u_z - u_a) * rzf, -uw);
+      G[G_WX][c] = fma(nxz, (w_p - w_a) * rxf, -uw);
+    }
+  }
+#undef UC
+#undef WC
+#undef VV
+#undef NT
+  (void)km; (void)im;
+}
+
 struct RhsArgs {
-  int sin, sbase, sout;   // velocity sets: RHS input, stage base (U^n), output
+  int sbase, sout;        // velocity sets: stage base (U^n), output
   double c1, c2;          // out = base + dt*(c1*F1 + c2*F)
-  int mode;               // 0: stage 1 (store F1), 1: stages 2/3, 2: pressure RHS only
+  int mode;               // 0: stage 1 (store F1), 1: stages 2/3, 2: actual-pressure RHS only
 };
 
 __global__ void __launch_bounds__(256)
-k_rhs(ChlMap map, RhsArgs a) {
+k_rhs_update(ChlMap map, RhsArgs a) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -26,144 +116,32 @@ k_rhs(ChlMap map, RhsArgs a) {
   const int k = (int)(t / ((long)Nx * Ny));
   const int im = wrap(i - 1, Nx), ip = wrap(i + 1, Nx);
   const int km = wrap(k - 1, Nz), kp = wrap(k + 1, Nz);
-
-  const double* __restrict__ U = I.U[a.sin];
-  const double* __restrict__ V = I.V[a.sin];
-  const double* __restrict__ W = I.W[a.sin];
-  const double* __restrict__ nt = I.nut;
-  const double nu = I.nu;
-  const double* rdxc = I.rdxc; const double* rdxf = I.rdxf;
-  const double* rdzc = I.rdzc; const double* rdzf = I.rdzf;
-  const double* rdyc = I.rdyc; const double* rdyf = I.rdyf;
-  const double* w0 = I.w0; const double* w1 = I.w1;
-
-#define Uc(ii, jj, kk) LDG(U + cidx(I, ii, jj, kk))
-#define Wc(ii, jj, kk) LDG(W + cidx(I, ii, jj, kk))
-#define Vv(ii, jj, kk) LDG(V + vidx(I, ii, jj, kk))
-#define NT(ii, jj, kk) LDG(nt + cidx(I, ii, jj, kk))
-
-  const double rxc = LDG(rdxc + i), rxcp = LDG(rdxc + i + 1);
-  const double rxf = LDG(rdxf + i), rxfm = LDG(rdxf + i - 1);
-  const double rzc = LDG(rdzc + k), rzcp = LDG(rdzc + k + 1);
-  const double rzf = LDG(rdzf + k), rzfm = LDG(rdzf + k - 1);
-
-  // ------------------------------------------------------------------ u
-  double Fu, Fv = 0.0, Fw;
-  {
-    const double u0 = Uc(i, jc, k), uxm = Uc(im, jc, k), uxp = Uc(ip, jc, k);
-    const double uym = Uc(i, jc - 1, k), uyp = Uc(i, jc + 1, k);
-    const double uzm = Uc(i, jc, km), uzp = Uc(i, jc, kp);
-    // -d(uu)/dx: centre values 0.5(U(c-1)+U(c)) at centres i and i+1
-    const double ca = 0.5 * (uxm + u0), cb = 0.5 * (u0 + uxp);
-    double f = -(cb * cb - ca * ca) * rxf;
-    // -d(uv)/dy: u on faces jc-1, jc times v on x-face i
-    const double w0a = LDG(w0 + jc - 1), w1a = LDG(w1 + jc - 1);
-    const double w0b = LDG(w0 + jc), w1b = LDG(w1 + jc);
-    const double uyl = w0a * uym + w1a * u0, uyh = w0b * u0 + w1b * uyp;
-    const double vxl = 0.5 * (Vv(i, jc - 1, k) + Vv(ip, jc - 1, k));
-    const double vxh = 0.5 * (Vv(i, jc, k) + Vv(ip, jc, k));
-    f += -(uyh * vxh - uyl * vxl) * LDG(rdyc + jc);
-    // -d(uw)/dz
-    const double uzl = 0.5 * (uzm + u0), uzh = 0.5 * (u0 + uzp);
-    const double wxl = 0.5 * (Wc(i, jc, km) + Wc(ip, jc, km));
-    const double wxh = 0.5 * (Wc(i, jc, k) + Wc(ip, jc, k));
-    f += -(uzh * wxh - uzl * wxl) * rzc;
-    // viscous
-    const double n00 = NT(i, jc, k), n10 = NT(ip, jc, k);
-    const double nux1 = nu + n00, nux2 = nu + n10;
-    double vis = rxf * (nux2 * rxcp * (uxp - u0) - nux1 * rxc * (u0 - uxm));
-    const double nym0 = NT(i, jc - 1, k), nym1 = NT(ip, jc - 1, k);
-    const double nyp0 = NT(i, jc + 1, k), nyp1 = NT(ip, jc + 1, k);
-    const double nuy1 = nu + 0.5 * (w0a * nym0 + w1a * n00 + w0a * nym1 + w1a * n10);
-    const double nuy2 = nu + 0.5 * (w0b * n00 + w1b * nyp0 + w0b * n10 + w1b * nyp1);
-    const double t2l = (u0 - uym) * LDG(rdyf + jc - 1), t2h = (uyp - u0) * LDG(rdyf + jc);
-    vis += LDG(rdyc + jc) * (nuy2 * t2h - nuy1 * t2l);
-    const double nuz1 = nu + 0.25 * (n00 + NT(i, jc, km) + n10 + NT(ip, jc, km));
-    const double nuz2 = nu + 0.25 * (n00 + NT(i, jc, kp) + n10 + NT(ip, jc, kp));
-    vis += rzc * (nuz2 * rzf * (uzp - u0) - nuz1 * rzfm * (u0 - uzm));
-    Fu = f + vis + I.scal[CHL_S_DPDX];
-  }
-  // ------------------------------------------------------------------ v (face row jv = jc)
-  const int jv = jc;
-  const bool hasv = jv <= Ny - 1;
+  const double* const* G = I.G;
+  const double rxc = LDG(I.rdxc + i), rxf = LDG(I.rdxf + i);
+  const double rzc = LDG(I.rdzc + k), rzf = LDG(I.rdzf + k);
+  const double ryc = LDG(I.rdyc + jc);
+  const size_t c = cidx(I, i, jc, k);
+  const size_t e = vidx(I, i, jc, k), em = vidx(I, i, jc - 1, k);
+  // u at (x-face i, row jc, z-centre k)
+  double Fu = (LDG(G[G_UX] + cidx(I, ip, jc, k)) - LDG(G[G_UX] + c)) * rxf;
+  Fu = fma(LDG(G[G_UY] + e) - LDG(G[G_UY] + em), ryc, Fu);
+  Fu = fma(LDG(G[G_UZ] + c) - LDG(G[G_UZ] + cidx(I, i, jc, km)), rzc, Fu);
+  Fu += I.scal[CHL_S_DPDX];
+  // w at (x-centre i, row jc, z-face k)
+  double Fw = (LDG(G[G_WX] + c) - LDG(G[G_WX] + cidx(I, im, jc, k))) * rxc;
+  Fw = fma(LDG(G[G_WY] + e) - LDG(G[G_WY] + em), ryc, Fw);
+  Fw = fma(LDG(G[G_WZ] + cidx(I, i, jc, kp)) - LDG(G[G_WZ] + c), rzf, Fw);
+  // v at (x-centre i, y-face jv = jc, z-centre k)
+  const bool hasv = jc <= Ny - 1;
+  double Fv = 0.0;
   if (hasv) {
-    const double v0 = Vv(i, jv, k), vxm = Vv(im, jv, k), vxp = Vv(ip, jv, k);
-    const double vym = Vv(i, jv - 1, k), vyp = Vv(i, jv + 1, k);
-    const double vzm = Vv(i, jv, km), vzp = Vv(i, jv, kp);
-    // -d(vv)/dy: centre values at rows jv and jv+1
-    const double ca = 0.5 * (vym + v0), cb = 0.5 * (v0 + vyp);
-    double f = -(cb * cb - ca * ca) * LDG(rdyf + jv);
-    // -d(uv)/dx: u on y-face jv at x-faces i-1, i; v on those x-faces
-    const double w0j = LDG(w0 + jv), w1j = LDG(w1 + jv);
-    const double uyl = w0j * Uc(im, jv, k) + w1j * Uc(im, jv + 1, k);
-    const double uyh = w0j * Uc(i, jv, k) + w1j * Uc(i, jv + 1, k);
-    const double vxl = 0.5 * (vxm + v0), vxh = 0.5 * (v0 + vxp);
-    f += -(uyh * vxh - uyl * vxl) * rxc;
-    // -d(vw)/dz
-    const double vzl = 0.5 * (vzm + v0), vzh = 0.5 * (v0 + vzp);
-    const double wyl = w0j * Wc(i, jv, km) + w1j * Wc(i, jv + 1, km);
-    const double wyh = w0j * Wc(i, jv, k) + w1j * Wc(i, jv + 1, k);
-    f += -(vzh * wyh - vzl * wyl) * rzc;
-    // viscous
-    const double a0 = NT(i, jv, k), a1 = NT(i, jv + 1, k);
-    const double bm0 = NT(im, jv, k), bm1 = NT(im, jv + 1, k);
-    const double bp0 = NT(ip, jv, k), bp1 = NT(ip, jv + 1, k);
-    const double nux1 = nu + 0.5 * (w0j * bm0 + w1j * bm1 + w0j * a0 + w1j * a1);
-    const double nux2 = nu + 0.5 * (w0j * a0 + w1j * a1 + w0j * bp0 + w1j * bp1);
-    double vis = rxc * (nux2 * rxf * (vxp - v0) - nux1 * rxfm * (v0 - vxm));
-    vis += LDG(rdyf + jv) * ((nu + a1) * LDG(rdyc + jv + 1) * (vyp - v0) - (nu + a0) * LDG(rdyc + jv) * (v0 - vym));
-    const double cm0 = NT(i, jv, km), cm1 = NT(i, jv + 1, km);
-    const double cp0 = NT(i, jv, kp), cp1 = NT(i, jv + 1, kp);
-    const double nuz1 = nu + 0.5 * (w0j * cm0 + w1j * cm1 + w0j * a0 + w1j * a1);
-    const double nuz2 = nu + 0.5 * (w0j * a0 + w1j * a1 + w0j * cp0 + w1j * cp1);
-    vis += rzc * (nuz2 * rzf * (vzp - v0) - nuz1 * rzfm * (v0 - vzm));
-    Fv = f + vis;
+    Fv = (LDG(G[G_VX] + e) - LDG(G[G_VX] + vidx(I, im, jc, k))) * rxc;
+    Fv = fma(LDG(G[G_VY] + cidx(I, i, jc + 1, k)) - LDG(G[G_VY] + c), LDG(I.rdyf + jc), Fv);
+    Fv = fma(LDG(G[G_VZ] + e) - LDG(G[G_VZ] + vidx(I, i, jc, km)), rzc, Fv);
   }
-  // ------------------------------------------------------------------ w (face k, row jc)
-  {
-    const double w_0 = Wc(i, jc, k), wxm = Wc(im, jc, k), wxp = Wc(ip, jc, k);
-    const double wym = Wc(i, jc - 1, k), wyp = Wc(i, jc + 1, k);
-    const double wzm = Wc(i, jc, km), wzp = Wc(i, jc, kp);
-    // -d(ww)/dz: centre values at z-centres k and k+1
-    const double ca = 0.5 * (wzm + w_0), cb = 0.5 * (w_0 + wzp);
-    double f = -(cb * cb - ca * ca) * rzf;
-    // -d(uw)/dx
-    const double uzl = 0.5 * (Uc(im, jc, k) + Uc(im, jc, kp));
-    const double uzh = 0.5 * (Uc(i, jc, k) + Uc(i, jc, kp));
-    const double wxl = 0.5 * (wxm + w_0), wxh = 0.5 * (w_0 + wxp);
-    f += -(uzh * wxh - uzl * wxl) * rxc;
-    // -d(vw)/dy
-    const double w0a = LDG(w0 + jc - 1), w1a = LDG(w1 + jc - 1);
-    const double w0b = LDG(w0 + jc), w1b = LDG(w1 + jc);
-    const double vzl = 0.5 * (Vv(i, jc - 1, k) + Vv(i, jc - 1, kp));
-    const double vzh = 0.5 * (Vv(i, jc, k) + Vv(i, jc, kp));
-    const double wyl = w0a * wym + w1a * w_0, wyh = w0b * w_0 + w1b * wyp;
-    f += -(vzh * wyh - vzl * wyl) * LDG(rdyc + jc);
-    // viscous
-    const double n0 = NT(i, jc, k), n1 = NT(i, jc, kp);
-    const double nm0 = NT(im, jc, k), nm1 = NT(im, jc, kp);
-    const double np0 = NT(ip, jc, k), np1 = NT(ip, jc, kp);
-    const double nux1 = nu + 0.25 * (n0 + n1 + nm0 + nm1);
-    const double nux2 = nu + 0.25 * (n0 + n1 + np0 + np1);
-    double vis = rxc * (nux2 * rxf * (wxp - w_0) - nux1 * rxfm * (w_0 - wxm));
-    const double ym0 = NT(i, jc - 1, k), ym1 = NT(i, jc - 1, kp);
-    const double yp0 = NT(i, jc + 1, k), yp1 = NT(i, jc + 1, kp);
-    const double nuy1 = nu + 0.5 * (w0a * ym0 + w1a * n0 + w0a * ym1 + w1a * n1);
-    const double nuy2 = nu + 0.5 * (w0b * n0 + w1b * yp0 + w0b * n1 + w1b * yp1);
-    const double t2l = (w_0 - wym) * LDG(rdyf + jc - 1), t2h = (wyp - w_0) * LDG(rdyf + jc);
-    vis += LDG(rdyc + jc) * (nuy2 * t2h - nuy1 * t2l);
-    vis += rzf * ((nu + n1) * rzcp * (wzp - w_0) - (nu + n0) * rzc * (w_0 - wzm));
-    Fw = f + vis;
-  }
-#undef Uc
-#undef Wc
-#undef Vv
-#undef NT
-  const size_t ci = cidx(I, i, jc, k);
-  const size_t vi = vidx(I, i, jv, k);
   if (a.mode == 2) {           // actual-pressure RHS: keep F only
-    I.Fp[0][ci] = Fu; I.Fp[2][ci] = Fw;
-    if (hasv) I.Fp[1][vi] = Fv;
+    I.Fp[0][c] = Fu; I.Fp[2][c] = Fw;
+    if (hasv) I.Fp[1][e] = Fv;
     return;
   }
   const double dt = I.scal[CHL_S_DT];
@@ -171,24 +149,29 @@ k_rhs(ChlMap map, RhsArgs a) {
   const double* Ub = I.U[a.sbase]; const double* Vb = I.V[a.sbase]; const double* Wb = I.W[a.sbase];
   double un, vn = 0.0, wn;
   if (a.mode == 0) {
-    I.F1[0][ci] = Fu; I.F1[2][ci] = Fw;
-    if (hasv) I.F1[1][vi] = Fv;
-    un = Ub[ci] + dt * (a.c2 * Fu);
-    wn = Wb[ci] + dt * (a.c2 * Fw);
-    if (hasv) vn = Vb[vi] + dt * (a.c2 * Fv);
+    I.F1[0][c] = Fu; I.F1[2][c] = Fw;
+    if (hasv) I.F1[1][e] = Fv;
+    un = Ub[c] + dt * (a.c2 * Fu);
+    wn = Wb[c] + dt * (a.c2 * Fw);
+    if (hasv) vn = Vb[e] + dt * (a.c2 * Fv);
   } else {
-    un = Ub[ci] + dt * (a.c1 * I.F1[0][ci] + a.c2 * Fu);
-    wn = Wb[ci] + dt * (a.c1 * I.F1[2][ci] + a.c2 * Fw);
-    if (hasv) vn = Vb[vi] + dt * (a.c1 * I.F1[1][vi] + a.c2 * Fv);
+    un = Ub[c] + dt * fma(a.c1, I.F1[0][c], a.c2 * Fu);
+    wn = Wb[c] + dt * fma(a.c1, I.F1[2][c], a.c2 * Fw);
+    if (hasv) vn = Vb[e] + dt * fma(a.c1, I.F1[1][e], a.c2 * Fv);
   }
-  Uo[ci] = un; Wo[ci] = wn;
-  if (hasv) Vo[vi] = vn;
+  Uo[c] = un; Wo[c] = wn;
+  if (hasv) Vo[e] = vn;
   if (jc == 1) { Uo[cidx(I, i, 0, k)] = -un; Wo[cidx(I, i, 0, k)] = -wn; }
   if (jc == Ny) { Uo[cidx(I, i, Ny + 1, k)] = -un; Wo[cidx(I, i, Ny + 1, k)] = -wn; }
 }
 
-extern "C" void chl_launch_rhs(const ChlMap& map, int nblocks, int sin, int sbase, int sout,
-                               double c1, double c2, int mode, cudaStream_t st) {
-  RhsArgs a{sin, sbase, sout, c1, c2, mode};
-  k_rhs<<<nblocks, 256, 0, st>>>(map, a);
+extern "C" {
+void chl_launch_flux(const ChlMap& map, int nb_edge, int sin, cudaStream_t st) {
+  k_flux<<<nb_edge, 256, 0, st>>>(map, sin);
+}
+void chl_launch_update(const ChlMap& map, int nb_pt, int sbase, int sout, double c1, double c2, int mode,
+                       cudaStream_t st) {
+  RhsArgs a{sbase, sout, c1, c2, mode};
+  k_rhs_update<<<nb_pt, 256, 0, st>>>(map, a);
+}
 }

@@ -113,11 +113,13 @@ k_centre(ChlMap map, int s_in, int dsm) {
 // y pass: q (and the velocity set s_in for the three face components) -> r.
 // Centre components use rows 1..Ny, U and W rows 0..Ny+1, V rows 0..Ny, each
 // with the one-sided rule at its first and last row.
+// Branch-free: at the first (last) row the missing neighbour is replaced by
+// the other one, so lo + 4q + hi becomes 4q + 2*hi (4q + 2*lo), the
+// one-sided 2/3-1/3 rule times 6.  Only the addresses are selected.
 __device__ __forceinline__ double fy(const double* f, size_t c, size_t pitch, int j, int j0, int j1) {
-  const double q = LDG(f + c);
-  if (j == j0) return fma(4.0, q, 2.0 * LDG(f + c + pitch));
-  if (j == j1) return fma(4.0, q, 2.0 * LDG(f + c - pitch));
-  return fma(4.0, q, LDG(f + c - pitch) + LDG(f + c + pitch));
+  const size_t lo = (j == j0) ? c + pitch : c - pitch;
+  const size_t hi = (j == j1) ? c - pitch : c + pitch;
+  return fma(4.0, LDG(f + c), LDG(f + lo) + LDG(f + hi));
 }
 
 __global__ void __launch_bounds__(256)
@@ -263,19 +265,30 @@ __global__ void k_coef(ChlMap map) {
 #define EQWM_KAPPA 0.41
 #define EQWM_B 5.2
 #define EQWM_ITERS 12
-__device__ double eqlog_tau(double u, double h, double nu) {
+// Newton on f(ut) = ut (ln(h ut/nu)/kappa + B) - |u|.  f is convex and
+// increasing, so from any start right of the root the iterates decrease
+// monotonically; `guess` (the previous stage's u_tau, when it lies right of
+// the root) saves most iterations.  The iteration stops when the update is
+// below 4 ulp; the root agrees with a fixed-count solve to rounding.
+__device__ double eqlog_tau(double u, double h, double nu, double guess) {
   const double au = fabs(u);
   const double ut_lam = sqrt(nu * au / h);
-  const double f0 = ut_lam * (log(h * ut_lam / nu) / EQWM_KAPPA + EQWM_B) - au;
+  const double yp_lam = h * ut_lam / nu;
+  const double f0 = ut_lam * (log(yp_lam) / EQWM_KAPPA + EQWM_B) - au;
   double ut = ut_lam;
-  if (f0 < 0.0) {
-    for (int it = 0; it < EQWM_ITERS; ++it) {
+  // log law only above its upper crossing with u+ = y+ (y+ ~ 11)
+  if (f0 < 0.0 && yp_lam >= 1.0) {
+    if (guess > ut_lam) {
+      const double fg = guess * (log(h * guess / nu) / EQWM_KAPPA + EQWM_B) - au;
+      if (fg >= 0.0) ut = guess;
+    }
+    for (int it = 0; it < 2 * EQWM_ITERS; ++it) {
       const double lg = log(h * ut / nu);
       const double f = ut * (lg / EQWM_KAPPA + EQWM_B) - au;
       const double fp = lg / EQWM_KAPPA + EQWM_B + 1.0 / EQWM_KAPPA;
       const double d = f / fp;
       ut = ut - d;
-      if (fabs(d) <= 1e-17 * ut) break;
+      if (fabs(d) <= 9e-16 * ut) break;
     }
   }
   const double tau = ut * ut;
@@ -291,7 +304,8 @@ __global__ void k_eqwm(ChlMap map, int s_in) {
   const int a = (int)(t % Nx), k = (int)((t / Nx) % Nz), wall = (int)(t / ((long)Nx * Nz));
   const double* U = I.U[s_in];
   const double u = wall == 0 ? U[cidx(I, a, 3, k)] : U[cidx(I, a, Ny - 2, k)];
-  I.alpha[t] = eqlog_tau(u, wall == 0 ? I.hb : I.ht, I.nu);
+  const double prev = I.alpha[t];
+  I.alpha[t] = eqlog_tau(u, wall == 0 ? I.hb : I.ht, I.nu, sqrt(fabs(prev)));
 }
 
 // ------------------------------------------------------------ nu_t (+ wall model rows)
@@ -325,7 +339,8 @@ k_nut(ChlMap map, int s_in, int use_wm) {
     const double* U = I.U[s_in];
     v = 0.5 * (wm_face(I, U, wrap(i - 1, Nx), k, wall) + wm_face(I, U, i, k, wall));
   }
-  I.nut[cidx(I, i, jc, k)] = v;
+  // stored as nu + nu_t: every consumer adds nu (equations.f90:139-155)
+  I.nut[cidx(I, i, jc, k)] = I.nu + v;
 }
 
 // ------------------------------------------------------------ launchers

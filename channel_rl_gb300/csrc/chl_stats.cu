@@ -67,8 +67,8 @@ k_stats_wall(ChlMap map, int s, double* out, int pitch) {
     const int i = (int)(w % Nx), k = (int)(w / Nx), ip = wrap(i + 1, Nx);
     const double ntf0 = 0.5 * (nt[cidx(I, i, 0, k)] + nt[cidx(I, ip, 0, k)]);
     const double ntf1 = 0.5 * (nt[cidx(I, i, 1, k)] + nt[cidx(I, ip, 1, k)]);
-    const double ntw = w0 * ntf0 + w1 * ntf1;
-    tau += (U[cidx(I, i, 1, k)] - U[cidx(I, i, 0, k)]) / I.dyw * (I.nu + ntw);
+    const double ntw = w0 * ntf0 + w1 * ntf1;      // nu + nu_t at the wall (weights sum to 1)
+    tau += (U[cidx(I, i, 1, k)] - U[cidx(I, i, 0, k)]) / I.dyw * ntw;
   }
   for (long w = threadIdx.x; w < (long)Nx * (Ny - 1) * Nz; w += blockDim.x) {
     const int i = (int)(w % Nx), jc = 2 + (int)((w / Nx) % (Ny - 1)), k = (int)(w / ((long)Nx * (Ny - 1)));

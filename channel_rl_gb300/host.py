@@ -53,7 +53,8 @@ EXPORTS = (
     "chl_compute_wall_model", "chl_compute_rhs", "chl_compute_projection_step",
     "chl_compute_dPx_for_constant_mass_flow", "chl_compute_pressure", "chl_check_divergence",
     "chl_stats", "chl_stats_profiles", "chl_synchronize", "chl_grid_constants_size",
-    "chl_grid_constants",
+    "chl_grid_constants", "chl_set_fields", "chl_download_async", "chl_time_steps",
+    "chl_graph_kernel_count", "chl_profile_step",
 )
 
 
@@ -98,6 +99,11 @@ def load(build_if_missing=True):
     lib.chl_stats_profiles.argtypes = [H, C.c_int] + [_F64P] * 7
     lib.chl_grid_constants_size.argtypes = [C.POINTER(GridDesc)]
     lib.chl_grid_constants.argtypes = [C.POINTER(GridDesc), _F64P]
+    lib.chl_set_fields.argtypes = [H, C.c_int, _F64P, _F64P, _F64P]
+    lib.chl_download_async.argtypes = [H, C.c_int, _F64P, _F64P, _F64P]
+    lib.chl_time_steps.argtypes = [H, C.c_int, _F64P]
+    lib.chl_graph_kernel_count.argtypes = [H, C.POINTER(C.c_int)]
+    lib.chl_profile_step.argtypes = [H, C.c_int, C.c_int, C.c_char_p, _F64P, C.POINTER(C.c_int)]
     _LIB = lib
     return lib
 
@@ -232,6 +238,40 @@ class Channel:
         cur.update(kw)
         s = np.array([cur["dt"], cur["t"], cur["dPdx"], cur["Qflow_x_0"]])
         self._check(self.lib.chl_set_scalars(self.h, inst, _ptr(s)), "chl_set_scalars")
+
+    def set_fields_ptr(self, U, V, W, inst=0):
+        """Stream-ordered replacement of U, V, W from host buffers (no sync)."""
+        self._check(self.lib.chl_set_fields(self.h, inst, _ptr(U), _ptr(V), _ptr(W)), "chl_set_fields")
+
+    def download_async(self, U, V, W, inst=0):
+        self._check(self.lib.chl_download_async(self.h, inst, _ptr(U), _ptr(V), _ptr(W)), "chl_download_async")
+
+    # -- measurement -------------------------------------------------------------
+    def time_steps(self, nsteps):
+        """Device milliseconds of nsteps graph replays (events on the library stream)."""
+        ms = C.c_double()
+        self._check(self.lib.chl_time_steps(self.h, nsteps, C.byref(ms)), "chl_time_steps")
+        return ms.value
+
+    def graph_kernel_count(self):
+        n = C.c_int()
+        self._check(self.lib.chl_graph_kernel_count(self.h, C.byref(n)), "chl_graph_kernel_count")
+        return n.value
+
+    def profile_step(self, reps=3, maxk=64):
+        """{kernel: (ms per step, launches per step)} from event-bracketed steps."""
+        names = C.create_string_buffer(32 * maxk)
+        ms = np.zeros(maxk)
+        cnt = (C.c_int * maxk)()
+        n = self.lib.chl_profile_step(self.h, reps, maxk, names, _ptr(ms), cnt)
+        if n < 0:
+            self._check(-n, "chl_profile_step")
+        raw = names.raw
+        out = {}
+        for i in range(n):
+            nm = raw[32 * i:32 * i + 32].split(b"\0", 1)[0].decode()
+            out[nm] = (float(ms[i]), int(cnt[i]))
+        return out
 
     # -- reference subroutines -------------------------------------------------
     def compute_dt(self):

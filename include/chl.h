@@ -124,6 +124,23 @@ int chl_stats_profiles(chl_handle* h, int inst, double* Umean, double* Vmean, do
 
 int chl_synchronize(chl_handle* h);
 
+/* Replace U, V, W of a running instance (no new Qflow_x_0, no sync): the
+ * host-buffer round trip of a Fortran caller that keeps its own copy. */
+int chl_set_fields(chl_handle* h, int inst, const double* U, const double* V, const double* W);
+/* Stream-ordered download of U, V, W into (pinned) host buffers; completes
+ * at the next chl_synchronize. */
+int chl_download_async(chl_handle* h, int inst, double* U, double* V, double* W);
+
+/* Measurement: device time (CUDA events on the handle's stream) of nsteps
+ * replays of the step graph. */
+int chl_time_steps(chl_handle* h, int nsteps, double* ms);
+/* Number of kernel nodes in one step graph (compute_dt + RK3). */
+int chl_graph_kernel_count(chl_handle* h, int* count);
+/* Per-kernel device time of one step, averaged over reps un-graphed steps:
+ * names[32*i] (NUL-terminated), ms_per_step[i], launches_per_step[i];
+ * returns the number of kernel kinds (<= maxk) or <0 on error. */
+int chl_profile_step(chl_handle* h, int reps, int maxk, char* names, double* ms_per_step, int* launches_per_step);
+
 /* Host-only: the grid constants chl_create derives (initialization.f90:
  * 187-427), for checking without a GPU.  out must hold chl_grid_constants_size
  * doubles: [kxx(0:Nx-1), kzz(0:Nz-1), Dd(2:nyg-1), Du(2:nyg-1), Dl(2:nyg-1),

@@ -901,8 +901,11 @@ def eqlog_tau(u, h, nu):
     ut = ut_lam.copy()
     lam = np.zeros(au.shape, dtype=bool)
     with np.errstate(divide="ignore", invalid="ignore"):
-        f0 = ut_lam * (np.log(h * ut_lam / nu) / KAPPA + B_LOG) - au
-        lam = ~(f0 < 0.0)
+        yp_lam = h * ut_lam / nu
+        f0 = ut_lam * (np.log(yp_lam) / KAPPA + B_LOG) - au
+        # log law only above the upper crossing with u+ = y+ (y+ ~ 11);
+        # below y+ = 1 the log law is meaningless (second crossing near 0.05)
+        lam = ~((f0 < 0.0) & (yp_lam >= 1.0))
         for _ in range(EQWM_NEWTON_ITERS):
             lg = np.log(h * ut / nu)
             f = ut * (lg / KAPPA + B_LOG) - au
