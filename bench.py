@@ -296,7 +296,6 @@ def run_ours(args):
     peaks = load_json(os.path.join(HERE, "MEASURED_PEAKS.json"), {})
     hbm_peak = float(peaks.get("hbm_gbs", 6789.6))
     fp64 = load_json(os.path.join(HERE, "profiles", "fp64_peak.json"), {})
-    fp64_peak = fp64.get("dfma_gflops")
     traffic = load_json(os.path.join(HERE, "profiles", "kernel_traffic.json"), {})
     byt = KERNEL_BYTES.get(dom, 0.0) * points
     achieved = byt / per_launch_s / 1e9
@@ -307,11 +306,21 @@ def run_ours(args):
     sgs = "dsm" if cases_[0].LES_model == 2 else "smag"
     step_bytes = 8 * STEP_STREAMS[sgs] * points
     roof["step_hbm_gbs_vs_fused_minimum"] = step_bytes / (tmax_ms / args.steps * 1e-3) / 1e9
-    fl = traffic.get("fp64_ops_per_point", {}).get(args.workload, {}) if traffic else {}
-    if fp64_peak and dom in fl:
-        fp = fl[dom] * 2.0 * points / per_launch_s / 1e9   # DFMA counted as 2 flops
-        roof["fp64"] = {"bound": "fp64", "achieved": fp, "peak": fp64_peak, "unit": "GFLOP/s",
-                        "frac": fp / fp64_peak, "peak_source": "measured (profiles/fp64_peak.json)"}
+    # FP64 issue roofline (the binding one on GB300): FP64-pipe instructions
+    # per grid point of each kernel from the committed ncu capture, against
+    # the measured DFMA issue rate.
+    fl = (traffic or {}).get("fp64_instr_per_point", {}).get(args.workload, {})
+    peak_gops = fp64.get("dfma_gops")
+    if peak_gops and dom in fl:
+        ach = fl[dom] * points / per_launch_s / 1e9
+        step_instr = sum(fl.get(k, 0.0) * n for k, (_, n) in prof.items()) * points
+        step_ach = step_instr / (tmax_ms / args.steps * 1e-3) / 1e9
+        roof["fp64"] = {"bound": "fp64-issue", "kernel": dom, "achieved": ach, "peak": peak_gops,
+                        "unit": "G FP64 instr/s", "frac": ach / peak_gops,
+                        "step_achieved": step_ach, "step_frac": step_ach / peak_gops,
+                        "step_fp64_instr_per_point": step_instr / points,
+                        "peak_source": "measured (profiles/fp64_peak.json, DFMA issue rate)"}
+        roof["binding"] = "fp64"
     # e2e through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e and len(cases_) == 1:
