@@ -55,6 +55,7 @@ EXPORTS = (
     "chl_stats", "chl_stats_profiles", "chl_synchronize", "chl_grid_constants_size",
     "chl_grid_constants", "chl_set_fields", "chl_download_async", "chl_time_steps",
     "chl_graph_kernel_count", "chl_profile_step",
+    "chl_check_divergence_noalloc", "chl_noalloc_last_error",
 )
 
 

@@ -141,6 +141,28 @@ int chl_graph_kernel_count(chl_handle* h, int* count);
  * returns the number of kernel kinds (<= maxk) or <0 on error. */
 int chl_profile_step(chl_handle* h, int reps, int maxk, char* names, double* ms_per_step, int* launches_per_step);
 
+/* Allocation-free divergence check, for callers that must not let a
+ * library allocate device memory (their device memory comes from their own
+ * pool or a framework's allocator, or their time loop cannot take the
+ * implicit synchronisation of cudaMalloc/cudaFree); such callers cannot use
+ * chl_create.  No counterpart in the reference: it reports what
+ * chl_check_divergence reports (signed max of div u and max |div u| over
+ * centres i=2..nxg-1, j=2..nyg-1, k=2..nzg-1) from caller-owned DEVICE
+ * arrays U(nx,nyg,nzg), V(nxg,ny,nzg), W(nxg,nyg,nz) and face coordinates
+ * x(nx), y(ny), z(nz) with consistent ghosts, on `stream` (a cudaStream_t,
+ * NULL for the default stream); it synchronises that stream.
+ * Limit: nz - 1 <= 4096 (its scratch is a fixed 64 KiB device array held by
+ * every GPU that loads the library); larger grids return CHL_E_ARG.
+ * The first call on each device looks up the scratch address and should
+ * come before any stream capture.  Calls that overlap on the GPU race on
+ * the shared scratch and must be serialised by the caller.
+ * Errors: chl_noalloc_last_error() (per host thread). */
+int chl_check_divergence_noalloc(const double* U, const double* V, const double* W,
+                                 const double* x, const double* y, const double* z,
+                                 int nx, int ny, int nz, void* stream,
+                                 double* max_div, double* max_abs_div);
+const char* chl_noalloc_last_error(void);
+
 /* Host-only: the grid constants chl_create derives (initialization.f90:
  * 187-427), for checking without a GPU.  out must hold chl_grid_constants_size
  * doubles: [kxx(0:Nx-1), kzz(0:Nz-1), Dd(2:nyg-1), Du(2:nyg-1), Dl(2:nyg-1),
