@@ -77,6 +77,8 @@ def workload(name):
         return [C.c2_wm64()]
     if name == "c4":
         return C.c4_ensemble()
+    if name == "c5":
+        return C.c5_learned()
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -271,6 +273,8 @@ def run_ours(args):
     ch = Channel(cases_)
     for q, case in enumerate(cases_):
         ch.upload(*C.initial_fields(case), inst=q)
+    if cases_[0].wall_model == C.WM_MLP:
+        ch.mlp_set_params(mlp_params()[0])
     points = sum(c.points for c in cases_)
     # warm-up (builds the graph on the first call)
     ch.step(max(args.warmup, 1))
@@ -333,6 +337,8 @@ def run_ours(args):
             "host_wall_s": wall,
             "kernels_ms_per_step": {k: round(v[0], 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
             "profiled_step_ms": tot_prof}
+    if args.workload in ("c3_dsm", "c3_smag") and not args.no_batched:
+        line["batched_mlp"] = batched_mlp_rate(args)
     if rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
         samp = cpu_sample(cases_)
         rate, nsteps, secs = oracle_step_rate(samp, args.cpu_budget, 50)
@@ -343,6 +349,46 @@ def run_ours(args):
     if rank == 0:
         print(json.dumps(line), flush=True)
     ch.close()
+
+
+def mlp_params():
+    """Trained wall-model parameters if a checkpoint ships with the package,
+    else the seeded initial network."""
+    from channel_rl_gb300 import rl
+    path = os.path.join(HERE, "channel_rl_gb300", "data", "mlp_wm.npy")
+    if os.path.exists(path):
+        return np.load(path).astype(np.float32), "trained checkpoint"
+    return rl.init_params(1234), "seeded Xavier initialisation"
+
+
+def timed_rate(cases_, args, steps, setup=None):
+    from channel_rl_gb300.host import Channel
+    ch = Channel(cases_)
+    for q, c in enumerate(cases_):
+        ch.upload(*C.initial_fields(c), inst=q)
+    if setup:
+        setup(ch)
+    ch.step(max(args.warmup, 3))
+    ch.synchronize()
+    ms = ch.time_steps(steps)
+    ch.close()
+    return sum(c.points for c in cases_) * steps / (ms * 1e-3), ms / steps
+
+
+def batched_mlp_rate(args):
+    """16 uneven channels with the learned wall model in one launch per
+    kernel, against one of them run alone with the plain method."""
+    from dataclasses import replace
+    batch = C.c5_learned()
+    theta, src = mlp_params()
+    rate_b, ms_b = timed_rate(batch, args, 20, setup=lambda ch: ch.mlp_set_params(theta))
+    single = replace(batch[0], wall_model=C.WM_EQLOG)
+    rate_s, ms_s = timed_rate([single], args, 40)
+    return {"metric": METRIC, "value": rate_b, "unit": UNIT, "ms_per_step": ms_b, "instances": len(batch),
+            "points": sum(c.points for c in batch), "wall_model": f"mlp ({src})",
+            "plain_single_instance": {"value": rate_s, "grid": f"{single.Nx}x{single.Ny}x{single.Nz}",
+                                      "ms_per_step": ms_s, "wall_model": "equilibrium-loglaw"},
+            "speedup_vs_plain_single": rate_b / rate_s}
 
 
 def e2e_rate(ch, case, args):
@@ -385,6 +431,7 @@ def main():
     ap.add_argument("--workload", default="c3_dsm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched learned-wall-model line")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--prof-reps", type=int, default=3)
     ap.add_argument("--cpu-budget", type=float, default=20.0)

@@ -60,6 +60,11 @@ struct ChlInst {
   unsigned long long *minabs;     // [Nx+1 | Nz] min |u| bit patterns (dt)
   double *red;                    // reduction scratch [nblocks]
   int *status;                    // device status word (0 ok)
+  // learned wall model (chl_mlp.cu)
+  double retau;                   // nominal Re_tau of the instance (feature ln(h Re_tau))
+  float *mlp_trace;               // policy-gradient trace of this instance (4545)
+  const float *mlp_theta;         // network parameters, shared by the batch (4545)
+  unsigned int *mlp_cfg;          // shared: sigma bits, train, seed lo/hi, evaluation counter
 };
 
 // device scalar slots

@@ -47,6 +47,10 @@ void chl_launch_tadvance(const ChlMap&, cudaStream_t);
 void chl_launch_divmax(const ChlMap&, int, double*, cudaStream_t);
 void chl_launch_qflow(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_stats(const ChlMap&, int, double*, int, int, cudaStream_t);
+int chl_mlp_setup();
+void chl_launch_mlp(const ChlMap&, int, int, int, int*, cudaStream_t);
+void chl_launch_mlp_test(const float*, const float*, const float*, int, float*, float*, int*, cudaStream_t);
+int chl_tc_selftest_launch(const void*, const void*, float*, int, int*, cudaStream_t);
 }
 
 namespace {
@@ -54,7 +58,8 @@ namespace {
 constexpr double RK_T[3] = {8.0 / 15.0, 2.0 / 3.0, 1.0};
 constexpr double RK_C[3][3] = {{8.0 / 15.0, 0.0, 0.0}, {1.0 / 4.0, 5.0 / 12.0, 0.0}, {1.0 / 4.0, 0.0, 3.0 / 4.0}};
 
-enum { M_PT, M_EDGE, M_FULL, M_DSMF, M_WALL, M_PLANE, M_FFTX, M_FFTZ, M_TRI, M_MINABS, M_ROWS, NMAP };
+enum { M_PT, M_EDGE, M_FULL, M_DSMF, M_WALL, M_PLANE, M_FFTX, M_FFTZ, M_TRI, M_MINABS, M_ROWS, M_MLP, NMAP };
+constexpr int MLP_NPARAM = 4545;
 
 // Grid constants of one instance (host, FP64), in the device index
 // convention of chl_common.cuh.  Arrays along x and z carry one slot of
@@ -195,6 +200,9 @@ struct chl_handle {
   int nblk[NMAP] = {};
   size_t smem_x = 0, smem_z = 0, smem_min = 0;
   int LES_model = 0, wall_model = 0, any_mass = 0;
+  float* d_mlp_theta = nullptr;       // learned wall model parameters (shared)
+  unsigned int* d_mlp_cfg = nullptr;  // sigma, train, seed lo/hi, evaluation counter
+  int* d_mlp_status = nullptr;
   double* d_divout = nullptr;
   double* d_stats = nullptr;
   int stats_pitch = 0;
@@ -247,6 +255,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   size_t o_part = A.take(8 * 2 * (size_t)(Ny + 2) * npart);
   size_t o_coef = A.take(8 * (Ny + 2)), o_scal = A.take(8 * CHL_S_NSCAL);
   size_t o_min = A.take(8 * (size_t)(Nx + Ny + 1 + Nz)), o_status = A.take(64);
+  size_t o_trace = A.take(4 * (size_t)MLP_NPARAM);
   I.nstage = (size_t)c.nxg * c.nyg * c.nzg;
   size_t o_stage = A.take(8 * I.nstage);
   cudaError_t e = cudaMalloc(&I.arena, A.off);
@@ -288,6 +297,10 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.alpha = P(o_alpha); D.bc = P(o_bc); D.part = P(o_part); D.npart = npart;
   D.coef = P(o_coef); D.scal = P(o_scal);
   D.minabs = (unsigned long long*)(base + o_min); D.red = nullptr; D.status = (int*)(base + o_status);
+  D.retau = I.d.Re_tau;
+  D.mlp_trace = (float*)(base + o_trace);
+  D.mlp_theta = h->d_mlp_theta;
+  D.mlp_cfg = h->d_mlp_cfg;
   I.staging = P(o_stage);
   // host constant arrays -> device
   auto put = [&](size_t o, const std::vector<double>& v) { return cudaMemcpyAsync(base + o, v.data(), 8 * v.size(), cudaMemcpyHostToDevice, h->st); };
@@ -356,6 +369,7 @@ static int build_maps(chl_handle* h) {
         case M_TRI: b = cdiv((long)Nz * Nxh, 128); break;
         case M_MINABS: b = Nz; break;
         case M_ROWS: b = Ny + 1; break;
+        case M_MLP: b = cdiv(2L * Nx * Nz, 128); break;
       }
       off[q + 1] = off[q] + b;
     }
@@ -377,11 +391,12 @@ static int build_maps(chl_handle* h) {
   h->smem_z = chl_smem_fftz(mz);
   h->smem_min = 8 * (size_t)mmin;
   if (chl_fft_setup(h->smem_x, h->smem_z)) { h->err = "FFT shared-memory size not supported"; return CHL_E_ARG; }
+  if (chl_mlp_setup()) { h->err = "wall-model network shared-memory size not supported"; return CHL_E_ARG; }
   return CHL_OK;
 }
 
 // ------------------------------------------------------------ schedules
-static int enqueue_sgs(chl_handle* h, int s, bool with_wm) {
+static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
   cudaStream_t st = h->st;
   if (h->LES_model == CHL_LES_DYNAMIC) {
     KL("edges", chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st));
@@ -396,7 +411,10 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm) {
     KL("centre_strain", chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 0, st));
   }
   KL("nut_coef", chl_launch_coef(h->map(M_PT), st));
-  if (with_wm && h->wall_model == CHL_WM_EQLOG) KL("eq_wallmodel", chl_launch_eqwm(h->map(M_WALL), h->nblk[M_WALL], s, st));
+  if (with_wm && (h->wall_model == CHL_WM_EQLOG || h->wall_model == CHL_WM_MLP))
+    KL("eq_wallmodel", chl_launch_eqwm(h->map(M_WALL), h->nblk[M_WALL], s, st));
+  if (with_wm && h->wall_model == CHL_WM_MLP)
+    KL("mlp_wallmodel", chl_launch_mlp(h->map(M_MLP), h->nblk[M_MLP], s, stage, h->d_mlp_status, st));
   KL("nut", chl_launch_nut(h->map(M_FULL), h->nblk[M_FULL], s, with_wm ? 1 : 0, st));
   LAUNCHED();
   return CHL_OK;
@@ -425,7 +443,7 @@ static int enqueue_rk3(chl_handle* h) {
   // set in -> out per stage: 0 -> 1, 1 -> 2, 2 -> 0 (base is always set 0)
   const int sin[3] = {0, 1, 2}, sout[3] = {1, 2, 0};
   for (int s = 0; s < 3; ++s) {
-    int rc = enqueue_sgs(h, sin[s], h->wall_model != CHL_WM_NONE);
+    int rc = enqueue_sgs(h, sin[s], h->wall_model != CHL_WM_NONE, s);
     if (rc) return rc;
     const double c1 = s == 0 ? 0.0 : RK_C[s][0];
     const double c2 = RK_C[s][s];
@@ -492,19 +510,29 @@ int chl_batch_create(int n, const chl_grid_desc* descs, chl_handle** out) {
     I.d = descs[q];
     int rc = make_consts(I.d, I.c, h->err);
     if (rc) { *out = h; return rc; }
-    if (I.d.LES_model < 0 || I.d.LES_model > 2 || I.d.wall_model < 0 || I.d.wall_model > 2) {
+    if (I.d.LES_model < 0 || I.d.LES_model > 2 || I.d.wall_model < 0 || I.d.wall_model > 3) {
       h->err = "unsupported LES_model / wall_model"; *out = h; return CHL_E_ARG;
     }
     if (q > 0 && (I.d.LES_model != h->in[0].d.LES_model || I.d.wall_model != h->in[0].d.wall_model)) {
       h->err = "instances of one batch must share LES_model and wall_model"; *out = h; return CHL_E_ARG;
     }
-    if (I.d.wall_model == CHL_WM_EQLOG && I.c.Ny < 8) { h->err = "equilibrium wall model needs Ny >= 8"; *out = h; return CHL_E_ARG; }
+    if (I.d.wall_model >= CHL_WM_EQLOG && I.c.Ny < 8) { h->err = "equilibrium wall model needs Ny >= 8"; *out = h; return CHL_E_ARG; }
+    if (I.d.wall_model == CHL_WM_MLP && !(I.d.Re_tau > 0.0)) { h->err = "learned wall model needs Re_tau > 0"; *out = h; return CHL_E_ARG; }
     if (I.d.x_mass_cte) h->any_mass = 1;
   }
   h->LES_model = h->in[0].d.LES_model;
   h->wall_model = h->in[0].d.wall_model;
   cudaError_t e = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking);
   if (e != cudaSuccess) { h->err = std::string("CUDA: ") + cudaGetErrorString(e); *out = h; return CHL_E_CUDA; }
+  // learned wall model: zero network (mu = 0: the equilibrium stress), no noise, no trace
+  if (cudaMalloc(&h->d_mlp_theta, sizeof(float) * MLP_NPARAM) != cudaSuccess ||
+      cudaMalloc(&h->d_mlp_cfg, sizeof(unsigned int) * 8) != cudaSuccess ||
+      cudaMalloc(&h->d_mlp_status, sizeof(int) * 2) != cudaSuccess) {
+    h->err = "device allocation failed"; *out = h; return CHL_E_NOMEM;
+  }
+  cudaMemset(h->d_mlp_theta, 0, sizeof(float) * MLP_NPARAM);
+  cudaMemset(h->d_mlp_cfg, 0, sizeof(unsigned int) * 8);
+  cudaMemset(h->d_mlp_status, 0, sizeof(int) * 2);
   for (auto& I : h->in) { int rc = upload_consts(h, I); if (rc) { *out = h; return rc; } }
   std::vector<ChlInst> hv(n);
   for (int q = 0; q < n; ++q) hv[q] = h->in[q].dev;
@@ -535,6 +563,9 @@ int chl_destroy(chl_handle* h) {
   if (h->d_inst) cudaFree(h->d_inst);
   if (h->d_divout) cudaFree(h->d_divout);
   if (h->d_stats) cudaFree(h->d_stats);
+  if (h->d_mlp_theta) cudaFree(h->d_mlp_theta);
+  if (h->d_mlp_cfg) cudaFree(h->d_mlp_cfg);
+  if (h->d_mlp_status) cudaFree(h->d_mlp_status);
   for (auto& e : h->ev) cudaEventDestroy(e);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
@@ -695,7 +726,8 @@ int chl_compute_eddy_viscosity(chl_handle* h) {
 
 int chl_compute_wall_model(chl_handle* h) {
   int rc = check_ready(h); if (rc) return rc;
-  if (h->wall_model == CHL_WM_EQLOG) chl_launch_eqwm(h->map(M_WALL), h->nblk[M_WALL], 0, h->st);
+  if (h->wall_model >= CHL_WM_EQLOG) chl_launch_eqwm(h->map(M_WALL), h->nblk[M_WALL], 0, h->st);
+  if (h->wall_model == CHL_WM_MLP) chl_launch_mlp(h->map(M_MLP), h->nblk[M_MLP], 0, 0, h->d_mlp_status, h->st);
   chl_launch_nut(h->map(M_FULL), h->nblk[M_FULL], 0, h->wall_model != CHL_WM_NONE ? 1 : 0, h->st);
   LAUNCHED();
   return finish(h);
@@ -869,6 +901,92 @@ int chl_profile_step(chl_handle* h, int reps, int maxk, char* names, double* ms_
     launches_per_step[i] = cnt[i];
   }
   return nk;
+}
+
+// ------------------------------------------------------------ learned wall model
+int chl_mlp_set_params(chl_handle* h, const float* theta) {
+  if (!h || !theta) return CHL_E_ARG;
+  CK(cudaMemcpyAsync(h->d_mlp_theta, theta, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice, h->st));
+  return finish(h);
+}
+
+int chl_mlp_get_params(chl_handle* h, float* theta) {
+  if (!h || !theta) return CHL_E_ARG;
+  CK(cudaMemcpyAsync(theta, h->d_mlp_theta, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost, h->st));
+  return finish(h);
+}
+
+int chl_mlp_configure(chl_handle* h, float sigma, unsigned long long seed, int train) {
+  if (!h || !(sigma >= 0.0f)) { if (h) h->err = "sigma must be >= 0"; return CHL_E_ARG; }
+  unsigned int c[4];
+  std::memcpy(&c[0], &sigma, 4);
+  c[1] = train ? 1u : 0u;
+  c[2] = (unsigned int)(seed & 0xFFFFFFFFu);
+  c[3] = (unsigned int)(seed >> 32);
+  CK(cudaMemcpyAsync(h->d_mlp_cfg, c, sizeof(c), cudaMemcpyHostToDevice, h->st));   // counter [4] kept
+  return finish(h);
+}
+
+int chl_mlp_read_trace(chl_handle* h, int inst, float* trace, int zero_after) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !trace) return CHL_E_ARG;
+  CK(cudaMemcpyAsync(trace, I->dev.mlp_trace, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost, h->st));
+  if (zero_after) CK(cudaMemsetAsync(I->dev.mlp_trace, 0, sizeof(float) * MLP_NPARAM, h->st));
+  int st = 0;
+  CK(cudaMemcpyAsync(&st, h->d_mlp_status, sizeof(int), cudaMemcpyDeviceToHost, h->st));
+  int rc = finish(h);
+  if (rc) return rc;
+  if (st) { h->err = "wall-model network: tensor-core wait timed out"; return CHL_E_CUDA; }
+  return CHL_OK;
+}
+
+int chl_mlp_eval(chl_handle* h, const float* x, const float* g, int P, float* mu, float* trace) {
+  if (!h || !x || !g || !mu || !trace || P <= 0) return CHL_E_ARG;
+  float *dx = nullptr, *dg = nullptr, *dmu = nullptr, *dtr = nullptr;
+  int rc = CHL_OK;
+  if (cudaMalloc(&dx, sizeof(float) * 4 * P) != cudaSuccess || cudaMalloc(&dg, sizeof(float) * P) != cudaSuccess ||
+      cudaMalloc(&dmu, sizeof(float) * P) != cudaSuccess || cudaMalloc(&dtr, sizeof(float) * MLP_NPARAM) != cudaSuccess) {
+    h->err = "device allocation failed"; rc = CHL_E_NOMEM;
+  }
+  int st = 0;
+  if (!rc) {
+    cudaMemcpyAsync(dx, x, sizeof(float) * 4 * P, cudaMemcpyHostToDevice, h->st);
+    cudaMemcpyAsync(dg, g, sizeof(float) * P, cudaMemcpyHostToDevice, h->st);
+    cudaMemsetAsync(dtr, 0, sizeof(float) * MLP_NPARAM, h->st);
+    cudaMemsetAsync(h->d_mlp_status, 0, sizeof(int), h->st);
+    chl_launch_mlp_test(h->d_mlp_theta, dx, dg, P, dmu, dtr, h->d_mlp_status, h->st);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaMemcpyAsync(mu, dmu, sizeof(float) * P, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(trace, dtr, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&st, h->d_mlp_status, sizeof(int), cudaMemcpyDeviceToHost, h->st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+    if (e != cudaSuccess) { h->err = std::string("CUDA: ") + cudaGetErrorString(e); rc = CHL_E_CUDA; }
+    else if (st) { h->err = "wall-model network: tensor-core wait timed out"; rc = CHL_E_CUDA; }
+  }
+  cudaFree(dx); cudaFree(dg); cudaFree(dmu); cudaFree(dtr);
+  return rc;
+}
+
+int chl_tc_selftest(const unsigned short* A, const unsigned short* B, float* D, int variant) {
+  if (!A || !B || !D || variant < 0 || variant > 1) return CHL_E_ARG;
+  void *dA = nullptr, *dB = nullptr; float* dD = nullptr; int* ds = nullptr;
+  int rc = CHL_OK;
+  if (cudaMalloc(&dA, 2 * 128 * 64) != cudaSuccess || cudaMalloc(&dB, 2 * 64 * 64) != cudaSuccess ||
+      cudaMalloc(&dD, 4 * 128 * 64) != cudaSuccess || cudaMalloc(&ds, sizeof(int)) != cudaSuccess) rc = CHL_E_NOMEM;
+  if (!rc) {
+    cudaMemcpy(dA, A, 2 * 128 * 64, cudaMemcpyHostToDevice);
+    cudaMemcpy(dB, B, 2 * 64 * 64, cudaMemcpyHostToDevice);
+    cudaMemset(dD, 0, 4 * 128 * 64);
+    cudaMemset(ds, 0, sizeof(int));
+    if (chl_tc_selftest_launch(dA, dB, dD, variant, ds, 0)) rc = CHL_E_CUDA;
+    cudaError_t e = cudaDeviceSynchronize();
+    int st = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(D, dD, 4 * 128 * 64, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(&st, ds, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess || st) rc = CHL_E_CUDA;
+  }
+  cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(ds);
+  return rc;
 }
 
 static int run_stats(chl_handle* h, int inst, std::vector<double>& buf) {

@@ -193,6 +193,8 @@ k_shift(ChlMap map, int s) {
 __global__ void k_tadvance(ChlMap map) {
   const ChlInst& I = map.inst[blockIdx.x];
   if (threadIdx.x == 0) I.scal[CHL_S_T] = I.scal[CHL_S_T] + 1.0 * I.scal[CHL_S_DT];
+  // step counter of the wall-model exploration noise (shared by the batch)
+  if (blockIdx.x == 0 && threadIdx.x == 0 && I.mlp_cfg) atomicAdd(I.mlp_cfg + 4, 1u);
 }
 
 // ------------------------------------------------------------ divergence check

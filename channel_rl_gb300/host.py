@@ -35,7 +35,7 @@ class GridDesc(C.Structure):
                 ("x", _F64P), ("y", _F64P), ("z", _F64P),
                 ("nu", C.c_double), ("CFL", C.c_double), ("dPdx", C.c_double),
                 ("x_mass_cte", C.c_int), ("LES_model", C.c_int), ("Dirichlet_nu_t", C.c_int),
-                ("wall_model", C.c_int), ("Cs", C.c_double)]
+                ("wall_model", C.c_int), ("Cs", C.c_double), ("Re_tau", C.c_double)]
 
 
 class StatsOut(C.Structure):
@@ -56,7 +56,11 @@ EXPORTS = (
     "chl_grid_constants", "chl_set_fields", "chl_download_async", "chl_time_steps",
     "chl_graph_kernel_count", "chl_profile_step",
     "chl_check_divergence_noalloc", "chl_noalloc_last_error",
+    "chl_mlp_set_params", "chl_mlp_get_params", "chl_mlp_configure", "chl_mlp_read_trace",
+    "chl_mlp_eval", "chl_tc_selftest",
 )
+MLP_NPARAM = 4545
+_F32P = C.POINTER(C.c_float)
 
 
 def library_path():
@@ -105,6 +109,12 @@ def load(build_if_missing=True):
     lib.chl_time_steps.argtypes = [H, C.c_int, _F64P]
     lib.chl_graph_kernel_count.argtypes = [H, C.POINTER(C.c_int)]
     lib.chl_profile_step.argtypes = [H, C.c_int, C.c_int, C.c_char_p, _F64P, C.POINTER(C.c_int)]
+    lib.chl_mlp_set_params.argtypes = [H, _F32P]
+    lib.chl_mlp_get_params.argtypes = [H, _F32P]
+    lib.chl_mlp_configure.argtypes = [H, C.c_float, C.c_ulonglong, C.c_int]
+    lib.chl_mlp_read_trace.argtypes = [H, C.c_int, _F32P, C.c_int]
+    lib.chl_mlp_eval.argtypes = [H, _F32P, _F32P, C.c_int, _F32P, _F32P]
+    lib.chl_tc_selftest.argtypes = [C.POINTER(C.c_ushort), C.POINTER(C.c_ushort), _F32P, C.c_int]
     _LIB = lib
     return lib
 
@@ -126,9 +136,27 @@ class _Keep:
 def grid_desc(case: Case, keep: list):
     x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in faces(case))
     keep.append(_Keep(x, y, z))
-    wm = case.wall_model if case.wall_model in (0, 1, 2) else 1
     return GridDesc(case.nx, case.ny, case.nz, _ptr(x), _ptr(y), _ptr(z), case.nu, case.CFL,
-                    case.dPdx, case.x_mass_cte, case.LES_model, case.Dirichlet_nu_t, wm, case.Cs)
+                    case.dPdx, case.x_mass_cte, case.LES_model, case.Dirichlet_nu_t, case.wall_model,
+                    case.Cs, case.Retau)
+
+
+def _f32(a):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a, a.ctypes.data_as(_F32P)
+
+
+def tc_selftest(A_bf16_bits, B_bf16_bits, variant=0):
+    """D = A B^T on one CTA's tensor cores (tcgen05); A (128,64), B (64,64) uint16 BF16 bits."""
+    lib = load()
+    A = np.ascontiguousarray(A_bf16_bits, dtype=np.uint16)
+    B = np.ascontiguousarray(B_bf16_bits, dtype=np.uint16)
+    D = np.zeros((128, 64), np.float32)
+    rc = lib.chl_tc_selftest(A.ctypes.data_as(C.POINTER(C.c_ushort)), B.ctypes.data_as(C.POINTER(C.c_ushort)),
+                             D.ctypes.data_as(_F32P), variant)
+    if rc:
+        raise ChlError(f"chl_tc_selftest failed ({rc})")
+    return D
 
 
 def grid_constants(case: Case):
@@ -246,6 +274,36 @@ class Channel:
 
     def download_async(self, U, V, W, inst=0):
         self._check(self.lib.chl_download_async(self.h, inst, _ptr(U), _ptr(V), _ptr(W)), "chl_download_async")
+
+    # -- learned wall model -------------------------------------------------------
+    def mlp_set_params(self, theta):
+        t, p = _f32(theta)
+        assert t.size == MLP_NPARAM
+        self._check(self.lib.chl_mlp_set_params(self.h, p), "chl_mlp_set_params")
+
+    def mlp_params(self):
+        t = np.zeros(MLP_NPARAM, np.float32)
+        self._check(self.lib.chl_mlp_get_params(self.h, t.ctypes.data_as(_F32P)), "chl_mlp_get_params")
+        return t
+
+    def mlp_configure(self, sigma=0.0, seed=0, train=False):
+        self._check(self.lib.chl_mlp_configure(self.h, float(sigma), int(seed), int(bool(train))), "chl_mlp_configure")
+
+    def mlp_trace(self, inst=0, zero=True):
+        t = np.zeros(MLP_NPARAM, np.float32)
+        self._check(self.lib.chl_mlp_read_trace(self.h, inst, t.ctypes.data_as(_F32P), int(zero)), "chl_mlp_read_trace")
+        return t
+
+    def mlp_eval(self, x, g):
+        """mu and sum_p g_p dmu_p/dtheta of the network on given features (tensor-core kernel)."""
+        xx, px = _f32(x)
+        gg, pg = _f32(g)
+        P = gg.size
+        mu = np.zeros(P, np.float32)
+        tr = np.zeros(MLP_NPARAM, np.float32)
+        self._check(self.lib.chl_mlp_eval(self.h, px, pg, P, mu.ctypes.data_as(_F32P), tr.ctypes.data_as(_F32P)),
+                    "chl_mlp_eval")
+        return mu, tr
 
     # -- measurement -------------------------------------------------------------
     def time_steps(self, nsteps):

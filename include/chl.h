@@ -42,6 +42,7 @@ extern "C" {
 #define CHL_WM_NONE 0     /* no-slip: compute_wall_model skipped */
 #define CHL_WM_STRESS 1   /* compute_wall_model with a caller-set alpha_x (wallmodel.f90:23-46) */
 #define CHL_WM_EQLOG 2    /* equilibrium log law at the third cell computes alpha_x each stage */
+#define CHL_WM_MLP 3      /* equilibrium stress times exp(MLP correction), chl_mlp_* below */
 
 typedef struct chl_handle chl_handle;
 
@@ -61,6 +62,7 @@ typedef struct {
   int Dirichlet_nu_t;          /* 1: nu_t ghost = -nu_t (Dirichlet), 0: Neumann */
   int wall_model;              /* CHL_WM_* */
   double Cs;                   /* static Smagorinsky constant */
+  double Re_tau;               /* nominal friction Reynolds number (CHL_WM_MLP feature) */
 } chl_grid_desc;
 
 /* Statistics of compute_statistics (statistics.f90:22-145). */
@@ -140,6 +142,26 @@ int chl_graph_kernel_count(chl_handle* h, int* count);
  * names[32*i] (NUL-terminated), ms_per_step[i], launches_per_step[i];
  * returns the number of kernel kinds (<= maxk) or <0 on error. */
 int chl_profile_step(chl_handle* h, int reps, int maxk, char* names, double* ms_per_step, int* launches_per_step);
+
+/* Learned wall model (CHL_WM_MLP).  Counterpart of the smarties policy that
+ * sets alpha_x from per-agent states (smarties_stat.f90:24-260): a
+ * 4-64-64-1 tanh network per wall point, BF16 weights, FP32 accumulation,
+ * tensor-core GEMMs.  theta: 4545 FP32 values, W1(64x4) b1 W2(64x64) b2
+ * w3(64) b3, row major (one network shared by all instances of a batch). */
+#define CHL_MLP_NPARAM 4545
+int chl_mlp_set_params(chl_handle* h, const float* theta);
+int chl_mlp_get_params(chl_handle* h, float* theta);
+/* Gaussian exploration noise sigma on the log-stress action, its seed, and
+ * whether steps accumulate the policy-gradient trace sum_t eps/sigma dmu/dtheta. */
+int chl_mlp_configure(chl_handle* h, float sigma, unsigned long long seed, int train);
+/* Trace of one instance (4545 floats); zero it afterwards if zero_after. */
+int chl_mlp_read_trace(chl_handle* h, int inst, float* trace, int zero_after);
+/* Network on given points (no channel): x[P][4] normalised features,
+ * g[P] upstream weights -> mu[P] and trace = sum_p g_p dmu_p/dtheta. */
+int chl_mlp_eval(chl_handle* h, const float* x, const float* g, int P, float* mu, float* trace);
+/* Standalone tensor-core check: D[128x64] = A[128x64] B[64x64]^T, BF16
+ * inputs (raw 16-bit patterns, row major), FP32 output. */
+int chl_tc_selftest(const unsigned short* A, const unsigned short* B, float* D, int variant);
 
 /* Allocation-free divergence check, for callers that must not let a
  * library allocate device memory (their device memory comes from their own

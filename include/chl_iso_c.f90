@@ -21,7 +21,7 @@ Module chl_iso_c
      Type(c_ptr)    :: x, y, z
      Real(c_double) :: nu, CFL, dPdx
      Integer(c_int) :: x_mass_cte, LES_model, Dirichlet_nu_t, wall_model
-     Real(c_double) :: Cs
+     Real(c_double) :: Cs, Re_tau
   End Type chl_grid_desc
 
   Interface
@@ -144,7 +144,7 @@ Contains
     d%x = c_loc(xs); d%y = c_loc(ys); d%z = c_loc(zs)
     d%nu = nu; d%CFL = CFL; d%dPdx = dPdx
     d%x_mass_cte = x_mass_cte; d%LES_model = LES_model; d%Dirichlet_nu_t = Dirichlet_nu_t
-    d%wall_model = wall_model; d%Cs = 0.1d0
+    d%wall_model = wall_model; d%Cs = 0.1d0; d%Re_tau = 0d0
     Call chl_check(chl_create(d, chl_h), 'chl_create')
     Call chl_check(chl_upload(chl_h, 0_c_int, U, V, W), 'chl_upload')
     Call chl_check(chl_set_wall_stress(chl_h, 0_c_int, alpha_x), 'chl_set_wall_stress')

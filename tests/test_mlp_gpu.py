@@ -1,0 +1,84 @@
+"""Learned wall model on the GPU: tensor-core tile, network and policy-gradient
+trace against the CPU reference, and its coupling to the channel."""
+import numpy as np
+import pytest
+
+from channel_rl_gb300 import cases as C
+from oracle import mlp_ref as M
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    return M.bf16(a).view(np.uint32) >> 16
+
+
+def test_tensor_core_tile_gemm():
+    from channel_rl_gb300.host import tc_selftest
+    rng = np.random.default_rng(0)
+    A = M.bf16(rng.standard_normal((128, 64)).astype(np.float32))
+    B = M.bf16(rng.standard_normal((64, 64)).astype(np.float32))
+    D = tc_selftest(_bits(A).astype(np.uint16), _bits(B).astype(np.uint16), variant=0)
+    ref = A.astype(np.float64) @ B.astype(np.float64).T
+    assert np.abs(D - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+def _channel(case):
+    from channel_rl_gb300.host import Channel
+    return Channel(case)
+
+
+def test_network_and_trace_match_reference():
+    case = C.smaller(C.c2_wm64(), 32, 32, 32)
+    ch = _channel(case)
+    rng = np.random.default_rng(1)
+    theta = M.xavier_init(7)
+    theta[M.H * M.NIN:M.H * M.NIN + M.H] = rng.standard_normal(M.H).astype(np.float32) * 0.1
+    ch.mlp_set_params(theta)
+    assert np.array_equal(ch.mlp_params(), theta)
+    P = 1000                                   # not a multiple of the 128-point tile
+    x = (rng.standard_normal((P, 4)) * 0.7).astype(np.float32)
+    g = rng.standard_normal(P).astype(np.float32)
+    mu, tr = ch.mlp_eval(x, g)
+    ref = M.forward(theta, x)["mu"]
+    assert np.abs(mu - ref).max() < 4e-3          # BF16 activations: a last-bit flip of h1 moves mu by ~1e-3
+    rt = M.trace_grad(theta, x, g)
+    assert np.linalg.norm(tr - rt) / np.linalg.norm(rt) < 2e-2
+    for name, sl in (("W2", slice(320, 4416)), ("W1", slice(0, 256)), ("w3", slice(4480, 4544))):
+        assert np.linalg.norm(tr[sl] - rt[sl]) / np.linalg.norm(rt[sl]) < 3e-2, name
+    ch.close()
+
+
+def test_zero_network_is_the_equilibrium_model():
+    """mu = 0 gives tau_w = tau_eq * exp(0): the fields match the equilibrium run bit for bit."""
+    from dataclasses import replace
+    eq = C.smaller(C.c2_wm64(), 32, 32, 32)
+    ml = replace(eq, wall_model=C.WM_MLP)
+    a, b = _channel(eq), _channel(ml)
+    U, V, W = C.initial_fields(eq)
+    a.upload(U, V, W)
+    b.upload(U, V, W)
+    a.step(3)
+    b.step(3)
+    da, db = a.download(), b.download()
+    for f in "UVW":
+        assert np.array_equal(da[f], db[f]), f
+    a.close()
+    b.close()
+
+
+def test_exploration_trace_accumulates():
+    from dataclasses import replace
+    ml = replace(C.smaller(C.c2_wm64(), 32, 32, 32), wall_model=C.WM_MLP)
+    ch = _channel(ml)
+    ch.upload(*C.initial_fields(ml))
+    ch.mlp_set_params(M.xavier_init(11))
+    ch.mlp_configure(sigma=0.1, seed=5, train=True)
+    ch.step(2)
+    ch.synchronize()
+    tr = ch.mlp_trace(zero=True)
+    assert np.all(np.isfinite(tr)) and np.abs(tr).max() > 0
+    assert np.abs(ch.mlp_trace(zero=False)).max() == 0
+    d = ch.download()
+    assert all(np.isfinite(v).all() for v in d.values())
+    ch.close()
