@@ -13,9 +13,10 @@ iteration of the reference's solver loop: compute_dt + compute_time_step_RK3
           U, V, W from pinned host memory (chl_set_fields), steps, and reads
           U, V, W back (chl_download_async), timed on the host clock.
   --impl reference
-          the reference algorithm on the host cores: the oracle restatement
-          (the Fortran reference cannot be built: no gfortran/MPI/FFTW here or
-          on the GPU host), each step a bounded sample of the same workload.
+          the reference algorithm on all host cores: the oracle's C++/OpenMP
+          restatement of the step (the Fortran reference cannot be built: no
+          gfortran/MPI/FFTW here or on the GPU host), whole steps of the same
+          workload until a time budget (--ref-budget) is spent.
 
 Multi-GPU (torchrun): independent replicas (one channel per rank, weak
 scaling); value = all ranks' grid-point steps / max rank time.
@@ -179,27 +180,55 @@ def barrier(dist):
         dist.barrier()
 
 
-# ---------------------------------------------------------------- CPU (oracle) timing
-SAMPLE_POINTS = 600_000
+# ---------------------------------------------------------------- host-core timing
+def host_step_rate(cases_, budget_s, max_steps, warmup=1):
+    """Grid-point steps/s of the oracle's multi-core C++ restatement of the
+    reference step (OpenMP over all host cores) on the given workload: per
+    instance `warmup` untimed steps, then whole steps until its share of
+    budget_s is spent (at least one).  The learned wall model has no host
+    restatement; its instances run the equilibrium model it corrects."""
+    from dataclasses import replace
+    from oracle.refcpu import RefCPU
+    total_pts, total_t, nsteps = 0, 0.0, 0
+    for case in cases_:
+        c = replace(case, wall_model=min(case.wall_model, C.WM_EQLOG))
+        r = RefCPU(c, threads=os.cpu_count())
+        r.upload(*C.initial_fields(c))
+        r.step(warmup)
+        t0 = time.perf_counter()
+        n = 0
+        while n < max_steps:
+            r.step(1)
+            n += 1
+            if time.perf_counter() - t0 > budget_s / len(cases_):
+                break
+        total_t += time.perf_counter() - t0
+        total_pts += c.points * n
+        nsteps += n
+        r.close()
+    return total_pts / total_t, nsteps, total_t, RefCPU.threads()
 
 
-def cpu_sample(cases_):
-    """Bounded sample of a workload for the host-core timing: instances in
-    order up to ~SAMPLE_POINTS cells; an instance larger than that keeps its
-    x-y plane and physics and is cut to fewer z planes (a slab), so the
-    per-point work is that of the full workload."""
-    out, pts = [], 0
-    for c in cases_:
-        if pts >= SAMPLE_POINTS:
-            break
-        if c.points > SAMPLE_POINTS:
-            nz = c.Nz
-            while c.Nx * c.Ny * nz > SAMPLE_POINTS and nz % 2 == 0 and nz > 8:
-                nz //= 2
-            c = C.smaller(c, c.Nx, c.Ny, nz)
-        out.append(c)
-        pts += c.points
-    return out
+def host_single_thread_rate(case):
+    """The same restatement on one host thread: one untimed and one timed
+    whole step of the workload's first instance."""
+    from dataclasses import replace
+    from oracle.refcpu import RefCPU
+    c = replace(case, wall_model=min(case.wall_model, C.WM_EQLOG))
+    r = RefCPU(c)
+    n0 = RefCPU.threads()
+    RefCPU.set_threads(1)
+    try:
+        r.upload(*C.initial_fields(c))
+        r.step(1)
+        t0 = time.perf_counter()
+        r.step(1)
+        secs = time.perf_counter() - t0
+    finally:
+        RefCPU.set_threads(n0)
+        r.close()
+    return {"value": c.points / secs, "unit": UNIT, "cores": 1,
+            "sample": f"1 whole RK3 step of {c.Nx}x{c.Ny}x{c.Nz}, {secs:.2f} s on 1 host thread"}
 
 
 def describe(cases_):
@@ -209,28 +238,11 @@ def describe(cases_):
     return f"{len(cases_)} instances, {sum(c.points for c in cases_)} cells"
 
 
-def oracle_step_rate(cases_, budget_s, max_steps):
-    """Grid-point steps/s of the oracle restatement on this host, timing
-    whole steps of the given workload until budget_s (at least one)."""
-    from oracle.channel_ref import ChannelOracle, Grid, Params
-    total_pts, total_t, nsteps = 0, 0.0, 0
-    for case in cases_:
-        o = ChannelOracle(Grid(*C.faces(case)),
-                          Params(nu=case.nu, CFL=case.CFL, dPdx=case.dPdx, x_mass_cte=case.x_mass_cte,
-                                 LES_model=case.LES_model, Dirichlet_nu_t=case.Dirichlet_nu_t,
-                                 wall_model=min(case.wall_model, 2), Cs=case.Cs))
-        o.set_fields(*C.initial_fields(case))
-        t0 = time.perf_counter()
-        n = 0
-        while n < max_steps:
-            o.step()
-            n += 1
-            if time.perf_counter() - t0 > budget_s / len(cases_):
-                break
-        total_t += time.perf_counter() - t0
-        total_pts += case.points * n
-        nsteps += n
-    return total_pts / total_t, nsteps, total_t
+def host_sample_text(nsteps, cases_, args, secs, cores):
+    wm = " (learned wall model replaced by the equilibrium model)" if cases_[0].wall_model == C.WM_MLP else ""
+    return (f"{nsteps} whole RK3 step(s) (compute_dt + compute_time_step_RK3) of {args.workload} "
+            f"({describe(cases_)}){wm}, C++/OpenMP restatement of the reference step "
+            f"(oracle/refcpu.cpp), {secs:.1f} s on {cores} host threads")
 
 
 def run_reference(args):
@@ -238,16 +250,14 @@ def run_reference(args):
     if rank != 0:
         return
     cases_ = workload(args.workload)
-    samp = cpu_sample(cases_)
-    rate, nsteps, secs = oracle_step_rate(samp, args.ref_budget, max(1, args.steps))
-    sample = (f"{nsteps} RK3 step(s) (compute_dt + compute_time_step_RK3) of {describe(samp)} cut from "
-              f"{args.workload} ({describe(cases_)}): same physics, NumPy restatement of the reference, "
-              f"{secs:.1f} s on 1 host core")
+    rate, nsteps, secs, cores = host_step_rate(cases_, args.ref_budget, max(1, args.steps),
+                                               warmup=min(max(args.warmup, 0), 1))
+    sample = host_sample_text(nsteps, cases_, args, secs, cores)
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": nsteps, "warmup": 0, "ms_per_step": 1e3 * secs / nsteps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_of(args, cases_),
-            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+            "steps": nsteps, "warmup": min(max(args.warmup, 0), 1), "ms_per_step": 1e3 * secs / nsteps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_of(args, cases_),
+            "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -256,10 +266,15 @@ def config_of(args, cases_):
     c0 = cases_[0]
     les = {0: "none", 1: "static-smagorinsky", 2: "dynamic-smagorinsky"}[c0.LES_model]
     wm = {0: "none", 1: "stress", 2: "equilibrium-loglaw", 3: "mlp"}[c0.wall_model]
+    pts = sum(c.points for c in cases_)
+    streams = STEP_STREAMS["dsm" if c0.LES_model == C.LES_DSM else "smag"]
+    ws = pts * streams * 8
+    l2 = (f"inputs larger than L2 (per-step compulsory traffic {ws / 1e9:.2f} GB vs 129 MB L2)" if ws > 129e6
+          else f"working set {ws / 1e6:.0f} MB fits L2, no flush (small-instance line)")
     return {"workload": args.workload, "instances": len(cases_),
             "grid": f"{c0.Nx}x{c0.Ny}x{c0.Nz}" if len(cases_) == 1 else "mixed",
-            "points": sum(c.points for c in cases_), "Re_tau": c0.Retau, "sgs": les, "wall_model": wm,
-            "parallelism": f"replicas{args.gpus}", "l2": "inputs larger than L2 (per-step working set > 1 GB)"}
+            "points": pts, "Re_tau": c0.Retau, "sgs": les, "wall_model": wm,
+            "parallelism": f"replicas{args.gpus}", "l2": l2}
 
 
 # ---------------------------------------------------------------- our arm
@@ -340,12 +355,10 @@ def run_ours(args):
     if args.workload in ("c3_dsm", "c3_smag") and not args.no_batched:
         line["batched_mlp"] = batched_mlp_rate(args)
     if rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
-        samp = cpu_sample(cases_)
-        rate, nsteps, secs = oracle_step_rate(samp, args.cpu_budget, 50)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"{nsteps} RK3 step(s) of {describe(samp)} cut from {args.workload} "
-                                          f"({describe(cases_)}), same physics, NumPy restatement of the "
-                                          f"reference, {secs:.1f} s on 1 host core"}
+        rate, nsteps, secs, cores = host_step_rate(cases_, args.cpu_budget, 50)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": host_sample_text(nsteps, cases_, args, secs, cores),
+                                "single_thread": host_single_thread_rate(cases_[0])}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ch.close()
@@ -377,18 +390,32 @@ def timed_rate(cases_, args, steps, setup=None):
 
 def batched_mlp_rate(args):
     """16 uneven channels with the learned wall model in one launch per
-    kernel, against one of them run alone with the plain method."""
+    kernel, against the same 16 channels run one at a time, each as a plain
+    single instance (equilibrium wall model): sum of points / sum of times."""
     from dataclasses import replace
     batch = C.c5_learned()
     theta, src = mlp_params()
     rate_b, ms_b = timed_rate(batch, args, 20, setup=lambda ch: ch.mlp_set_params(theta))
-    single = replace(batch[0], wall_model=C.WM_EQLOG)
-    rate_s, ms_s = timed_rate([single], args, 40)
+    ms_seq, smallest = 0.0, None
+    for c in batch:
+        single = replace(c, wall_model=C.WM_EQLOG)
+        r, ms = timed_rate([single], args, 20)
+        ms_seq += ms
+        if smallest is None or single.points < smallest[0]:
+            smallest = (single.points, r, f"{single.Nx}x{single.Ny}x{single.Nz}")
+    pts = sum(c.points for c in batch)
+    rate_s = pts / (ms_seq * 1e-3)
+    small = C.c1_small()
+    rate_c1, _ = timed_rate([small], args, 40)
     return {"metric": METRIC, "value": rate_b, "unit": UNIT, "ms_per_step": ms_b, "instances": len(batch),
-            "points": sum(c.points for c in batch), "wall_model": f"mlp ({src})",
-            "plain_single_instance": {"value": rate_s, "grid": f"{single.Nx}x{single.Ny}x{single.Nz}",
-                                      "ms_per_step": ms_s, "wall_model": "equilibrium-loglaw"},
-            "speedup_vs_plain_single": rate_b / rate_s}
+            "points": pts, "wall_model": f"mlp ({src})",
+            "plain_single_instances_in_sequence": {"value": rate_s, "ms_per_step": ms_seq,
+                                                   "wall_model": "equilibrium-loglaw"},
+            "smallest_plain_single_instance": {"grid": smallest[2], "value": smallest[1]},
+            "speedup_vs_plain_single": rate_b / rate_s,
+            "plain_single_small_channel": {"grid": f"{small.Nx}x{small.Ny}x{small.Nz}", "value": rate_c1,
+                                           "sgs": "dynamic-smagorinsky", "wall_model": "none"},
+            "speedup_vs_plain_single_small_channel": rate_b / rate_c1}
 
 
 def e2e_rate(ch, case, args):
