@@ -119,14 +119,24 @@ class Trainer:
             self.ch.set_fields_ptr(*(np.asfortranarray(s[f]) for f in "UVW"), inst=q)
         self.ch.synchronize()
 
-    def rollout_reward(self, steps, chunks=4):
-        """Mean profile error per instance, profiles averaged over the rollout."""
+    def rollout(self, steps, chunks=4):
+        """(profile error, mean wall stress) per instance: the mean profile
+        and the plane-averaged wall stress sampled `chunks` times over the
+        rollout and averaged."""
         acc = [np.zeros(c.ny) for c in self.cases]
+        tau = np.zeros(len(self.cases))
         for _ in range(chunks):
             self.ch.step(max(1, steps // chunks))
             for q in range(len(self.cases)):
-                acc[q] += self.ch.compute_statistics(q)["Umean"]
-        return np.array([profile_error(a / chunks, c) for a, c in zip(acc, self.cases)])
+                st = self.ch.compute_statistics(q)
+                acc[q] += st["Umean"]
+                tau[q] += st["tau_wall"]
+        err = np.array([profile_error(a / chunks, c) for a, c in zip(acc, self.cases)])
+        return err, tau / chunks
+
+    def rollout_reward(self, steps, chunks=4):
+        """Mean profile error per instance, profiles averaged over the rollout."""
+        return self.rollout(steps, chunks)[0]
 
     def update(self, steps=100, it=0):
         self.restore()
@@ -152,17 +162,19 @@ class Trainer:
         self.ch.mlp_configure(sigma=0.0, seed=0, train=False)
         return float(err.mean())
 
-    def evaluate(self, theta, steps=200):
+    def evaluate(self, theta, steps=200, chunks=4):
         """(profile error, u_tau error) per instance of a deterministic policy
-        from the spun-up state; theta=None is the equilibrium model (mu = 0)."""
+        from the spun-up state; theta=None is the equilibrium model (mu = 0).
+        u_tau comes from the wall stress averaged over the rollout,
+        u_tau = sqrt(2 <tau_w> / L_y) as statistics.f90:108-116 forms it."""
         self.restore()
         self.ch.mlp_set_params(np.zeros(MLP_NPARAM, np.float32) if theta is None else theta)
         self.ch.mlp_configure(sigma=0.0, seed=0, train=False)
-        err = self.rollout_reward(steps)
+        err, tau = self.rollout(steps, chunks)
         ut = []
         for q, c in enumerate(self.cases):
-            st = self.ch.compute_statistics(q)
-            ut.append(abs(st["utau"] - math.sqrt(c.dPdx)) / math.sqrt(c.dPdx))
+            u = math.sqrt(max(tau[q], 0.0) * 2.0 / 2.0)
+            ut.append(abs(u - math.sqrt(c.dPdx)) / math.sqrt(c.dPdx))
         self.ch.mlp_set_params(self.theta)
         return err, np.array(ut)
 
