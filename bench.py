@@ -264,7 +264,7 @@ def run_reference(args):
 
 def config_of(args, cases_):
     c0 = cases_[0]
-    les = {0: "none", 1: "static-smagorinsky", 2: "dynamic-smagorinsky"}[c0.LES_model]
+    les = {0: "none", 1: "static-smagorinsky", 2: "dynamic-smagorinsky", 3: "amd", 4: "vreman"}[c0.LES_model]
     wm = {0: "none", 1: "stress", 2: "equilibrium-loglaw", 3: "mlp"}[c0.wall_model]
     pts = sum(c.points for c in cases_)
     streams = STEP_STREAMS["dsm" if c0.LES_model == C.LES_DSM else "smag"]

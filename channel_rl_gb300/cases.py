@@ -27,7 +27,7 @@ import numpy as np
 KAPPA = 0.41
 B_LOG = 5.2
 
-LES_NONE, LES_SMAG, LES_DSM = 0, 1, 2
+LES_NONE, LES_SMAG, LES_DSM, LES_AMD, LES_VREMAN = 0, 1, 2, 3, 4
 WM_NONE, WM_STRESS, WM_EQLOG, WM_MLP = 0, 1, 2, 3
 
 

@@ -28,6 +28,7 @@ struct ChlInst {
   double hb, ht;                // matching heights of the log-law wall model
   double cbc1, cbc2;            // coef_bc_1*(yg(2)-yg(1)), coef_bc_2*(yg(nyg)-yg(nyg-1))
   double ybot, ytop;            // y(1), y(ny)
+  double dy1;                   // y(2)-y(1) (nu_t ghost rule 2 of AMD and Vreman)
   double gb1, gb2, gt1, gt2;    // pressure-BC metric factors g, g2 (pressure.f90:282-316)
   double dygb, dygt;            // yg(2)-yg(1), yg(nyg)-yg(nyg-1)
   double mass_norm;             // 1/(Nx*Nz)

@@ -26,6 +26,8 @@ void chl_launch_dsm_final(const ChlMap&, int, cudaStream_t);
 void chl_launch_coef(const ChlMap&, cudaStream_t);
 void chl_launch_eqwm(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_nut(const ChlMap&, int, int, int, cudaStream_t);
+void chl_launch_amd(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_vreman(const ChlMap&, int, int, cudaStream_t);
 size_t chl_smem_fftx(int);
 size_t chl_smem_fftz(int);
 int chl_fft_setup(size_t, size_t);
@@ -275,6 +277,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.cbc1 = c.coef_bc_1 * (c.yg[2] - c.yg[1]);
   D.cbc2 = c.coef_bc_2 * (c.yg[c.nyg] - c.yg[c.nyg - 1]);
   D.ybot = c.yf[1]; D.ytop = c.yf[c.ny];
+  D.dy1 = c.yf[2] - c.yf[1];
   const std::vector<double>& y = c.yf;
   D.gb1 = (-3.0 * y[1] + 4.0 * y[2] - y[3]) / 2.0;
   D.gb2 = 2.0 * y[1] - 5.0 * y[2] + 4.0 * y[3] - 1.0 * y[4];
@@ -409,6 +412,11 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
   } else if (h->LES_model == CHL_LES_SMAGORINSKY) {
     KL("edges", chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st));
     KL("centre_strain", chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 0, st));
+  } else if (h->LES_model == CHL_LES_AMD) {
+    KL("edges", chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st));
+    KL("amd", chl_launch_amd(h->map(M_PT), h->nblk[M_PT], s, st));
+  } else if (h->LES_model == CHL_LES_VREMAN) {
+    KL("vreman", chl_launch_vreman(h->map(M_PT), h->nblk[M_PT], s, st));
   }
   KL("nut_coef", chl_launch_coef(h->map(M_PT), st));
   if (with_wm && (h->wall_model == CHL_WM_EQLOG || h->wall_model == CHL_WM_MLP))
@@ -510,8 +518,11 @@ int chl_batch_create(int n, const chl_grid_desc* descs, chl_handle** out) {
     I.d = descs[q];
     int rc = make_consts(I.d, I.c, h->err);
     if (rc) { *out = h; return rc; }
-    if (I.d.LES_model < 0 || I.d.LES_model > 2 || I.d.wall_model < 0 || I.d.wall_model > 3) {
+    if (I.d.LES_model < 0 || I.d.LES_model > 4 || I.d.wall_model < 0 || I.d.wall_model > 3) {
       h->err = "unsupported LES_model / wall_model"; *out = h; return CHL_E_ARG;
+    }
+    if (I.d.Dirichlet_nu_t < 0 || I.d.Dirichlet_nu_t > 2) {
+      h->err = "unsupported Dirichlet_nu_t (0, 1 or 2)"; *out = h; return CHL_E_ARG;
     }
     if (q > 0 && (I.d.LES_model != h->in[0].d.LES_model || I.d.wall_model != h->in[0].d.wall_model)) {
       h->err = "instances of one batch must share LES_model and wall_model"; *out = h; return CHL_E_ARG;

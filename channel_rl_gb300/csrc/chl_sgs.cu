@@ -255,6 +255,8 @@ __global__ void k_coef(ChlMap map) {
         if (I.Dirichlet_nu_t == 0) f = 1.0;
         const double cd = I.smag_csdelta[jc] * f;   // Cs*Delta_j*f
         c = cd * cd;
+      } else if (I.LES_model >= 3) {
+        c = 1.0;                           // AMD, Vreman: S holds nu_t itself
       }
     }
     I.coef[jc] = c;
@@ -328,11 +330,17 @@ k_nut(ChlMap map, int s_in, int use_wm) {
   const int k = (int)(t / ((long)Nx * (Ny + 2)));
   double v = 0.0;
   if (I.LES_model != 0) {
-    int js = jc, sgn = 1;
-    if (jc == 0) { js = 1; sgn = I.Dirichlet_nu_t == 1 ? -1 : 1; }
-    if (jc == Ny + 1) { js = Ny; sgn = I.Dirichlet_nu_t == 1 ? -1 : 1; }
+    const bool ghost = jc == 0 || jc == Ny + 1;
+    const int js = jc == 0 ? 1 : (jc == Ny + 1 ? Ny : jc);
     v = fmax(I.coef[js] * I.S[cidx(I, i, js, k)], 0.0);
-    if (sgn < 0) v = -v;
+    if (ghost) {
+      if (I.Dirichlet_nu_t == 1) {
+        v = -v;
+      } else if (I.Dirichlet_nu_t == 2 && I.LES_model >= 3) {
+        // -nu_t + 2*0.38*dPdx^0.5*(y(2)-y(1))/2 (subgrid.f90:868-871, 998-1001)
+        v = -v + 2.0 * 0.38 * sqrt(I.scal[CHL_S_DPDX]) * I.dy1 / 2.0;
+      }
+    }
   }
   if (use_wm && I.wall_model != 0 && (jc <= 1 || jc >= Ny)) {
     const int wall = jc <= 1 ? 0 : 1;

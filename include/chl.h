@@ -38,6 +38,8 @@ extern "C" {
 #define CHL_LES_NONE 0
 #define CHL_LES_SMAGORINSKY 1
 #define CHL_LES_DYNAMIC 2
+#define CHL_LES_AMD 3          /* anisotropic minimum dissipation (subgrid.f90:632-874) */
+#define CHL_LES_VREMAN 4       /* Vreman (subgrid.f90:897-1004) */
 /* wall_model */
 #define CHL_WM_NONE 0     /* no-slip: compute_wall_model skipped */
 #define CHL_WM_STRESS 1   /* compute_wall_model with a caller-set alpha_x (wallmodel.f90:23-46) */
@@ -59,7 +61,9 @@ typedef struct {
   double dPdx;                 /* imposed pressure gradient (x_mass_cte = 0) */
   int x_mass_cte;              /* 1: constant mass flow (mass_flow.f90:360-413) */
   int LES_model;               /* CHL_LES_* */
-  int Dirichlet_nu_t;          /* 1: nu_t ghost = -nu_t (Dirichlet), 0: Neumann */
+  int Dirichlet_nu_t;          /* 1: nu_t ghost = -nu_t (Dirichlet), 0: Neumann; 2 (AMD, Vreman):
+                                  -nu_t + 0.38 sqrt(dPdx) (y(2)-y(1)) (subgrid.f90:868-871); DSM and
+                                  static Smagorinsky treat 2 as Neumann (subgrid.f90:529-533) */
   int wall_model;              /* CHL_WM_* */
   double Cs;                   /* static Smagorinsky constant */
   double Re_tau;               /* nominal friction Reynolds number (CHL_WM_MLP feature) */

@@ -63,7 +63,7 @@ KAPPA = 0.41
 B_LOG = 5.2
 EQWM_NEWTON_ITERS = 12
 
-LES_NONE, LES_SMAG, LES_DSM = 0, 1, 2
+LES_NONE, LES_SMAG, LES_DSM, LES_AMD, LES_VREMAN = 0, 1, 2, 3, 4
 WM_NONE, WM_STRESS, WM_EQLOG = 0, 1, 2
 
 
@@ -239,6 +239,18 @@ def filter_xzy(Uin):
         for k in (-1, 0, 1):
             out += Y[1 + i:n1 - 1 + i, :, 1 + k:n3 - 1 + k] * _FIL[(i, k)]
     return out
+
+
+def _iavg(u, axis):
+    """interpolate_x / interpolate_z (any di) and interpolate_y with di=1
+    (interpolation.f90:24-105) of the section ``u`` along ``axis``:
+    ui(m) = 0.5 (u(m) + u(m+1)), one point shorter than ``u``."""
+    n = u.shape[axis]
+    lo = [slice(None)] * 3
+    hi = [slice(None)] * 3
+    lo[axis] = slice(0, n - 1)
+    hi[axis] = slice(1, n)
+    return 0.5 * (u[tuple(lo)] + u[tuple(hi)])
 
 
 # ---------------------------------------------------------------------------
@@ -455,12 +467,246 @@ class ChannelOracle:
         self.nu_t = nu_t
         return nu_t
 
+    # -- ghost rows of the AMD and Vreman models (subgrid.f90:858-871, 991-1002)
+    def _nut_ghost_rows_amd_vreman(self, nu_t):
+        g, p = self.g, self.p
+        per_x(nu_t, g, 2)
+        per_z(nu_t, g, 4)
+        if p.Dirichlet_nu_t == 1:
+            dir_y(nu_t, g, 2)
+        elif p.Dirichlet_nu_t == 0:
+            neu_y(nu_t, g, 2)
+        elif p.Dirichlet_nu_t == 2:
+            c = 2.0 * 0.38 * self.dPdx ** 0.5 * (g.y[2] - g.y[1]) / 2.0
+            nu_t[:, 1, :] = -nu_t[:, 2, :] + c
+            nu_t[:, g.nyg, :] = -nu_t[:, g.nyg - 1, :] + c
+        return nu_t
+
+    # -- anisotropic minimum dissipation (subgrid.f90:632-874) ---------------
+    def sgs_AMD(self):
+        """nu_t = max(0, -C sum_k (d^_k u_i)(d^_k u_j) S_ij / (d_k u_l)^2), C = 0.3,
+        restated statement by statement: d^ are grid-scaled differences
+        interpolated to centres in the reference's order; the interior centres
+        (the only ones that survive the ghost-row rules) are evaluated."""
+        g = self.g
+        nx, ny, nz, nxg, nyg, nzg = g.nx, g.ny, g.nz, g.nxg, g.nyg, g.nzg
+        x, y, z, xg, yg, zg = g.x, g.y, g.z, g.xg, g.yg, g.zg
+        U, V, W = self.U, self.V, self.W
+        Cp = 0.3
+        Sij, _ = self.compute_Sij(U, V, W)
+        S = [None] + [Sij[:, :, :, m] for m in range(1, 7)]
+        sh = (nxg + 1, nyg + 1, nzg + 1)
+        t, t1, t2, t3, t4 = (np.zeros(sh) for _ in range(5))
+        B = (slice(2, nxg), slice(2, nyg), slice(2, nzg))
+        nu = np.zeros(sh)
+        ax = _iavg
+        dyg = (yg[2:nyg + 1] - yg[1:nyg])[None, :, None]
+        dzg = (zg[2:nzg + 1] - zg[1:nzg])[None, None, :]
+        dxg = (xg[2:nxg + 1] - xg[1:nxg])[:, None, None]
+        # (d^ U)^2 S11 and (d U)^2 (subgrid.f90:650-681)
+        t2[2:nx + 1] = U[2:nx + 1] - U[1:nx]
+        t4[2:nx + 1] = (U[2:nx + 1] - U[1:nx]) ** 2.0 / ((x[2:nx + 1] - x[1:nx]) ** 2.0)[:, None, None]
+        nu[B] = t2[B] ** 2.0 * S[1][B]
+        t[1:nx + 1, 2:nyg + 1] = U[1:nx + 1, 2:nyg + 1] - U[1:nx + 1, 1:nyg]
+        t1[1:nx + 1, 2:nyg + 1] = t[1:nx + 1, 2:nyg + 1] / dyg
+        t2[2:nx + 1, 2:nyg + 1] = ax(t1[1:nx + 1, 2:nyg + 1], 0)
+        t3[2:nx + 1, 2:nyg] = ax(t2[2:nx + 1, 2:nyg + 1], 1)
+        t4 = t4 + t3 ** 2.0
+        t1[2:nx + 1, 2:nyg + 1] = ax(t[1:nx + 1, 2:nyg + 1], 0)
+        t2[2:nx + 1, 2:nyg] = ax(t1[2:nx + 1, 2:nyg + 1], 1)
+        nu[B] = nu[B] + t2[B] ** 2.0 * S[1][B]
+        t[1:nx + 1, :, 2:nzg + 1] = U[1:nx + 1, :, 2:nzg + 1] - U[1:nx + 1, :, 1:nzg]
+        t1[1:nx + 1, :, 2:nzg + 1] = t[1:nx + 1, :, 2:nzg + 1] / dzg
+        t2[2:nx + 1, :, 2:nzg + 1] = ax(t1[1:nx + 1, :, 2:nzg + 1], 0)
+        t3[2:nx + 1, :, 2:nzg] = ax(t2[2:nx + 1, :, 2:nzg + 1], 2)
+        t4 = t4 + t3 ** 2.0
+        t1[2:nx + 1, :, 2:nzg + 1] = ax(t[1:nx + 1, :, 2:nzg + 1], 0)
+        t2[2:nx + 1, :, 2:nzg] = ax(t1[2:nx + 1, :, 2:nzg + 1], 2)
+        nu[B] = nu[B] + t2[B] ** 2.0 * S[1][B]
+        # V (subgrid.f90:683-716)
+        t2[:, 2:ny + 1] = V[:, 2:ny + 1] - V[:, 1:ny]
+        t4[:, 2:ny + 1] = t4[:, 2:ny + 1] + t2[:, 2:ny + 1] ** 2.0 / ((y[2:ny + 1] - y[1:ny]) ** 2.0)[None, :, None]
+        nu[B] = nu[B] + t2[B] ** 2.0 * S[2][B]
+        t[2:nxg + 1, 1:ny + 1] = V[2:nxg + 1, 1:ny + 1] - V[1:nxg, 1:ny + 1]
+        t1[2:nxg + 1, 1:ny + 1] = t[2:nxg + 1, 1:ny + 1] / dxg
+        t2[2:nxg + 1, 2:ny + 1] = ax(t1[2:nxg + 1, 1:ny + 1], 1)
+        t3[2:nxg, 2:ny + 1] = ax(t2[2:nxg + 1, 2:ny + 1], 0)
+        t4 = t4 + t3 ** 2.0
+        t1[2:nxg + 1, 2:ny + 1] = ax(t[2:nxg + 1, 1:ny + 1], 1)
+        t2[2:nxg, 2:ny + 1] = ax(t1[2:nxg + 1, 2:ny + 1], 0)
+        nu[B] = nu[B] + t2[B] ** 2.0 * S[2][B]
+        t[:, 1:ny + 1, 2:nzg + 1] = V[:, 1:ny + 1, 2:nzg + 1] - V[:, 1:ny + 1, 1:nzg]
+        t1[:, 1:ny + 1, 2:nzg + 1] = t[:, 1:ny + 1, 2:nzg + 1] / dzg
+        t2[:, 2:ny + 1, 2:nzg + 1] = ax(t1[:, 1:ny + 1, 2:nzg + 1], 1)
+        t3[:, 2:ny + 1, 2:nzg] = ax(t2[:, 2:ny + 1, 2:nzg + 1], 2)
+        t4 = t4 + t3 ** 2.0
+        t1[:, 2:ny + 1, 2:nzg + 1] = ax(t[:, 1:ny + 1, 2:nzg + 1], 1)
+        t2[:, 2:ny + 1, 2:nzg] = ax(t1[:, 2:ny + 1, 2:nzg + 1], 2)
+        nu[B] = nu[B] + t2[B] ** 2.0 * S[2][B]
+        # W (subgrid.f90:718-749)
+        t2[:, :, 2:nz + 1] = (W[:, :, 2:nz + 1] - W[:, :, 1:nz]) ** 2.0
+        t4[:, :, 2:nz + 1] = t4[:, :, 2:nz + 1] + t2[:, :, 2:nz + 1] / ((z[2:nz + 1] - z[1:nz]) ** 2.0)[None, None, :]
+        nu[B] = nu[B] + t2[B] * S[3][B]
+        t[2:nxg + 1, :, 1:nz + 1] = W[2:nxg + 1, :, 1:nz + 1] - W[1:nxg, :, 1:nz + 1]
+        t1[2:nxg + 1, :, 1:nz + 1] = t[2:nxg + 1, :, 1:nz + 1] / dxg
+        t2[2:nxg + 1, :, 2:nz + 1] = ax(t1[2:nxg + 1, :, 1:nz + 1], 2)
+        t3[2:nxg, :, 2:nz + 1] = ax(t2[2:nxg + 1, :, 2:nz + 1], 0)
+        t4 = t4 + t3 ** 2.0
+        t1[2:nxg + 1, :, 2:nz + 1] = ax(t[2:nxg + 1, :, 1:nz + 1], 2)
+        t2[2:nxg, :, 2:nz + 1] = ax(t1[2:nxg + 1, :, 2:nz + 1], 0)
+        nu[B] = nu[B] + t2[B] ** 2.0 * S[3][B]
+        t[:, 2:nyg + 1, 1:nz + 1] = W[:, 2:nyg + 1, 1:nz + 1] - W[:, 1:nyg, 1:nz + 1]
+        t1[:, 2:nyg + 1, 1:nz + 1] = t[:, 2:nyg + 1, 1:nz + 1] / dyg
+        t2[:, 2:nyg + 1, 2:nz + 1] = ax(t1[:, 2:nyg + 1, 1:nz + 1], 2)
+        t3[:, 2:nyg, 2:nz + 1] = ax(t2[:, 2:nyg + 1, 2:nz + 1], 1)
+        t4 = t4 + t3 ** 2.0
+        t1[:, 2:nyg + 1, 2:nz + 1] = ax(t[:, 2:nyg + 1, 1:nz + 1], 2)
+        t2[:, 2:nyg, 2:nz + 1] = ax(t1[:, 2:nyg + 1, 2:nz + 1], 1)
+        nu[B] = nu[B] + t2[B] ** 2.0 * S[3][B]
+        nu = self._amd_cross_terms(nu, S, B)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            out = alloc(nxg, nyg, nzg)
+            out[B] = -Cp * nu[B] / t4[B]
+        out = np.maximum(out, 0.0)
+        self.nu_t = self._nut_ghost_rows_amd_vreman(out)
+        self.amd_terms = (nu, t4)
+        return self.nu_t
+
+    def _amd_cross_terms(self, nu, S, B):
+        """2 (d^_k u_i)(d^_k u_j) S_ij, i != j (subgrid.f90:751-851)."""
+        g = self.g
+        nx, ny, nz, nxg, nyg, nzg = g.nx, g.ny, g.nz, g.nxg, g.nyg, g.nzg
+        U, V, W = self.U, self.V, self.W
+        sh = (nxg + 1, nyg + 1, nzg + 1)
+        t, t1, t2 = (np.zeros(sh) for _ in range(3))
+        ax = _iavg
+        # S12: k = x, y, z
+        t[2:nxg + 1, 1:ny + 1] = V[2:nxg + 1, 1:ny + 1] - V[1:nxg, 1:ny + 1]
+        t1[2:nxg + 1, 2:ny + 1] = ax(t[2:nxg + 1, 1:ny + 1], 1)
+        t2[2:nxg, 2:ny + 1] = ax(t1[2:nxg + 1, 2:ny + 1], 0)
+        t1[2:nx + 1, 2:nyg] = t2[2:nx + 1, 2:nyg] * (U[2:nx + 1, 2:nyg] - U[1:nx, 2:nyg])
+        nu[B] = nu[B] + 2.0 * t1[B] * S[4][B]
+        t[1:nx + 1, 2:nyg + 1] = U[1:nx + 1, 2:nyg + 1] - U[1:nx + 1, 1:nyg]
+        t1[2:nx + 1, 2:nyg + 1] = ax(t[1:nx + 1, 2:nyg + 1], 0)
+        t2[2:nx + 1, 2:nyg] = ax(t1[2:nx + 1, 2:nyg + 1], 1)
+        t1[2:nxg, 2:ny + 1] = t2[2:nxg, 2:ny + 1] * (V[2:nxg, 2:ny + 1] - V[2:nxg, 1:ny])
+        nu[B] = nu[B] + 2.0 * t1[B] * S[4][B]
+        t[1:nx + 1, :, 2:nzg + 1] = U[1:nx + 1, :, 2:nzg + 1] - U[1:nx + 1, :, 1:nzg]
+        t1[2:nx + 1, :, 2:nzg + 1] = ax(t[1:nx + 1, :, 2:nzg + 1], 0)
+        t[:, 1:ny + 1, 2:nzg + 1] = V[:, 1:ny + 1, 2:nzg + 1] - V[:, 1:ny + 1, 1:nzg]
+        t2[:, 2:ny + 1, 2:nzg + 1] = ax(t[:, 1:ny + 1, 2:nzg + 1], 1)
+        t3 = t1 * t2
+        t1[2:nxg, 2:nyg, 2:nzg] = ax(t3[2:nxg, 2:nyg, 2:nzg + 1], 2)
+        nu[B] = nu[B] + 2.0 * t1[B] * S[4][B]
+        # S13: k = x, z, y
+        t[2:nxg + 1, :, 1:nz + 1] = W[2:nxg + 1, :, 1:nz + 1] - W[1:nxg, :, 1:nz + 1]
+        t1[2:nxg + 1, :, 2:nz + 1] = ax(t[2:nxg + 1, :, 1:nz + 1], 2)
+        t2[2:nxg, :, 2:nz + 1] = ax(t1[2:nxg + 1, :, 2:nz + 1], 0)
+        t1[2:nx + 1, 2:nyg] = t2[2:nx + 1, 2:nyg] * (U[2:nx + 1, 2:nyg] - U[1:nx, 2:nyg])
+        nu[B] = nu[B] + 2.0 * t1[B] * S[5][B]
+        t[1:nx + 1, :, 2:nzg + 1] = U[1:nx + 1, :, 2:nzg + 1] - U[1:nx + 1, :, 1:nzg]
+        t1[2:nx + 1, :, 2:nzg + 1] = ax(t[1:nx + 1, :, 2:nzg + 1], 0)
+        t2[2:nx + 1, :, 2:nzg] = ax(t1[2:nx + 1, :, 2:nzg + 1], 2)
+        t1[2:nxg, :, 2:nz + 1] = t2[2:nxg, :, 2:nz + 1] * (W[2:nxg, :, 2:nz + 1] - W[2:nxg, :, 1:nz])
+        nu[B] = nu[B] + 2.0 * t1[B] * S[5][B]
+        t[1:nx + 1, 2:nyg + 1] = U[1:nx + 1, 2:nyg + 1] - U[1:nx + 1, 1:nyg]
+        t1[2:nx + 1, 2:nyg + 1] = ax(t[1:nx + 1, 2:nyg + 1], 0)
+        t[:, 2:nyg + 1, 1:nz + 1] = W[:, 2:nyg + 1, 1:nz + 1] - W[:, 1:nyg, 1:nz + 1]
+        t2[:, 2:nyg + 1, 2:nz + 1] = ax(t[:, 2:nyg + 1, 1:nz + 1], 2)
+        t3 = t1 * t2
+        t1[2:nxg, 2:nyg, 2:nzg] = ax(t3[2:nxg, 2:nyg + 1, 2:nzg], 1)
+        nu[B] = nu[B] + 2.0 * t1[B] * S[5][B]
+        # S23: k = y, z, x
+        t[:, 2:nyg + 1, 1:nz + 1] = W[:, 2:nyg + 1, 1:nz + 1] - W[:, 1:nyg, 1:nz + 1]
+        t1[:, 2:nyg + 1, 2:nz + 1] = ax(t[:, 2:nyg + 1, 1:nz + 1], 2)
+        t2[:, 2:nyg, 2:nz + 1] = ax(t1[:, 2:nyg + 1, 2:nz + 1], 1)
+        t1[2:nxg, 2:ny + 1] = t2[2:nxg, 2:ny + 1] * (V[2:nxg, 2:ny + 1] - V[2:nxg, 1:ny])
+        nu[B] = nu[B] + 2.0 * t1[B] * S[6][B]
+        t[:, 1:ny + 1, 2:nzg + 1] = V[:, 1:ny + 1, 2:nzg + 1] - V[:, 1:ny + 1, 1:nzg]
+        t1[:, 2:ny + 1, 2:nzg + 1] = ax(t[:, 1:ny + 1, 2:nzg + 1], 1)
+        t2[:, 2:ny + 1, 2:nzg] = ax(t1[:, 2:ny + 1, 2:nzg + 1], 2)
+        t1[:, 2:nyg, 2:nz + 1] = t2[:, 2:nyg, 2:nz + 1] * (W[:, 2:nyg, 2:nz + 1] - W[:, 2:nyg, 1:nz])
+        nu[B] = nu[B] + 2.0 * t1[B] * S[6][B]
+        t[2:nxg + 1, 1:ny + 1] = V[2:nxg + 1, 1:ny + 1] - V[1:nxg, 1:ny + 1]
+        t1[2:nxg + 1, 2:ny + 1] = ax(t[2:nxg + 1, 1:ny + 1], 1)
+        t[2:nxg + 1, :, 1:nz + 1] = W[2:nxg + 1, :, 1:nz + 1] - W[1:nxg, :, 1:nz + 1]
+        t2[2:nxg + 1, :, 2:nz + 1] = ax(t[2:nxg + 1, :, 1:nz + 1], 2)
+        t3 = t1 * t2
+        t1[2:nxg, 2:nyg, 2:nzg] = ax(t3[2:nxg + 1, 2:nyg, 2:nzg], 0)
+        nu[B] = nu[B] + 2.0 * t1[B] * S[6][B]
+        return nu
+
+    # -- Vreman (subgrid.f90:897-1004) ---------------------------------------
+    def sgs_Vreman(self):
+        """nu_t = C sqrt(B_b / a_ij a_ij), C = 2.5 (0.1)^2, b_ij = sum_m d_m^2
+        a_mi a_mj with a_ij = du_j/dx_i at centres (off-diagonals: mean of the
+        four surrounding edge derivatives).  The U sections written 2:ny and
+        1:ny-1 where 2:nx and 1:nx-1 are meant (subgrid.f90:930-931,946-947)
+        start at the same index, so element-wise they read the intended U
+        values; that reading is restated here.  No clipping, as written."""
+        g = self.g
+        nxg, nyg, nzg = g.nxg, g.nyg, g.nzg
+        x, y, z, xg, yg, zg = g.x, g.y, g.z, g.xg, g.yg, g.zg
+        U, V, W = self.U, self.V, self.W
+        C = 2.5 * (0.1 ** 2.0)
+        I, J, K = slice(2, nxg), slice(2, nyg), slice(2, nzg)      # 2..n?g-1
+        Ip, Jp, Kp = slice(3, nxg + 1), slice(3, nyg + 1), slice(3, nzg + 1)
+        Im, Jm, Km = slice(1, nxg - 1), slice(1, nyg - 1), slice(1, nzg - 1)
+        dxl = (xg[2:nxg] - xg[1:nxg - 1])[:, None, None]            # xg(i)-xg(i-1)
+        dxr = (xg[3:nxg + 1] - xg[2:nxg])[:, None, None]            # xg(i+1)-xg(i)
+        dyl = (yg[2:nyg] - yg[1:nyg - 1])[None, :, None]
+        dyr = (yg[3:nyg + 1] - yg[2:nyg])[None, :, None]
+        dzl = (zg[2:nzg] - zg[1:nzg - 1])[None, None, :]
+        dzr = (zg[3:nzg + 1] - zg[2:nzg])[None, None, :]
+        a = [None] * 10
+        a[1] = (U[I, J, K] - U[Im, J, K]) / (x[2:nxg] - x[1:nxg - 1])[:, None, None]
+        a[4] = (0.25 * (V[I, J, K] - V[Im, J, K]) / dxl + 0.25 * (V[I, Jm, K] - V[Im, Jm, K]) / dxl
+                + 0.25 * (V[Ip, J, K] - V[I, J, K]) / dxr + 0.25 * (V[Ip, Jm, K] - V[I, Jm, K]) / dxr)
+        a[5] = (0.25 * (W[I, J, K] - W[Im, J, K]) / dxl + 0.25 * (W[I, J, Km] - W[Im, J, Km]) / dxl
+                + 0.25 * (W[Ip, J, K] - W[I, J, K]) / dxr + 0.25 * (W[Ip, J, Km] - W[I, J, Km]) / dxr)
+        a[2] = (V[I, J, K] - V[I, Jm, K]) / (y[2:nyg] - y[1:nyg - 1])[None, :, None]
+        a[7] = (0.25 * (U[I, J, K] - U[I, Jm, K]) / dyl + 0.25 * (U[Im, J, K] - U[Im, Jm, K]) / dyl
+                + 0.25 * (U[I, Jp, K] - U[I, J, K]) / dyr + 0.25 * (U[Im, Jp, K] - U[Im, J, K]) / dyr)
+        a[6] = (0.25 * (W[I, J, K] - W[I, Jm, K]) / dyl + 0.25 * (W[I, J, Km] - W[I, Jm, Km]) / dyl
+                + 0.25 * (W[I, Jp, K] - W[I, J, K]) / dyr + 0.25 * (W[I, Jp, Km] - W[I, J, Km]) / dyr)
+        a[3] = (W[I, J, K] - W[I, J, Km]) / (z[2:nzg] - z[1:nzg - 1])[None, None, :]
+        a[8] = (0.25 * (U[I, J, K] - U[I, J, Km]) / dzl + 0.25 * (U[Im, J, K] - U[Im, J, Km]) / dzl
+                + 0.25 * (U[I, J, Kp] - U[I, J, K]) / dzr + 0.25 * (U[Im, J, Kp] - U[Im, J, K]) / dzr)
+        a[9] = (0.25 * (V[I, J, K] - V[I, J, Km]) / dzl + 0.25 * (V[I, Jm, K] - V[I, Jm, Km]) / dzl
+                + 0.25 * (V[I, J, Kp] - V[I, J, K]) / dzr + 0.25 * (V[I, Jm, Kp] - V[I, Jm, K]) / dzr)
+        ddx = ((x[2:nxg] - x[1:nxg - 1]) ** 2.0)[:, None, None]
+        ddy = ((y[2:nyg] - y[1:nyg - 1]) ** 2.0)[None, :, None]
+        ddz = ((z[2:nzg] - z[1:nzg - 1]) ** 2.0)[None, None, :]
+        # b_ij components 1..6 = (11, 22, 33, 12, 13, 23); a layout (1 4 5; 7 2 6; 8 9 3)
+        px = {1: (1, 1), 2: (4, 4), 3: (5, 5), 4: (1, 4), 5: (1, 5), 6: (4, 5)}
+        py = {1: (7, 7), 2: (2, 2), 3: (6, 6), 4: (7, 2), 5: (7, 6), 6: (2, 6)}
+        pz = {1: (8, 8), 2: (9, 9), 3: (3, 3), 4: (8, 9), 5: (8, 3), 6: (9, 3)}
+        b = {}
+        for m in range(1, 7):
+            b[m] = 0.0 + ddx * a[px[m][0]] * a[px[m][1]]
+            b[m] = b[m] + ddy * a[py[m][0]] * a[py[m][1]]
+            b[m] = b[m] + ddz * a[pz[m][0]] * a[pz[m][1]]
+        Bb = (b[1] * b[2] - b[4] ** 2.0 + b[1] * b[3] - b[5] ** 2.0 + b[2] * b[3] - b[6] ** 2.0)
+        Ab = a[1] ** 2.0
+        for m in range(2, 10):
+            Ab = Ab + a[m] ** 2.0
+        out = alloc(nxg, nyg, nzg)
+        with np.errstate(divide="ignore", invalid="ignore"):
+            out[I, J, K] = C * (Bb / Ab) ** 0.5
+        self.vreman_terms = (Bb, Ab)
+        self.nu_t = self._nut_ghost_rows_amd_vreman(out)
+        return self.nu_t
+
     def compute_eddy_viscosity(self):
         """subgrid.f90:23-47."""
         if self.p.LES_model == LES_SMAG:
             return self.sgs_Smagorinsky()
         if self.p.LES_model == LES_DSM:
             return self.sgs_dynamic_Smagorinsky()
+        if self.p.LES_model == LES_AMD:
+            return self.sgs_AMD()
+        if self.p.LES_model == LES_VREMAN:
+            return self.sgs_Vreman()
         self.nu_t = alloc(self.g.nxg, self.g.nyg, self.g.nzg)
         return self.nu_t
 

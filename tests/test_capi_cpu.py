@@ -61,6 +61,8 @@ def _create(lib, case, mutate=None):
     (lambda d: setattr(d, "nx", 35), "even"),
     (lambda d: setattr(d, "nz", 4), "even"),
     (lambda d: setattr(d, "LES_model", 7), "LES_model"),
+    (lambda d: setattr(d, "LES_model", 5), "LES_model"),
+    (lambda d: setattr(d, "Dirichlet_nu_t", 3), "Dirichlet_nu_t"),
 ])
 def test_invalid_grid_rejected_without_gpu(lib, mutate, needle):
     rc, msg = _create(lib, CS.c1_small(), mutate)

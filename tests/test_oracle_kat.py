@@ -159,3 +159,43 @@ def test_rk3_step_keeps_mass_flow_constant():
         o.step()
         assert abs(o.compute_dPx_for_constant_mass_flow()) < 1e-12
         assert o.check_divergence()[1] < 1e-12
+
+
+def _linear_field_oracle(model, a=0.7):
+    """Uniform 16x12x8 grid, u = a x, v = -a y, w = 0 (no boundary conditions
+    applied: the SGS routines read the arrays as given)."""
+    case = C.Case(name="kat", Nx=16, Ny=12, Nz=8, Lx=2.0, Lz=1.0)
+    g = R.Grid(*C.faces(case))
+    o = R.ChannelOracle(g, R.Params(nu=1e-3, LES_model=model, Dirichlet_nu_t=0))
+    o.U[1:, 1:, 1:] = a * g.x[1:, None, None]
+    o.V[1:, 1:, 1:] = -a * g.y[None, 1:, None]
+    o.W[...] = 0.0
+    return o, g, 2.0 / 16, 2.0 / 12
+
+
+def test_amd_pure_strain_known_answer():
+    """AMD on u = a x, v = -a y: N = a^3 (dx^2 - dy^2), D = 2 a^2, so
+    nu_t = 0.15 a (dy^2 - dx^2) (subgrid.f90:632-874, C = 0.3)."""
+    a = 0.7
+    o, g, dx, dy = _linear_field_oracle(R.LES_AMD, a)
+    nt = o.compute_eddy_viscosity()[2:g.nxg - 1, 2:g.nyg, 2:g.nzg - 1]
+    assert np.allclose(nt, 0.15 * a * (dy * dy - dx * dx), rtol=1e-13, atol=0)
+
+
+def test_vreman_pure_strain_known_answer():
+    """Vreman on u = a x, v = -a y: B_b = dx^2 dy^2 a^4, a_ij a_ij = 2 a^2,
+    nu_t = C dx dy |a| / sqrt(2), C = 2.5 * 0.1^2 (subgrid.f90:897-1004)."""
+    a = 0.7
+    o, g, dx, dy = _linear_field_oracle(R.LES_VREMAN, a)
+    nt = o.compute_eddy_viscosity()[2:g.nxg - 1, 2:g.nyg, 2:g.nzg - 1]
+    assert np.allclose(nt, 0.025 * dx * dy * a / math.sqrt(2.0), rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("model", [3, 4])
+def test_amd_and_vreman_vanish_in_pure_shear(model):
+    """Both models are built to give no eddy viscosity in a pure shear u(y)."""
+    o, g, _, _ = _linear_field_oracle(model)
+    o.U[1:, 1:, 1:] = 0.3 * g.yg[None, 1:, None]
+    o.V[...] = 0.0
+    nt = o.compute_eddy_viscosity()[2:g.nxg - 1, 2:g.nyg, 2:g.nzg - 1]
+    assert np.abs(nt).max() == 0.0
