@@ -52,6 +52,10 @@ class Case:
     init: str = "laminar"
     amp: float = 0.1
     seed: int = 1234
+    # explicit face coordinates (e.g. from a snapshot file); None: built from Lx, Lz, stretch
+    xf: tuple | None = None
+    yf: tuple | None = None
+    zf: tuple | None = None
 
     # Fortran extents
     @property
@@ -139,7 +143,11 @@ def c5_learned(n=16, seed=5555):
 
 def faces(case: Case):
     """Face coordinates x(1:nx), y(1:ny), z(1:nz) as the reference's grid
-    arrays (global.f90:63-67): x(i) = (i-1) Lx/Nx so that x(nx-1) = Lx."""
+    arrays (global.f90:63-67): x(i) = (i-1) Lx/Nx so that x(nx-1) = Lx,
+    unless the case carries explicit coordinates."""
+    if case.xf is not None:
+        return (np.array(case.xf, dtype=np.float64), np.array(case.yf, dtype=np.float64),
+                np.array(case.zf, dtype=np.float64))
     dx = case.Lx / case.Nx
     dz = case.Lz / case.Nz
     x = np.arange(case.nx, dtype=np.float64) * dx
@@ -201,3 +209,26 @@ def initial_fields(case: Case):
 def smaller(case: Case, Nx, Ny, Nz):
     """Same physics on another grid (used for quick parity cases)."""
     return replace(case, Nx=Nx, Ny=Ny, Nz=Nz, name=f"{case.name}_as_{Nx}x{Ny}x{Nz}")
+
+
+def case_from_files(params_path, snapshot_path=None, wall_model=WM_STRESS, Cs=0.1, Retau=0.0):
+    """A case and its initial fields from the reference's own files: the
+    parameter file (read_input_parameters, input_output.f90:20-91) and the
+    snapshot it names (read_input_data, input_output.f90:390-560; resolved
+    against the parameter file's folder unless given).  The parameter file
+    has no wall-model entry (the reference always calls compute_wall_model
+    with the alpha_x its RL driver sets), hence the argument."""
+    import os
+    from .host import read_parameters, read_snapshot
+    p = read_parameters(params_path)
+    path = snapshot_path or os.path.join(os.path.dirname(os.path.abspath(params_path)), p["filein"])
+    snap = read_snapshot(path)
+    if (snap["x"].size, snap["y"].size, snap["z"].size) != (p["nx"], p["ny"], p["nz"]):
+        raise ValueError("snapshot extents differ from the parameter file")
+    x, y, z = snap["x"], snap["y"], snap["z"]
+    case = Case(name=os.path.basename(path), Nx=p["nx"] - 2, Ny=p["ny"] - 1, Nz=p["nz"] - 2,
+                Lx=float(x[-2] - x[0]), Lz=float(z[-2] - z[0]), nu=p["nu"], CFL=p["CFL"], dPdx=p["dPdx"],
+                x_mass_cte=p["x_mass_cte"], LES_model=p["LES_model"], Dirichlet_nu_t=p["Dirichlet_nu_t"],
+                wall_model=wall_model, Cs=Cs, Retau=Retau, init="file",
+                xf=tuple(x.tolist()), yf=tuple(y.tolist()), zf=tuple(z.tolist()))
+    return case, (snap["U"], snap["V"], snap["W"]), p

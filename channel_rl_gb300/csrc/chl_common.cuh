@@ -36,6 +36,7 @@ struct ChlInst {
   const double *rdxc, *rdxf, *rdyc, *rdyf, *rdzc, *rdzf;
   const double *dxf, *dyf, *dzf;  // raw spacings (dt)
   const double *w0, *w1;          // weight_y_0/1 by face row jv
+  const double *ygc;              // yg(1..nyg), centre y coordinates with the ghost rows
   const double *smag_csdelta;     // Cs*Delta_j by centre row (static Smagorinsky)
   const double *smag_dwall;       // distance of centre row to the nearer wall (van Driest)
   // Fourier / tridiagonal

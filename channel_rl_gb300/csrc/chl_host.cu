@@ -28,6 +28,7 @@ void chl_launch_eqwm(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_nut(const ChlMap&, int, int, int, cudaStream_t);
 void chl_launch_amd(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_vreman(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_agent_obs(const ChlInst*, int, int, double, const int*, const double*, double*, double*, cudaStream_t);
 size_t chl_smem_fftx(int);
 size_t chl_smem_fftz(int);
 int chl_fft_setup(size_t, size_t);
@@ -207,6 +208,8 @@ struct chl_handle {
   int* d_mlp_status = nullptr;
   double* d_divout = nullptr;
   double* d_stats = nullptr;
+  double* d_agent = nullptr;          // wall-agent observations: inputs and outputs
+  size_t agent_cap = 0;
   int stats_pitch = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -236,7 +239,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   size_t o_rdxc = A.take(8 * (Nx + 3)), o_rdxf = A.take(8 * (Nx + 3)), o_dxf = A.take(8 * (Nx + 3));
   size_t o_rdzc = A.take(8 * (Nz + 3)), o_rdzf = A.take(8 * (Nz + 3)), o_dzf = A.take(8 * (Nz + 3));
   size_t o_rdyc = A.take(8 * (Ny + 2)), o_rdyf = A.take(8 * (Ny + 2)), o_dyf = A.take(8 * (Ny + 2));
-  size_t o_w0 = A.take(8 * (Ny + 2)), o_w1 = A.take(8 * (Ny + 2));
+  size_t o_w0 = A.take(8 * (Ny + 2)), o_w1 = A.take(8 * (Ny + 2)), o_ygc = A.take(8 * (Ny + 2));
   size_t o_csd = A.take(8 * (Ny + 2)), o_dw = A.take(8 * (Ny + 2));
   size_t o_twx = A.take(16 * Nx), o_twz = A.take(16 * Nz);
   size_t o_ti = A.take(8 * ntri), o_tm = A.take(8 * ntri), o_tc = A.take(8 * ntri);
@@ -287,7 +290,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.mass_norm = 1.0 / ((double)Nx * Nz);
   D.rdxc = P(o_rdxc) + 1; D.rdxf = P(o_rdxf) + 1; D.dxf = P(o_dxf) + 1;
   D.rdzc = P(o_rdzc) + 1; D.rdzf = P(o_rdzf) + 1; D.dzf = P(o_dzf) + 1;
-  D.rdyc = P(o_rdyc); D.rdyf = P(o_rdyf); D.dyf = P(o_dyf); D.w0 = P(o_w0); D.w1 = P(o_w1);
+  D.rdyc = P(o_rdyc); D.rdyf = P(o_rdyf); D.dyf = P(o_dyf); D.w0 = P(o_w0); D.w1 = P(o_w1); D.ygc = P(o_ygc);
   D.smag_csdelta = P(o_csd); D.smag_dwall = P(o_dw);
   D.twx = (const double2*)(base + o_twx); D.twz = (const double2*)(base + o_twz);
   D.tri_inv = P(o_ti); D.tri_m = P(o_tm); D.tri_c = P(o_tc);
@@ -310,6 +313,8 @@ static int upload_consts(chl_handle* h, Inst& I) {
   CK(put(o_rdxc, c.rdxc)); CK(put(o_rdxf, c.rdxf)); CK(put(o_dxf, c.dxf));
   CK(put(o_rdzc, c.rdzc)); CK(put(o_rdzf, c.rdzf)); CK(put(o_dzf, c.dzf));
   CK(put(o_rdyc, c.rdyc)); CK(put(o_rdyf, c.rdyf)); CK(put(o_dyf, c.dyf));
+  const std::vector<double> ygc(c.yg.begin() + 1, c.yg.begin() + 1 + c.nyg);
+  CK(put(o_ygc, ygc));
   CK(put(o_w0, c.w0)); CK(put(o_w1, c.w1)); CK(put(o_csd, c.csdelta)); CK(put(o_dw, c.dwall));
   const double pi = 4.0 * std::atan(1.0);
   std::vector<double> tw(2 * (size_t)std::max(Nx, Nz));
@@ -574,6 +579,7 @@ int chl_destroy(chl_handle* h) {
   if (h->d_inst) cudaFree(h->d_inst);
   if (h->d_divout) cudaFree(h->d_divout);
   if (h->d_stats) cudaFree(h->d_stats);
+  if (h->d_agent) cudaFree(h->d_agent);
   if (h->d_mlp_theta) cudaFree(h->d_mlp_theta);
   if (h->d_mlp_cfg) cudaFree(h->d_mlp_cfg);
   if (h->d_mlp_status) cudaFree(h->d_mlp_status);
@@ -636,6 +642,38 @@ int chl_download(chl_handle* h, int inst, double* U, double* V, double* W, doubl
   return CHL_OK;
 }
 
+int chl_save_snapshot(chl_handle* h, int inst, const char* path, int with_pressure) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !path) return CHL_E_ARG;
+  const Consts& c = I->c;
+  int rc;
+  if (with_pressure && (rc = chl_compute_pressure(h))) return rc;
+  std::vector<double> U((size_t)c.nx * c.nyg * c.nzg), V((size_t)c.nxg * c.ny * c.nzg), W((size_t)c.nxg * c.nyg * c.nz);
+  std::vector<double> P, nt;
+  if (with_pressure) { P.resize((size_t)c.nxg * c.nyg * c.nzg); nt.resize(P.size()); }
+  if ((rc = chl_download(h, inst, U.data(), V.data(), W.data(), with_pressure ? P.data() : nullptr,
+                         with_pressure ? nt.data() : nullptr))) return rc;
+  rc = chl_snapshot_write(path, c.nx, c.ny, c.nz, c.xf.data() + 1, c.yf.data() + 1, c.zf.data() + 1,
+                          U.data(), V.data(), W.data(), with_pressure ? P.data() : nullptr,
+                          with_pressure ? nt.data() : nullptr);
+  if (rc) h->err = chl_io_last_error();
+  return rc;
+}
+
+int chl_load_snapshot(chl_handle* h, int inst, const char* path) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !path) return CHL_E_ARG;
+  const Consts& c = I->c;
+  std::vector<double> x(c.nx), y(c.ny), z(c.nz);
+  std::vector<double> U((size_t)c.nx * c.nyg * c.nzg), V((size_t)c.nxg * c.ny * c.nzg), W((size_t)c.nxg * c.nyg * c.nz);
+  int rc = chl_snapshot_read(path, c.nx, c.ny, c.nz, x.data(), y.data(), z.data(), U.data(), V.data(), W.data());
+  if (rc) { h->err = chl_io_last_error(); return rc; }
+  for (int i = 0; i < c.nx; ++i) if (x[i] != c.xf[i + 1]) { h->err = "snapshot: x mesh differs from the instance"; return CHL_E_ARG; }
+  for (int j = 0; j < c.ny; ++j) if (y[j] != c.yf[j + 1]) { h->err = "snapshot: y mesh differs from the instance"; return CHL_E_ARG; }
+  for (int k = 0; k < c.nz; ++k) if (z[k] != c.zf[k + 1]) { h->err = "snapshot: z mesh differs from the instance"; return CHL_E_ARG; }
+  return chl_upload(h, inst, U.data(), V.data(), W.data());
+}
+
 int chl_download_pseudo_pressure(chl_handle* h, int inst, double* p) {
   Inst* I = get_inst(h, inst);
   if (!I || !p) return CHL_E_ARG;
@@ -672,6 +710,73 @@ int chl_get_wall_stress(chl_handle* h, int inst, double* a) {
         a[(size_t)i1 + (size_t)c.nx * ((size_t)w + 2 * (size_t)k1)] = al[((size_t)w * c.Nz + k) * c.Nx + i];
       }
   return CHL_OK;
+}
+
+// ------------------------------------------------------------ wall agents (smarties_stat.f90:24-260)
+static int agent_check(chl_handle* h, Inst* I, int nagents) {
+  if (nagents < 1 || I->c.Nx % nagents) { h->err = "agents: nagents must divide Nx = nx-2"; return CHL_E_ARG; }
+  if (I->c.Ny < 8) { h->err = "agents: Ny >= 8 needed"; return CHL_E_ARG; }
+  return CHL_OK;
+}
+
+int chl_agent_observe(chl_handle* h, int inst, int nagents, const int* y_ind, const double* y_rand,
+                      double* states, double* rewards) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !y_ind || !y_rand || !states || !rewards) return CHL_E_ARG;
+  int rc = agent_check(h, I, nagents); if (rc) return rc;
+  const int n = 2 * nagents;
+  for (int t = 0; t < n; ++t)
+    if ((y_ind[t] != 3 && y_ind[t] != 4) || !(y_rand[t] >= 0.0 && y_rand[t] <= 1.0)) {
+      h->err = "agents: y_ind must be 3 or 4 and y_rand in [0, 1]"; return CHL_E_ARG;
+    }
+  // buffer: y_rand[n], states[6n], rewards[n], y_ind[n] (as int)
+  const size_t need = (size_t)8 * n + 8 * (size_t)n * 6 + 8 * (size_t)n + 4 * (size_t)n;
+  if (need > h->agent_cap) {
+    if (h->d_agent) { cudaFree(h->d_agent); h->d_agent = nullptr; h->agent_cap = 0; }
+    CK(cudaMalloc(&h->d_agent, need));
+    h->agent_cap = need;
+  }
+  double* d_r = h->d_agent;
+  double* d_s = d_r + n;
+  double* d_w = d_s + 6 * (size_t)n;
+  int* d_y = reinterpret_cast<int*>(d_w + n);
+  CK(cudaMemcpyAsync(d_r, y_rand, 8 * (size_t)n, cudaMemcpyHostToDevice, h->st));
+  CK(cudaMemcpyAsync(d_y, y_ind, 4 * (size_t)n, cudaMemcpyHostToDevice, h->st));
+  chl_launch_agent_obs(h->d_inst + inst, nagents, I->c.Nx / nagents, I->d.dPdx, d_y, d_r, d_s, d_w, h->st);
+  LAUNCHED();
+  CK(cudaMemcpyAsync(states, d_s, 8 * 6 * (size_t)n, cudaMemcpyDeviceToHost, h->st));
+  CK(cudaMemcpyAsync(rewards, d_w, 8 * (size_t)n, cudaMemcpyDeviceToHost, h->st));
+  return finish(h);
+}
+
+int chl_agent_act(chl_handle* h, int inst, int nagents, const double* action) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !action) return CHL_E_ARG;
+  int rc = agent_check(h, I, nagents); if (rc) return rc;
+  const Consts& c = I->c;
+  const int Nx = c.Nx, Nz = c.Nz, nxa = Nx / nagents;
+  std::vector<double> al(2 * (size_t)Nx * Nz);
+  CK(cudaMemcpyAsync(al.data(), I->dev.alpha, 8 * al.size(), cudaMemcpyDeviceToHost, h->st));
+  if ((rc = finish(h))) return rc;
+  // actions(iwall,na) = alpha_x((na-1)*nx_nagents+2, iwall, 2) * action
+  std::vector<double> act(2 * (size_t)nagents);
+  for (int w = 0; w < 2; ++w)
+    for (int na = 0; na < nagents; ++na)
+      act[(size_t)w * nagents + na] = al[(size_t)w * Nz * Nx + (size_t)na * nxa] * action[(size_t)w * nagents + na];
+  // linear in x between neighbouring agents, the last one towards the first;
+  // then the z "interpolation" between planes 2 and nzg, which hold the same value
+  for (int w = 0; w < 2; ++w)
+    for (int na = 0; na < nagents; ++na) {
+      const double a0 = act[(size_t)w * nagents + na], a1 = act[(size_t)w * nagents + (na + 1) % nagents];
+      for (int j = 1; j <= nxa; ++j) {
+        const double ax = (a0 * (double)(nxa - j + 1)) / (double)nxa + (a1 * (double)(j - 1)) / (double)nxa;
+        const int i = na * nxa + (j - 1);
+        for (int k = 0; k < Nz; ++k)
+          al[((size_t)w * Nz + k) * Nx + i] = (ax * (double)(Nz - k)) / (double)Nz + (ax * (double)k) / (double)Nz;
+      }
+    }
+  CK(cudaMemcpyAsync(I->dev.alpha, al.data(), 8 * al.size(), cudaMemcpyHostToDevice, h->st));
+  return finish(h);
 }
 
 int chl_get_scalars(chl_handle* h, int inst, double* out4) {

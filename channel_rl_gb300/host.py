@@ -38,6 +38,16 @@ class GridDesc(C.Structure):
                 ("wall_model", C.c_int), ("Cs", C.c_double), ("Re_tau", C.c_double)]
 
 
+class ParamsOut(C.Structure):
+    """chl_parameters: the reference's parameter file (input_output.f90:20-91)."""
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("CFL", C.c_double), ("nu", C.c_double), ("dPdx", C.c_double),
+                ("x_mass_cte", C.c_int), ("LES_model", C.c_int),
+                ("nsteps", C.c_int), ("nsave", C.c_int), ("nstats", C.c_int), ("nmonitor", C.c_int),
+                ("filein", C.c_char * 256), ("fileout", C.c_char * 256),
+                ("nstep_init", C.c_int), ("random_init", C.c_int), ("Dirichlet_nu_t", C.c_int)]
+
+
 class StatsOut(C.Structure):
     _fields_ = [(n, C.c_double) for n in
                 ("utau", "Retau", "tau_wall", "Qflow_x", "Qflow_y", "dt", "t", "dPdx",
@@ -58,6 +68,9 @@ EXPORTS = (
     "chl_check_divergence_noalloc", "chl_noalloc_last_error",
     "chl_mlp_set_params", "chl_mlp_get_params", "chl_mlp_configure", "chl_mlp_read_trace",
     "chl_mlp_eval", "chl_tc_selftest",
+    "chl_snapshot_dims", "chl_snapshot_read", "chl_snapshot_write", "chl_io_last_error",
+    "chl_read_parameters", "chl_save_snapshot", "chl_load_snapshot",
+    "chl_agent_observe", "chl_agent_act",
 )
 MLP_NPARAM = 4545
 _F32P = C.POINTER(C.c_float)
@@ -115,6 +128,16 @@ def load(build_if_missing=True):
     lib.chl_mlp_read_trace.argtypes = [H, C.c_int, _F32P, C.c_int]
     lib.chl_mlp_eval.argtypes = [H, _F32P, _F32P, C.c_int, _F32P, _F32P]
     lib.chl_tc_selftest.argtypes = [C.POINTER(C.c_ushort), C.POINTER(C.c_ushort), _F32P, C.c_int]
+    I = C.POINTER(C.c_int)
+    lib.chl_snapshot_dims.argtypes = [C.c_char_p, I, I, I]
+    lib.chl_snapshot_read.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int] + [_F64P] * 6
+    lib.chl_snapshot_write.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int] + [_F64P] * 8
+    lib.chl_io_last_error.restype = C.c_char_p
+    lib.chl_read_parameters.argtypes = [C.c_char_p, C.POINTER(ParamsOut)]
+    lib.chl_save_snapshot.argtypes = [H, C.c_int, C.c_char_p, C.c_int]
+    lib.chl_load_snapshot.argtypes = [H, C.c_int, C.c_char_p]
+    lib.chl_agent_observe.argtypes = [H, C.c_int, C.c_int, I, _F64P, _F64P, _F64P]
+    lib.chl_agent_act.argtypes = [H, C.c_int, C.c_int, _F64P]
     _LIB = lib
     return lib
 
@@ -139,6 +162,63 @@ def grid_desc(case: Case, keep: list):
     return GridDesc(case.nx, case.ny, case.nz, _ptr(x), _ptr(y), _ptr(z), case.nu, case.CFL,
                     case.dPdx, case.x_mass_cte, case.LES_model, case.Dirichlet_nu_t, case.wall_model,
                     case.Cs, case.Retau)
+
+
+def _io_check(rc, what):
+    if rc:
+        raise ChlError(f"{what} failed ({rc}): {load().chl_io_last_error().decode()}")
+
+
+def snapshot_dims(path):
+    """(nx, ny, nz) face counts of a snapshot file."""
+    n = [C.c_int(0) for _ in range(3)]
+    _io_check(load().chl_snapshot_dims(os.fsencode(path), *(C.byref(v) for v in n)), "chl_snapshot_dims")
+    return tuple(v.value for v in n)
+
+
+def read_snapshot(path):
+    """Mesh and fields of a snapshot in the reference's stream layout
+    (read_input_data, input_output.f90:390-560): x, y, z and Fortran-ordered
+    U(nx,nyg,nzg), V(nxg,ny,nzg), W(nxg,nyg,nz)."""
+    nx, ny, nz = snapshot_dims(path)
+    x, y, z = np.zeros(nx), np.zeros(ny), np.zeros(nz)
+    U = np.zeros((nx, ny + 1, nz + 1), order="F")
+    V = np.zeros((nx + 1, ny, nz + 1), order="F")
+    W = np.zeros((nx + 1, ny + 1, nz), order="F")
+    _io_check(load().chl_snapshot_read(os.fsencode(path), nx, ny, nz, *(_ptr(a) for a in (x, y, z)),
+                                       *(a.ctypes.data_as(_F64P) for a in (U, V, W))), "chl_snapshot_read")
+    return {"x": x, "y": y, "z": z, "U": U, "V": V, "W": W}
+
+
+def write_snapshot(path, x, y, z, U, V, W, P=None, nu_t=None):
+    """Write a snapshot as output_data does (input_output.f90:593-730);
+    without P and nu_t it is an initial-field file."""
+    x, y, z = (np.ascontiguousarray(a, dtype=np.float64) for a in (x, y, z))
+    nx, ny, nz = x.size, y.size, z.size
+    shapes = {"U": (nx, ny + 1, nz + 1), "V": (nx + 1, ny, nz + 1), "W": (nx + 1, ny + 1, nz),
+              "P": (nx + 1, ny + 1, nz + 1), "nu_t": (nx + 1, ny + 1, nz + 1)}
+    arrs = []
+    for name, a in (("U", U), ("V", V), ("W", W), ("P", P), ("nu_t", nu_t)):
+        if a is None:
+            arrs.append(None)
+            continue
+        a = np.asfortranarray(a, dtype=np.float64)
+        if a.shape != shapes[name]:
+            raise ValueError(f"{name}: shape {a.shape} != {shapes[name]}")
+        arrs.append(a)
+    ptrs = [a.ctypes.data_as(_F64P) if a is not None else None for a in arrs]
+    _io_check(load().chl_snapshot_write(os.fsencode(path), nx, ny, nz, _ptr(x), _ptr(y), _ptr(z), *ptrs),
+              "chl_snapshot_write")
+
+
+def read_parameters(path):
+    """The reference's parameter file (read_input_parameters, input_output.f90:20-91) as a dict."""
+    p = ParamsOut()
+    _io_check(load().chl_read_parameters(os.fsencode(path), C.byref(p)), "chl_read_parameters")
+    out = {n: getattr(p, n) for n, _ in ParamsOut._fields_}
+    out["filein"] = p.filein.decode()
+    out["fileout"] = p.fileout.decode()
+    return out
 
 
 def _f32(a):
@@ -224,6 +304,35 @@ class Channel:
                 raise ValueError(f"{f} has shape {a.shape}, expected {self._shape(inst, f)}")
         rc = self.lib.chl_upload(self.h, inst, *[_ptr(a) for a in arrs])
         self._check(rc, "chl_upload")
+
+    def save_snapshot(self, path, inst=0, with_pressure=True):
+        """output_data (input_output.f90:593-730) of one instance: mesh, U, V,
+        W and, with the actual pressure computed first, P and nu_t."""
+        self._check(self.lib.chl_save_snapshot(self.h, inst, os.fsencode(path), int(bool(with_pressure))),
+                    "chl_save_snapshot")
+
+    def load_snapshot(self, path, inst=0):
+        """read_input_data (input_output.f90:390-560) into one instance; the
+        file's mesh must be the instance's."""
+        self._check(self.lib.chl_load_snapshot(self.h, inst, os.fsencode(path)), "chl_load_snapshot")
+
+    def agent_observe(self, nagents, y_ind, y_rand, inst=0):
+        """States [2][nagents][6] and rewards [2][nagents] of the wall agents
+        (send_recv_state_action, smarties_stat.f90:24-176) for given sampling
+        rows y_ind (3 or 4) and weights y_rand, both [2][nagents]."""
+        yi = np.ascontiguousarray(y_ind, dtype=np.int32).reshape(2, nagents)
+        yr = np.ascontiguousarray(y_rand, dtype=np.float64).reshape(2, nagents)
+        st = np.zeros((2, nagents, 6))
+        rw = np.zeros((2, nagents))
+        self._check(self.lib.chl_agent_observe(self.h, inst, nagents, yi.ctypes.data_as(C.POINTER(C.c_int)),
+                                               _ptr(yr), _ptr(st), _ptr(rw)), "chl_agent_observe")
+        return st, rw
+
+    def agent_act(self, nagents, action, inst=0):
+        """Wall stress from the agents' multiplicative actions [2][nagents]
+        (smarties_stat.f90:193-256)."""
+        a = np.ascontiguousarray(action, dtype=np.float64).reshape(2, nagents)
+        self._check(self.lib.chl_agent_act(self.h, inst, nagents, _ptr(a)), "chl_agent_act")
 
     def download(self, inst=0, fields=("U", "V", "W")):
         out = {}

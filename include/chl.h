@@ -33,6 +33,7 @@ extern "C" {
 #define CHL_E_NOMEM 3    /* device allocation failed */
 #define CHL_E_STATE 4    /* call out of order (e.g. step before upload) */
 #define CHL_E_NAN 5      /* non-finite values detected in the fields */
+#define CHL_E_IO 6       /* file could not be opened, read or written */
 
 /* LES_model (subgrid.f90:30-45) */
 #define CHL_LES_NONE 0
@@ -195,6 +196,64 @@ const char* chl_noalloc_last_error(void);
  * w0(1:ny), dxmin, dymin, dzmin, coef_bc_1, coef_bc_2]. */
 int chl_grid_constants_size(const chl_grid_desc* desc);
 int chl_grid_constants(const chl_grid_desc* desc, double* out);
+
+/* ---- files in the reference's formats (host only, no GPU needed) ----------
+ * Snapshot: the stream layout of output_data / read_input_data
+ * (input_output.f90:390-730), as scripts/check_file.m reads it: int32 n and
+ * float64[n] for x, y, z and the centres xm, ym, zm, then per field int32[3]
+ * extents and the float64 array in Fortran order (U, V, W; P and nu_t when
+ * written by a solver step), little-endian.  Arrays have the reference's
+ * global ghosted extents (nx, nyg, nzg etc.).  The reference stops on a
+ * size mismatch; these return CHL_E_ARG / CHL_E_IO with chl_io_last_error().
+ * read_input_data also adds 0.1 (rand() - 0.5) noise to the fields it read
+ * (input_output.f90:526-550); chl_snapshot_read returns the file's values. */
+int chl_snapshot_dims(const char* path, int* nx, int* ny, int* nz);
+int chl_snapshot_read(const char* path, int nx, int ny, int nz, double* x, double* y, double* z,
+                      double* U, double* V, double* W);
+/* P and nu_t: both NULL (an initial-field file) or both given. */
+int chl_snapshot_write(const char* path, int nx, int ny, int nz, const double* x, const double* y,
+                       const double* z, const double* U, const double* V, const double* W,
+                       const double* P, const double* nu_t);
+const char* chl_io_last_error(void);
+
+/* Parameter file of read_input_parameters (input_output.f90:20-91):
+ * comment lines alternating with list-directed value lines. */
+typedef struct {
+  int nx, ny, nz;              /* face counts (nx_global, ny_global, nz_global) */
+  double CFL, nu, dPdx;
+  int x_mass_cte, LES_model;
+  int nsteps, nsave, nstats, nmonitor;
+  char filein[256], fileout[256];
+  int nstep_init, random_init, Dirichlet_nu_t;
+} chl_parameters;
+int chl_read_parameters(const char* path, chl_parameters* out);
+
+/* Device state of instance inst to/from a snapshot file (output_data without
+ * the step-number suffix, read_input_data without the noise).  Save computes
+ * the actual pressure first when with_pressure is 1 (output_data calls
+ * compute_pressure unless it is current, input_output.f90:604-606) and writes
+ * P and nu_t; with 0 it writes U, V, W only.  Load checks the file's extents
+ * against the instance and uploads with the boundary conditions applied. */
+int chl_save_snapshot(chl_handle* h, int inst, const char* path, int with_pressure);
+int chl_load_snapshot(chl_handle* h, int inst, const char* path);
+
+/* ---- wall agents of the reference's RL environment ----------------------
+ * send_recv_state_action (smarties_stat.f90:24-260) without the smarties
+ * transport.  nagents agents per wall sit at x faces (na-1)*(nx-2)/nagents+2
+ * of the first z plane; nagents must divide nx-2 (the reference uses
+ * NUM_AGENTS/nprocs/2 = 128 for one rank).
+ * chl_agent_observe: states[2][nagents][6] = (dU l/u_tau, U/u_tau - dU l/u_tau
+ * ln(l u_tau/nu), U, l, u_tau, dPdx_ref) and rewards[2][nagents] = 100 - 5000
+ * |sqrt(tau_w) - sqrt(dPdx_ref)|/sqrt(dPdx_ref) (smarties_stat.f90:84-176),
+ * index [wall][agent]; the reference draws the sampling row y_ind (3 or 4)
+ * and weight y_rand in [0,1] with RANDOM_NUMBER, here the caller passes them
+ * ([2][nagents] each).  dPdx_ref is the descriptor's dPdx.
+ * chl_agent_act: action[2][nagents] multiplies the current wall stress at
+ * each agent (smarties_stat.f90:193-216), and alpha_x is rebuilt by linear
+ * interpolation along x between agents and the z pass of :228-256. */
+int chl_agent_observe(chl_handle* h, int inst, int nagents, const int* y_ind, const double* y_rand,
+                      double* states, double* rewards);
+int chl_agent_act(chl_handle* h, int inst, int nagents, const double* action);
 
 #ifdef __cplusplus
 }
