@@ -59,6 +59,8 @@ KERNEL_BYTES = {
     "project": 8 * 7.0,
     "massflow_shift": 8 * 2.0,
     "dt_minabs": 8 * 3.0,
+    "amd": 8 * 4.0,              # U, V, W in, nu_t out
+    "vreman": 8 * 4.0,           # U, V, W in, nu_t out
 }
 # Compulsory traffic of an ideally fused step (8-byte streams per point):
 # 107 with the dynamic model, 101 with static Smagorinsky.
@@ -66,10 +68,15 @@ STEP_STREAMS = {"dsm": 107, "smag": 101}
 
 
 def workload(name):
+    from dataclasses import replace
     if name == "c3_dsm":
         return [C.c3_roofline(les=C.LES_DSM)]
     if name == "c3_smag":
         return [C.c3_roofline(les=C.LES_SMAG)]
+    if name == "c3_amd":
+        return [replace(C.c3_roofline(les=C.LES_DSM), LES_model=C.LES_AMD, name="c3_256x96x192_amd_eqwm")]
+    if name == "c3_vreman":
+        return [replace(C.c3_roofline(les=C.LES_DSM), LES_model=C.LES_VREMAN, name="c3_256x96x192_vreman_eqwm")]
     if name == "c3_dsm_small":
         return [C.smaller(C.c3_roofline(les=C.LES_DSM), 128, 96, 96)]
     if name == "c1":
@@ -354,7 +361,10 @@ def run_ours(args):
             "profiled_step_ms": tot_prof}
     if args.workload in ("c3_dsm", "c3_smag") and not args.no_batched:
         line["batched_mlp"] = batched_mlp_rate(args)
-    if rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
+    if rank == 0 and args.gpus == 1 and not args.no_cpu_baseline and cases_[0].LES_model > C.LES_DSM:
+        line["cpu_baseline"] = {"value": None, "unit": UNIT,
+                                "note": "the host restatement covers the none/static/dynamic SGS models only"}
+    elif rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
         rate, nsteps, secs, cores = host_step_rate(cases_, args.cpu_budget, 50)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": host_sample_text(nsteps, cases_, args, secs, cores),

@@ -35,6 +35,7 @@ struct ChlInst {
   // geometry (reciprocal spacings; see chl_host.cpp for the exact list)
   const double *rdxc, *rdxf, *rdyc, *rdyf, *rdzc, *rdzf;
   const double *dxf, *dyf, *dzf;  // raw spacings (dt)
+  const double *hx2, *hy2, *hz2;  // squared centre widths (x(i)-x(i-1))^2 etc. (Vreman)
   const double *w0, *w1;          // weight_y_0/1 by face row jv
   const double *ygc;              // yg(1..nyg), centre y coordinates with the ghost rows
   const double *smag_csdelta;     // Cs*Delta_j by centre row (static Smagorinsky)

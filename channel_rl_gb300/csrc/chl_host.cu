@@ -71,6 +71,7 @@ struct Consts {
   int nx, ny, nz, nxg, nyg, nzg, Nx, Ny, Nz, Nxh;
   std::vector<double> xf, yf, zf, xg, yg, zg;   // 1-based Fortran copies (index 0 unused)
   std::vector<double> rdxc, rdxf, dxf, rdzc, rdzf, dzf;   // offset 1, length N+3
+  std::vector<double> hx2, hz2, hy2;                       // squared centre widths (x, z offset 1)
   std::vector<double> rdyc, rdyf, dyf, w0, w1;            // length Ny+2
   std::vector<double> csdelta, dwall;                     // length Ny+2
   std::vector<double> kxx, kzz;
@@ -131,6 +132,14 @@ int make_consts(const chl_grid_desc& d, Consts& c, std::string& err) {
   };
   periodic(c.xf, c.xg, c.Nx, c.rdxc, c.rdxf, c.dxf);
   periodic(c.zf, c.zg, c.Nz, c.rdzc, c.rdzf, c.dzf);
+  auto widths2 = [&](const std::vector<double>& f, int N, std::vector<double>& w) {
+    w.assign(N + 3, NaN);
+    for (int i = 0; i <= N; ++i) { const double d = f[i + 2] - f[i + 1]; w[i + 1] = d * d; }
+  };
+  widths2(c.xf, c.Nx, c.hx2);
+  widths2(c.zf, c.Nz, c.hz2);
+  c.hy2.assign(c.Ny + 2, NaN);
+  for (int jc = 1; jc <= c.Ny; ++jc) { const double d = c.yf[jc + 1] - c.yf[jc]; c.hy2[jc] = d * d; }
   const int Ny = c.Ny;
   c.rdyc.assign(Ny + 2, NaN); c.rdyf.assign(Ny + 2, NaN); c.dyf.assign(Ny + 2, NaN);
   c.w0.assign(Ny + 2, NaN); c.w1.assign(Ny + 2, NaN);
@@ -239,6 +248,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   size_t o_rdxc = A.take(8 * (Nx + 3)), o_rdxf = A.take(8 * (Nx + 3)), o_dxf = A.take(8 * (Nx + 3));
   size_t o_rdzc = A.take(8 * (Nz + 3)), o_rdzf = A.take(8 * (Nz + 3)), o_dzf = A.take(8 * (Nz + 3));
   size_t o_rdyc = A.take(8 * (Ny + 2)), o_rdyf = A.take(8 * (Ny + 2)), o_dyf = A.take(8 * (Ny + 2));
+  size_t o_hx2 = A.take(8 * (Nx + 3)), o_hz2 = A.take(8 * (Nz + 3)), o_hy2 = A.take(8 * (Ny + 2));
   size_t o_w0 = A.take(8 * (Ny + 2)), o_w1 = A.take(8 * (Ny + 2)), o_ygc = A.take(8 * (Ny + 2));
   size_t o_csd = A.take(8 * (Ny + 2)), o_dw = A.take(8 * (Ny + 2));
   size_t o_twx = A.take(16 * Nx), o_twz = A.take(16 * Nz);
@@ -290,6 +300,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.mass_norm = 1.0 / ((double)Nx * Nz);
   D.rdxc = P(o_rdxc) + 1; D.rdxf = P(o_rdxf) + 1; D.dxf = P(o_dxf) + 1;
   D.rdzc = P(o_rdzc) + 1; D.rdzf = P(o_rdzf) + 1; D.dzf = P(o_dzf) + 1;
+  D.hx2 = P(o_hx2) + 1; D.hz2 = P(o_hz2) + 1; D.hy2 = P(o_hy2);
   D.rdyc = P(o_rdyc); D.rdyf = P(o_rdyf); D.dyf = P(o_dyf); D.w0 = P(o_w0); D.w1 = P(o_w1); D.ygc = P(o_ygc);
   D.smag_csdelta = P(o_csd); D.smag_dwall = P(o_dw);
   D.twx = (const double2*)(base + o_twx); D.twz = (const double2*)(base + o_twz);
@@ -313,6 +324,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   CK(put(o_rdxc, c.rdxc)); CK(put(o_rdxf, c.rdxf)); CK(put(o_dxf, c.dxf));
   CK(put(o_rdzc, c.rdzc)); CK(put(o_rdzf, c.rdzf)); CK(put(o_dzf, c.dzf));
   CK(put(o_rdyc, c.rdyc)); CK(put(o_rdyf, c.rdyf)); CK(put(o_dyf, c.dyf));
+  CK(put(o_hx2, c.hx2)); CK(put(o_hz2, c.hz2)); CK(put(o_hy2, c.hy2));
   const std::vector<double> ygc(c.yg.begin() + 1, c.yg.begin() + 1 + c.nyg);
   CK(put(o_ygc, ygc));
   CK(put(o_w0, c.w0)); CK(put(o_w1, c.w1)); CK(put(o_csd, c.csdelta)); CK(put(o_dw, c.dwall));
@@ -418,7 +430,6 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
     KL("edges", chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st));
     KL("centre_strain", chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 0, st));
   } else if (h->LES_model == CHL_LES_AMD) {
-    KL("edges", chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st));
     KL("amd", chl_launch_amd(h->map(M_PT), h->nblk[M_PT], s, st));
   } else if (h->LES_model == CHL_LES_VREMAN) {
     KL("vreman", chl_launch_vreman(h->map(M_PT), h->nblk[M_PT], s, st));
