@@ -387,7 +387,7 @@ static int build_maps(chl_handle* h) {
         case M_FFTX: b = cdiv((long)Ny * (Nz / 2), fftx_rows(Nx)); break;
         case M_FFTZ: b = Ny * cdiv(Nxh, 16); break;
         case M_TRI: b = cdiv((long)Nz * Nxh, 128); break;
-        case M_MINABS: b = Nz; break;
+        case M_MINABS: b = Nz * ((Ny + 15) / 16); break;   // planes x 16-row chunks (chl_misc.cu)
         case M_ROWS: b = Ny + 1; break;
         case M_MLP: b = cdiv(2L * Nx * Nz, 128); break;
       }

@@ -69,38 +69,65 @@ __device__ __forceinline__ unsigned long long absbits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
 }
 
-// one block per z plane of each instance
+// Blocks per instance: Nz planes x MINABS_CHUNKS(Ny) row chunks.  Threads
+// run over x (coalesced); each keeps its own minimum of |U| at its x-face
+// and of |W|, and the per-row minimum of |V| is formed by warp shuffles.
+// Mins of non-negative doubles are mins of their bit patterns, so the
+// reductions are exact and order-free.
+#define MINABS_ROWS 16
+__device__ __forceinline__ int minabs_chunks(int Ny) { return (Ny + MINABS_ROWS - 1) / MINABS_ROWS; }
+
 __global__ void __launch_bounds__(256)
 k_minabs(ChlMap map, int s) {
-  extern __shared__ unsigned long long smin[];   // [Nx] U, [Ny+1] V
+  __shared__ unsigned long long sv[MINABS_ROWS];
+  __shared__ unsigned long long swm[8];
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
-  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  const int k = lb;
-  unsigned long long* su = smin;
-  unsigned long long* sv = smin + Nx;
-  for (int w = threadIdx.x; w < Nx + Ny + 1; w += blockDim.x) smin[w] = CHL_BIG_BITS;
+  const int Nx = I.Nx, Ny = I.Ny;
+  const int nch = minabs_chunks(Ny);
+  const int k = lb / nch, j0 = 1 + (lb % nch) * MINABS_ROWS;
+  const int j1 = min(Ny, j0 + MINABS_ROWS - 1);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x < MINABS_ROWS) sv[threadIdx.x] = CHL_BIG_BITS;
   __syncthreads();
   const double* U = I.U[s]; const double* V = I.V[s]; const double* W = I.W[s];
-  unsigned long long mw = CHL_BIG_BITS;
-  for (int w = threadIdx.x; w < Nx * Ny; w += blockDim.x) {
-    const int i = w % Nx, jc = 1 + w / Nx;
-    atomicMin(su + i, absbits(U[cidx(I, i, jc, k)]));
-    atomicMin(sv + jc, absbits(V[vidx(I, i, jc, k)]));
-    const unsigned long long b = absbits(W[cidx(I, i, jc, k)]);
-    mw = b < mw ? b : mw;
-  }
-  __shared__ unsigned long long red[256];
-  red[threadIdx.x] = mw;
-  __syncthreads();
-  for (int h = 128; h > 0; h >>= 1) {
-    if (threadIdx.x < h) red[threadIdx.x] = min(red[threadIdx.x], red[threadIdx.x + h]);
-    __syncthreads();
-  }
   unsigned long long* g = I.minabs;      // [Nx] U, [Ny+1] V, [Nz] W
-  for (int w = threadIdx.x; w < Nx; w += blockDim.x) atomicMin(g + w, su[w]);
-  for (int w = threadIdx.x + 1; w <= Ny; w += blockDim.x) atomicMin(g + Nx + w, sv[w]);
-  if (threadIdx.x == 0) g[Nx + Ny + 1 + k] = red[0];
+  unsigned long long mw = CHL_BIG_BITS;
+  const int nxr = (Nx + 31) & ~31;       // whole warps take part in the shuffles
+  for (int i = threadIdx.x; i < nxr; i += blockDim.x) {
+    const bool ok = i < Nx;
+    unsigned long long mu = CHL_BIG_BITS;
+    for (int jc = j0; jc <= j1; ++jc) {
+      unsigned long long bv = CHL_BIG_BITS;
+      if (ok) {
+        const unsigned long long bu = absbits(U[cidx(I, i, jc, k)]);
+        const unsigned long long bw = absbits(W[cidx(I, i, jc, k)]);
+        bv = absbits(V[vidx(I, i, jc, k)]);
+        mu = bu < mu ? bu : mu;
+        mw = bw < mw ? bw : mw;
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long x = __shfl_xor_sync(0xffffffffu, bv, o);
+        bv = x < bv ? x : bv;
+      }
+      if (lane == 0) atomicMin(sv + (jc - j0), bv);
+    }
+    if (ok) atomicMin(g + i, mu);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, mw, o);
+    mw = x < mw ? x : mw;
+  }
+  if (lane == 0) swm[warp] = mw;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long m = swm[0];
+    for (int w = 1; w < (int)(blockDim.x >> 5); ++w) m = swm[w] < m ? swm[w] : m;
+    atomicMin(g + Nx + Ny + 1 + k, m);
+  }
+  if (threadIdx.x <= j1 - j0) atomicMin(g + Nx + j0 + threadIdx.x, sv[threadIdx.x]);
 }
 
 __global__ void k_minabs_init(ChlMap map) {
@@ -249,7 +276,8 @@ __global__ void k_qflow(ChlMap map, int s, int slot) {
 extern "C" {
 void chl_launch_minabs(const ChlMap& m, int nb, size_t smem, int s, cudaStream_t st) {
   k_minabs_init<<<m.n, 128, 0, st>>>(m);
-  k_minabs<<<nb, 256, smem, st>>>(m, s);
+  (void)smem;
+  k_minabs<<<nb, 256, 0, st>>>(m, s);
 }
 void chl_launch_dt(const ChlMap& m, cudaStream_t st) { k_dt<<<m.n, 128, 0, st>>>(m); }
 void chl_launch_massflow(const ChlMap& m, cudaStream_t st, int s, int force) { k_massflow<<<m.n, 256, 0, st>>>(m, s, force); }
