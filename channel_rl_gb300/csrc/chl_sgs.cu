@@ -135,8 +135,21 @@ k_filter_y(ChlMap map, int s_in) {
   const size_t c = cidx(I, i, j, k);
   const size_t pc = (size_t)Nx;
   if (j >= 1 && j <= Ny) {
+    // loads of five components are issued before their stores: the stores
+    // may alias the loads as far as the compiler knows, so this is what keeps
+    // enough loads in flight
+    const size_t lo = (j == 1) ? c + pc : c - pc, hi = (j == Ny) ? c - pc : c + pc;
 #pragma unroll
-    for (int m = 0; m < 15; ++m) I.r[m][c] = fy(I.q[m], c, pc, j, 1, Ny);
+    for (int m0 = 0; m0 < 15; m0 += 5) {
+      double a[5], b[5], d[5];
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {
+        const double* f = I.q[m0 + q];
+        a[q] = LDG(f + c); b[q] = LDG(f + lo); d[q] = LDG(f + hi);
+      }
+#pragma unroll
+      for (int q = 0; q < 5; ++q) I.r[m0 + q][c] = fma(4.0, a[q], b[q] + d[q]);
+    }
   }
   I.r[15][c] = fy(I.U[s_in], c, pc, j, 0, Ny + 1);
   I.r[17][c] = fy(I.W[s_in], c, pc, j, 0, Ny + 1);
@@ -165,8 +178,16 @@ k_filter_xz(ChlMap map, int from_r) {
   const size_t c = cidx(I, i, j, k), cm = cidx(I, im, j, km), cp = cidx(I, ip, j, kp);
   if (j >= 1 && j <= Ny) {
 #pragma unroll
-    for (int m = 0; m < 15; ++m)
-      out[m][c] = fma(4.0, LDG(in[m] + c), LDG(in[m] + cm) + LDG(in[m] + cp));
+    for (int m0 = 0; m0 < 15; m0 += 5) {       // five components' loads in flight (see k_filter_y)
+      double a[5], b[5], d[5];
+#pragma unroll
+      for (int q = 0; q < 5; ++q) {
+        const double* f = in[m0 + q];
+        a[q] = LDG(f + c); b[q] = LDG(f + cm); d[q] = LDG(f + cp);
+      }
+#pragma unroll
+      for (int q = 0; q < 5; ++q) out[m0 + q][c] = fma(4.0, a[q], b[q] + d[q]);
+    }
   }
   out[15][c] = fma(4.0, LDG(in[15] + c), LDG(in[15] + cm) + LDG(in[15] + cp));
   out[17][c] = fma(4.0, LDG(in[17] + c), LDG(in[17] + cm) + LDG(in[17] + cp));
