@@ -455,8 +455,15 @@ def e2e_rate(ch, case, args):
         ch.download_async(out[0][1], out[1][1], out[2][1])
         ch.synchronize()
     secs = time.perf_counter() - t0
-    return {"value": case.points * n / secs, "unit": UNIT, "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb,
-            "steps": n, "path": "chl_set_fields + chl_rk3_step + chl_download_async, pinned host U,V,W"}
+    out = {"value": case.points * n / secs, "unit": UNIT, "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb,
+           "steps": n, "ms_per_step": 1e3 * secs / n,
+           "path": "chl_set_fields + chl_rk3_step + chl_download_async, pinned host U,V,W"}
+    c2c = load_json(os.path.join(HERE, "profiles", "c2c_bandwidth.json"), {})
+    if c2c.get("memcpy_h2d_gbs") and c2c.get("memcpy_d2h_gbs"):
+        # the copies cannot overlap the step they feed or read: their time is a floor
+        out["transfer_floor_ms_per_step"] = 1e3 * (hb / (c2c["memcpy_h2d_gbs"] * 1e9) + hb / (c2c["memcpy_d2h_gbs"] * 1e9))
+        out["transfer_floor_source"] = "profiles/c2c_bandwidth.json (measured pinned-copy bandwidth)"
+    return out
 
 
 def main():

@@ -61,7 +61,7 @@ struct ChlInst {
   double *coef;                   // nu_t coefficient per centre row [Ny+2]
   double *scal;                   // device scalars (CHL_S_*)
   unsigned long long *minabs;     // [Nx+1 | Nz] min |u| bit patterns (dt)
-  double *red;                    // reduction scratch [nblocks]
+  double *red;                    // bulk-flow plane partials [2][Nz] (upload)
   int *status;                    // device status word (0 ok)
   // learned wall model (chl_mlp.cu)
   double retau;                   // nominal Re_tau of the instance (feature ln(h Re_tau))

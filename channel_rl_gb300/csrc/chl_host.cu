@@ -48,7 +48,7 @@ void chl_launch_massflow(const ChlMap&, cudaStream_t, int, int);
 void chl_launch_shift(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_tadvance(const ChlMap&, cudaStream_t);
 void chl_launch_divmax(const ChlMap&, int, double*, cudaStream_t);
-void chl_launch_qflow(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_qflow(const ChlInst*, int, int, int, cudaStream_t);
 void chl_launch_stats(const ChlMap&, int, double*, int, int, cudaStream_t);
 int chl_mlp_setup();
 void chl_launch_mlp(const ChlMap&, int, int, int, int*, cudaStream_t);
@@ -270,6 +270,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   size_t o_part = A.take(8 * 2 * (size_t)(Ny + 2) * npart);
   size_t o_coef = A.take(8 * (Ny + 2)), o_scal = A.take(8 * CHL_S_NSCAL);
   size_t o_min = A.take(8 * (size_t)(Nx + Ny + 1 + Nz)), o_status = A.take(64);
+  size_t o_red = A.take(8 * 2 * (size_t)Nz);
   size_t o_trace = A.take(4 * (size_t)MLP_NPARAM);
   I.nstage = (size_t)c.nxg * c.nyg * c.nzg;
   size_t o_stage = A.take(8 * I.nstage);
@@ -313,7 +314,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.spec = (double2*)(base + o_spec); D.p = P(o_p); D.P = P(o_P);
   D.alpha = P(o_alpha); D.bc = P(o_bc); D.part = P(o_part); D.npart = npart;
   D.coef = P(o_coef); D.scal = P(o_scal);
-  D.minabs = (unsigned long long*)(base + o_min); D.red = nullptr; D.status = (int*)(base + o_status);
+  D.minabs = (unsigned long long*)(base + o_min); D.red = P(o_red); D.status = (int*)(base + o_status);
   D.retau = I.d.Re_tau;
   D.mlp_trace = (float*)(base + o_trace);
   D.mlp_theta = h->d_mlp_theta;
@@ -624,8 +625,7 @@ int chl_upload(chl_handle* h, int inst, const double* U, const double* V, const 
     LAUNCHED();
   }
   // Qflow_x_0 of this instance (mass_flow.f90:271-309); the kernel runs per instance
-  ChlMap m{h->d_inst + inst, h->d_off[M_PT], 1};
-  chl_launch_qflow(m, 0, CHL_S_Q0, h->st);
+  chl_launch_qflow(h->d_inst + inst, Nz, 0, CHL_S_Q0, h->st);
   LAUNCHED();
   I->uploaded = true;
   return finish(h);

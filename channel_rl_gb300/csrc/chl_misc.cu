@@ -252,16 +252,22 @@ __global__ void k_divmax(ChlMap map, int s, double* out) {
 // ------------------------------------------------------------ initial bulk flow Qflow_x_0
 // compute_mean_mass_flow_U (mass_flow.f90:271-309), trapezoid over rows
 // j_f = 3..nyg-1 of the unique x-z points; one block per instance.
-__global__ void k_qflow(ChlMap map, int s, int slot) {
-  const ChlInst& I = map.inst[blockIdx.x];
-  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+// one block per z plane: compensated (Kahan) partial sums of the plane
+// into red[2k], red[2k+1]; k_qflow_final adds them in plane order
+__global__ void k_qflow_part(const ChlInst* inst, int s) {
+  const ChlInst& I = *inst;
+  const int Nx = I.Nx, Ny = I.Ny, k = blockIdx.x;
   const double* U = I.U[s];
-  double q = 0.0, n = 0.0;
-  for (long w = threadIdx.x; w < (long)Nx * (Ny - 1) * Nz; w += blockDim.x) {
-    const int i = (int)(w % Nx), jc = 2 + (int)((w / Nx) % (Ny - 1)), k = (int)(w / ((long)Nx * (Ny - 1)));
+  double q = 0.0, qc = 0.0, n = 0.0, nc = 0.0;
+  for (int w = threadIdx.x; w < Nx * (Ny - 1); w += blockDim.x) {
+    const int i = w % Nx, jc = 2 + w / Nx;
     const double dyg = I.dyf[jc - 1];          // yg(j)-yg(j-1), j_f = jc+1
-    q += (U[cidx(I, i, jc, k)] + U[cidx(I, i, jc - 1, k)]) * 0.5 * dyg;
-    n += (1.0 + 1.0) * 0.5 * dyg;
+    const double y1 = (U[cidx(I, i, jc, k)] + U[cidx(I, i, jc - 1, k)]) * 0.5 * dyg - qc;
+    const double t1 = q + y1;
+    qc = (t1 - q) - y1; q = t1;
+    const double y2 = (1.0 + 1.0) * 0.5 * dyg - nc;
+    const double t2 = n + y2;
+    nc = (t2 - n) - y2; n = t2;
   }
   __shared__ double r0[256], r1[256];
   r0[threadIdx.x] = q; r1[threadIdx.x] = n;
@@ -270,7 +276,19 @@ __global__ void k_qflow(ChlMap map, int s, int slot) {
     if (threadIdx.x < h) { r0[threadIdx.x] += r0[threadIdx.x + h]; r1[threadIdx.x] += r1[threadIdx.x + h]; }
     __syncthreads();
   }
-  if (threadIdx.x == 0) I.scal[slot] = r0[0] / r1[0];
+  if (threadIdx.x == 0) { I.red[2 * k] = r0[0]; I.red[2 * k + 1] = r1[0]; }
+}
+
+__global__ void k_qflow_final(const ChlInst* inst, int slot) {
+  const ChlInst& I = *inst;
+  double q = 0.0, qc = 0.0, n = 0.0, nc = 0.0;
+  for (int k = 0; k < I.Nz; ++k) {
+    const double y1 = I.red[2 * k] - qc, t1 = q + y1;
+    qc = (t1 - q) - y1; q = t1;
+    const double y2 = I.red[2 * k + 1] - nc, t2 = n + y2;
+    nc = (t2 - n) - y2; n = t2;
+  }
+  I.scal[slot] = q / n;
 }
 
 extern "C" {
@@ -284,5 +302,8 @@ void chl_launch_massflow(const ChlMap& m, cudaStream_t st, int s, int force) { k
 void chl_launch_shift(const ChlMap& m, int nb, int s, cudaStream_t st) { k_shift<<<nb, 256, 0, st>>>(m, s); }
 void chl_launch_tadvance(const ChlMap& m, cudaStream_t st) { k_tadvance<<<m.n, 32, 0, st>>>(m); }
 void chl_launch_divmax(const ChlMap& m, int s, double* out, cudaStream_t st) { k_divmax<<<m.n, 256, 0, st>>>(m, s, out); }
-void chl_launch_qflow(const ChlMap& m, int s, int slot, cudaStream_t st) { k_qflow<<<m.n, 256, 0, st>>>(m, s, slot); }
+void chl_launch_qflow(const ChlInst* inst, int Nz, int s, int slot, cudaStream_t st) {
+  k_qflow_part<<<Nz, 256, 0, st>>>(inst, s);
+  k_qflow_final<<<1, 1, 0, st>>>(inst, slot);
+}
 }
