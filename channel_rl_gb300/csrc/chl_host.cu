@@ -500,6 +500,22 @@ static int finish(chl_handle* h) {
   return CHL_OK;
 }
 
+// Non-finite velocities: the CFL pass of every step flags them in the
+// instance's status word (chl_misc.cu: k_minabs).  Checked at the calls that
+// synchronise; the flag stays set until the instance is uploaded again.
+static int check_finite(chl_handle* h) {
+  for (size_t q = 0; q < h->in.size(); ++q) {
+    int st = 0;
+    cudaError_t e = cudaMemcpy(&st, h->in[q].dev.status, sizeof(int), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) { h->err = std::string("CUDA: ") + cudaGetErrorString(e); return CHL_E_CUDA; }
+    if (st & 1) {
+      h->err = "non-finite velocity in instance " + std::to_string(q) + " (found by compute_dt); re-upload the fields";
+      return CHL_E_NAN;
+    }
+  }
+  return CHL_OK;
+}
+
 // ------------------------------------------------------------ C ABI
 extern "C" {
 
@@ -627,6 +643,7 @@ int chl_upload(chl_handle* h, int inst, const double* U, const double* V, const 
   // Qflow_x_0 of this instance (mass_flow.f90:271-309); the kernel runs per instance
   chl_launch_qflow(h->d_inst + inst, Nz, 0, CHL_S_Q0, h->st);
   LAUNCHED();
+  CK(cudaMemsetAsync(I->dev.status, 0, sizeof(int), h->st));
   I->uploaded = true;
   return finish(h);
 }
@@ -642,6 +659,8 @@ static int download_field(chl_handle* h, Inst* I, double* dst, const double* src
 int chl_download(chl_handle* h, int inst, double* U, double* V, double* W, double* P, double* nu_t) {
   Inst* I = get_inst(h, inst);
   if (!I) return CHL_E_ARG;
+  int rc0 = finish(h);
+  if (rc0 || (rc0 = check_finite(h))) return rc0;
   const Consts& c = I->c;
   const int Ny = c.Ny;
   int rc = 0;
@@ -843,7 +862,11 @@ int chl_rk3_step(chl_handle* h, int nsteps) {
   return CHL_OK;
 }
 
-int chl_synchronize(chl_handle* h) { if (!h) return CHL_E_ARG; return finish(h); }
+int chl_synchronize(chl_handle* h) {
+  if (!h) return CHL_E_ARG;
+  int rc = finish(h);
+  return rc ? rc : check_finite(h);
+}
 
 int chl_compute_eddy_viscosity(chl_handle* h) {
   int rc = check_ready(h); if (rc) return rc;
@@ -944,6 +967,7 @@ int chl_set_fields(chl_handle* h, int inst, const double* U, const double* V, co
     chl_launch_unpack(q.dst, I->staging, c.Nx, q.nrow, c.Nz, q.n1, q.n2, q.kind, h->st);
     LAUNCHED();
   }
+  CK(cudaMemsetAsync(I->dev.status, 0, sizeof(int), h->st));
   return CHL_OK;   // stream-ordered; no synchronisation
 }
 
@@ -1128,7 +1152,9 @@ static int run_stats(chl_handle* h, int inst, std::vector<double>& buf) {
 }
 
 int chl_stats(chl_handle* h, int inst, chl_stats_out* out) {
-  if (!out) return CHL_E_ARG;
+  if (!out || !h) return CHL_E_ARG;
+  int rc0 = finish(h);
+  if (rc0 || (rc0 = check_finite(h))) return rc0;
   std::vector<double> buf;
   int rc = run_stats(h, inst, buf); if (rc) return rc;
   const Inst& I = h->in[inst];

@@ -93,6 +93,7 @@ k_minabs(ChlMap map, int s) {
   const double* U = I.U[s]; const double* V = I.V[s]; const double* W = I.W[s];
   unsigned long long* g = I.minabs;      // [Nx] U, [Ny+1] V, [Nz] W
   unsigned long long mw = CHL_BIG_BITS;
+  bool bad = false;                      // a non-finite velocity (|x| bits >= those of inf)
   const int nxr = (Nx + 31) & ~31;       // whole warps take part in the shuffles
   for (int i = threadIdx.x; i < nxr; i += blockDim.x) {
     const bool ok = i < Nx;
@@ -105,6 +106,7 @@ k_minabs(ChlMap map, int s) {
         bv = absbits(V[vidx(I, i, jc, k)]);
         mu = bu < mu ? bu : mu;
         mw = bw < mw ? bw : mw;
+        bad |= (bu >= CHL_BIG_BITS) | (bw >= CHL_BIG_BITS) | (bv >= CHL_BIG_BITS);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
@@ -121,6 +123,7 @@ k_minabs(ChlMap map, int s) {
     mw = x < mw ? x : mw;
   }
   if (lane == 0) swm[warp] = mw;
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(I.status, 1);
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long m = swm[0];

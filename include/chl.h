@@ -32,7 +32,8 @@ extern "C" {
 #define CHL_E_CUDA 2     /* CUDA runtime error */
 #define CHL_E_NOMEM 3    /* device allocation failed */
 #define CHL_E_STATE 4    /* call out of order (e.g. step before upload) */
-#define CHL_E_NAN 5      /* non-finite values detected in the fields */
+#define CHL_E_NAN 5      /* non-finite velocity found by the step's CFL pass; reported by
+                            chl_synchronize, chl_download and chl_stats until the next upload */
 #define CHL_E_IO 6       /* file could not be opened, read or written */
 
 /* LES_model (subgrid.f90:30-45) */

@@ -191,3 +191,26 @@ def test_calls_out_of_order_report_errors():
     with pytest.raises(ValueError):
         ch.upload(np.zeros((3, 3, 3)), np.zeros((3, 3, 3)), np.zeros((3, 3, 3)))
     ch.close()
+
+
+def test_non_finite_velocity_is_reported():
+    """A NaN in the uploaded field (made on the host) is found by the next
+    step's CFL pass and reported as CHL_E_NAN at the synchronising calls,
+    until clean fields are uploaded again."""
+    from channel_rl_gb300.host import ChlError
+    case = C.smaller(C.c1_small(), 16, 12, 16)
+    U, V, W = C.initial_fields(case)
+    ch = _channel(case)
+    bad = U.copy()
+    bad[5, 6, 7] = np.nan
+    ch.upload(bad, V, W)
+    ch.step(1)
+    with pytest.raises(ChlError, match=r"\(5\).*non-finite"):
+        ch.synchronize()
+    with pytest.raises(ChlError, match="non-finite"):
+        ch.download()
+    ch.upload(U, V, W)
+    ch.step(1)
+    ch.synchronize()
+    assert np.isfinite(ch.download()["U"]).all()
+    ch.close()
