@@ -158,29 +158,28 @@ k_div_fftx(ChlMap map, int s_in, int mode) {
 }
 
 // ------------------------------------------------------------ z transform of the half spectrum
-#define ZCW 16
 __global__ void __launch_bounds__(256)
-k_fftz(ChlMap map, int inv) {
+k_fftz(ChlMap map, int inv, int zcw) {
+  // zcw kx columns per block (16, fewer for long z lines: chl_fftz_cols)
   extern __shared__ double2 sm[];
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
-  const int Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
-  const int ncb = (Nxh + ZCW - 1) / ZCW;
-  const int jc = 1 + lb / ncb, c0 = (lb % ncb) * ZCW;
-  const int cw = min(ZCW, Nxh - c0);
+  const int Nz = I.Nz, Nxh = I.Nxh;
+  const int ncb = (Nxh + zcw - 1) / zcw;
+  const int jc = 1 + lb / ncb, c0 = (lb % ncb) * zcw;
+  const int cw = min(zcw, Nxh - c0);
   double2* A = sm;
-  double2* B = sm + Nz * ZCW;
+  double2* B = sm + Nz * zcw;
   double2* base = I.spec + (size_t)jc * Nz * Nxh + c0;
-  for (int w = threadIdx.x; w < Nz * ZCW; w += blockDim.x) {
-    const int k = w / ZCW, c = w - k * ZCW;
-    A[k * ZCW + c] = c < cw ? base[(size_t)k * Nxh + c] : make_double2(0.0, 0.0);
+  for (int w = threadIdx.x; w < Nz * zcw; w += blockDim.x) {
+    const int k = w / zcw, c = w - k * zcw;
+    A[k * zcw + c] = c < cw ? base[(size_t)k * Nxh + c] : make_double2(0.0, 0.0);
   }
-  double2* res = fft_smem(A, B, ZCW, 1, ZCW, Nz, I.twz, inv != 0);
-  for (int w = threadIdx.x; w < Nz * ZCW; w += blockDim.x) {
-    const int k = w / ZCW, c = w - k * ZCW;
-    if (c < cw) base[(size_t)k * Nxh + c] = res[k * ZCW + c];
+  double2* res = fft_smem(A, B, zcw, 1, zcw, Nz, I.twz, inv != 0);
+  for (int w = threadIdx.x; w < Nz * zcw; w += blockDim.x) {
+    const int k = w / zcw, c = w - k * zcw;
+    if (c < cw) base[(size_t)k * Nxh + c] = res[k * zcw + c];
   }
-  (void)Ny;
 }
 
 // ------------------------------------------------------------ tridiagonal per mode
@@ -351,7 +350,14 @@ __global__ void k_pghost(ChlMap map) {
 
 extern "C" {
 size_t chl_smem_fftx(int maxNx) { int cr = 1024 / maxNx; if (cr < 1) cr = 1; return (size_t)2 * cr * maxNx * sizeof(double2); }
-size_t chl_smem_fftz(int maxNz) { return (size_t)2 * maxNz * ZCW * sizeof(double2); }
+size_t chl_smem_fftz(int maxNz, int zcw) { return (size_t)2 * maxNz * zcw * sizeof(double2); }
+// kx columns staged per z-transform block: 16, halved while two Nz x cols
+// complex tiles would exceed the 227 KB a block may use
+int chl_fftz_cols(int maxNz) {
+  int c = 16;
+  while (c > 1 && chl_smem_fftz(maxNz, c) > (size_t)227 * 1024) c /= 2;
+  return c;
+}
 int chl_fft_setup(size_t smx, size_t smz) {
   cudaError_t e1 = cudaFuncSetAttribute(k_div_fftx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
   cudaError_t e2 = cudaFuncSetAttribute(k_fftx_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
@@ -359,7 +365,7 @@ int chl_fft_setup(size_t smx, size_t smz) {
   return (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) ? 1 : 0;
 }
 void chl_launch_div_fftx(const ChlMap& m, int nb, size_t smem, int s_in, int mode, cudaStream_t st) { k_div_fftx<<<nb, 256, smem, st>>>(m, s_in, mode); }
-void chl_launch_fftz(const ChlMap& m, int nb, size_t smem, int inv, cudaStream_t st) { k_fftz<<<nb, 256, smem, st>>>(m, inv); }
+void chl_launch_fftz(const ChlMap& m, int nb, size_t smem, int inv, int zcw, cudaStream_t st) { k_fftz<<<nb, 256, smem, st>>>(m, inv, zcw); }
 void chl_launch_tri(const ChlMap& m, int nb, cudaStream_t st) { k_tri<<<nb, 128, 0, st>>>(m); }
 void chl_launch_fftx_inv(const ChlMap& m, int nb, size_t smem, int dst, cudaStream_t st) { k_fftx_inv<<<nb, 256, smem, st>>>(m, dst); }
 void chl_launch_project(const ChlMap& m, int nb, int s, cudaStream_t st) { k_project<<<nb, 256, 0, st>>>(m, s); }

@@ -30,10 +30,11 @@ void chl_launch_amd(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_vreman(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_agent_obs(const ChlInst*, int, int, double, const int*, const double*, double*, double*, cudaStream_t);
 size_t chl_smem_fftx(int);
-size_t chl_smem_fftz(int);
+size_t chl_smem_fftz(int, int);
+int chl_fftz_cols(int);
 int chl_fft_setup(size_t, size_t);
 void chl_launch_div_fftx(const ChlMap&, int, size_t, int, int, cudaStream_t);
-void chl_launch_fftz(const ChlMap&, int, size_t, int, cudaStream_t);
+void chl_launch_fftz(const ChlMap&, int, size_t, int, int, cudaStream_t);
 void chl_launch_tri(const ChlMap&, int, cudaStream_t);
 void chl_launch_fftx_inv(const ChlMap&, int, size_t, int, cudaStream_t);
 void chl_launch_project(const ChlMap&, int, int, cudaStream_t);
@@ -42,7 +43,7 @@ void chl_launch_pghost(const ChlMap&, int, cudaStream_t);
 void chl_launch_unpack(double*, const double*, int, int, int, int, int, int, cudaStream_t);
 void chl_launch_pack(double*, const double*, int, int, int, int, int, int, double, cudaStream_t);
 void chl_launch_pack_unique(double*, const double*, int, int, int, int, int, cudaStream_t);
-void chl_launch_minabs(const ChlMap&, int, size_t, int, cudaStream_t);
+void chl_launch_minabs(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_dt(const ChlMap&, cudaStream_t);
 void chl_launch_massflow(const ChlMap&, cudaStream_t, int, int);
 void chl_launch_shift(const ChlMap&, int, int, cudaStream_t);
@@ -210,7 +211,8 @@ struct chl_handle {
   std::string err;
   int* d_off[NMAP] = {};
   int nblk[NMAP] = {};
-  size_t smem_x = 0, smem_z = 0, smem_min = 0;
+  size_t smem_x = 0, smem_z = 0;
+  int zcw = 16;                       // kx columns per z-transform block
   int LES_model = 0, wall_model = 0, any_mass = 0;
   float* d_mlp_theta = nullptr;       // learned wall model parameters (shared)
   unsigned int* d_mlp_cfg = nullptr;  // sigma, train, seed lo/hi, evaluation counter
@@ -372,6 +374,9 @@ static int upload_consts(chl_handle* h, Inst& I) {
 static int build_maps(chl_handle* h) {
   const int n = (int)h->in.size();
   auto cdiv = [](long a, long b) { return (int)((a + b - 1) / b); };
+  int mz = 0;
+  for (auto& I : h->in) mz = std::max(mz, I.c.Nz);
+  h->zcw = chl_fftz_cols(mz);
   for (int m = 0; m < NMAP; ++m) {
     std::vector<int> off(n + 1, 0);
     for (int q = 0; q < n; ++q) {
@@ -386,7 +391,7 @@ static int build_maps(chl_handle* h) {
         case M_WALL: b = cdiv(2L * Nx * Nz, 256); break;
         case M_PLANE: b = cdiv((long)Nx * Nz, 256); break;
         case M_FFTX: b = cdiv((long)Ny * (Nz / 2), fftx_rows(Nx)); break;
-        case M_FFTZ: b = Ny * cdiv(Nxh, 16); break;
+        case M_FFTZ: b = Ny * cdiv(Nxh, h->zcw); break;
         case M_TRI: b = cdiv((long)Nz * Nxh, 128); break;
         case M_MINABS: b = Nz * ((Ny + 15) / 16); break;   // planes x 16-row chunks (chl_misc.cu)
         case M_ROWS: b = Ny + 1; break;
@@ -401,16 +406,10 @@ static int build_maps(chl_handle* h) {
   // dynamic shared memory is per launch, so it must hold the largest
   // per-instance need: the x transform of an instance stages
   // fftx_rows(Nx) rows of Nx, which is not monotonic in Nx
-  int mz = 0, mmin = 0;
   size_t sx = 0;
-  for (auto& I : h->in) {
-    sx = std::max(sx, chl_smem_fftx(I.c.Nx));
-    mz = std::max(mz, I.c.Nz);
-    mmin = std::max(mmin, I.c.Nx + I.c.Ny + 1);
-  }
+  for (auto& I : h->in) sx = std::max(sx, chl_smem_fftx(I.c.Nx));
   h->smem_x = sx;
-  h->smem_z = chl_smem_fftz(mz);
-  h->smem_min = 8 * (size_t)mmin;
+  h->smem_z = chl_smem_fftz(mz, h->zcw);
   if (chl_fft_setup(h->smem_x, h->smem_z)) { h->err = "FFT shared-memory size not supported"; return CHL_E_ARG; }
   if (chl_mlp_setup()) { h->err = "wall-model network shared-memory size not supported"; return CHL_E_ARG; }
   return CHL_OK;
@@ -448,9 +447,9 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
 static int enqueue_projection(chl_handle* h, int s, int mode) {
   cudaStream_t st = h->st;
   KL("div_fft_x", chl_launch_div_fftx(h->map(M_FFTX), h->nblk[M_FFTX], h->smem_x, s, mode, st));
-  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 0, st));
+  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 0, h->zcw, st));
   KL("tridiag", chl_launch_tri(h->map(M_TRI), h->nblk[M_TRI], st));
-  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 1, st));
+  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 1, h->zcw, st));
   KL("ifft_x", chl_launch_fftx_inv(h->map(M_FFTX), h->nblk[M_FFTX], h->smem_x, mode == 0 ? 0 : 1, st));
   if (mode == 0) KL("project", chl_launch_project(h->map(M_PT), h->nblk[M_PT], s, st));
   LAUNCHED();
@@ -458,7 +457,7 @@ static int enqueue_projection(chl_handle* h, int s, int mode) {
 }
 
 static int enqueue_dt(chl_handle* h) {
-  KL("dt_minabs", chl_launch_minabs(h->map(M_MINABS), h->nblk[M_MINABS], h->smem_min, 0, h->st));
+  KL("dt_minabs", chl_launch_minabs(h->map(M_MINABS), h->nblk[M_MINABS], 0, h->st));
   KL("dt", chl_launch_dt(h->map(M_PT), h->st));
   LAUNCHED();
   return CHL_OK;

@@ -295,9 +295,8 @@ __global__ void k_qflow_final(const ChlInst* inst, int slot) {
 }
 
 extern "C" {
-void chl_launch_minabs(const ChlMap& m, int nb, size_t smem, int s, cudaStream_t st) {
+void chl_launch_minabs(const ChlMap& m, int nb, int s, cudaStream_t st) {
   k_minabs_init<<<m.n, 128, 0, st>>>(m);
-  (void)smem;
   k_minabs<<<nb, 256, 0, st>>>(m, s);
 }
 void chl_launch_dt(const ChlMap& m, cudaStream_t st) { k_dt<<<m.n, 128, 0, st>>>(m); }
