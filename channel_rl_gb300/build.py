@@ -31,25 +31,32 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
-def _stale(srcs):
-    if not os.path.exists(LIB):
+# variants: None (the library) or "bounds" (every field index checked and
+# clamped, violations recorded in the instance's status word)
+VARIANTS = {None: (OUT, LIB, []),
+            "bounds": (os.path.join(OUT, "bounds"), os.path.join(OUT, "libchl_bounds.so"), ["-DCHL_BOUNDS_CHECK"])}
+
+
+def _stale(srcs, lib=LIB):
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     deps = srcs + [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cuh", ".h"))]
     deps.append(os.path.join(HERE, "..", "include", "chl.h"))
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 
-def build(force: bool = False, verbose: bool = False, extra=None) -> str:
+def build(force: bool = False, verbose: bool = False, extra=None, variant=None) -> str:
+    out_dir, lib, vflags = VARIANTS[variant]
     srcs = sources()
-    if not force and not _stale(srcs):
-        return LIB
-    os.makedirs(OUT, exist_ok=True)
+    if not force and not _stale(srcs, lib):
+        return lib
+    os.makedirs(out_dir, exist_ok=True)
     nv = nvcc()
-    extra = list(extra or [])
+    extra = list(extra or []) + vflags
 
     def comp(src):
-        obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
+        obj = os.path.join(out_dir, os.path.basename(src)[:-3] + ".o")
         cmd = [nv, *ARCH, *FLAGS, *extra, "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
@@ -60,13 +67,13 @@ def build(force: bool = False, verbose: bool = False, extra=None) -> str:
 
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(comp, srcs))
-    tmp = LIB + ".tmp"
+    tmp = lib + ".tmp"
     cmd = [nv, *ARCH, "-shared", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":

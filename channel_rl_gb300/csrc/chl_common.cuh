@@ -95,10 +95,31 @@ __device__ __forceinline__ int chl_find(const ChlMap& m, int b, int& local) {
 
 __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
+// Status word bits of an instance: 1 non-finite velocity (k_minabs),
+// 4 an index outside the field (bounds-checked build only).
+#define CHL_STATUS_NONFINITE 1
+#define CHL_STATUS_BOUNDS 4
+
+// The bounds-checked build (-DCHL_BOUNDS_CHECK, build.build(variant="bounds"))
+// records an out-of-range index in the status word and clamps it, so the
+// access stays inside the field.
+__device__ __forceinline__ void chl_clamp(const ChlInst& I, int& i, int& j, int& k, int jmax) {
+#ifdef CHL_BOUNDS_CHECK
+  if (i < 0 || i >= I.Nx || j < 0 || j > jmax || k < 0 || k >= I.Nz) {
+    atomicOr(I.status, CHL_STATUS_BOUNDS);
+    i = min(max(i, 0), I.Nx - 1); j = min(max(j, 0), jmax); k = min(max(k, 0), I.Nz - 1);
+  }
+#else
+  (void)I; (void)i; (void)j; (void)k; (void)jmax;
+#endif
+}
+
 __device__ __forceinline__ size_t cidx(const ChlInst& I, int i, int jc, int k) {
+  chl_clamp(I, i, jc, k, I.Ny + 1);
   return (size_t)i + (size_t)I.Nx * ((size_t)jc + (size_t)(I.Ny + 2) * (size_t)k);
 }
 __device__ __forceinline__ size_t vidx(const ChlInst& I, int i, int jv, int k) {
+  chl_clamp(I, i, jv, k, I.Ny);
   return (size_t)i + (size_t)I.Nx * ((size_t)jv + (size_t)(I.Ny + 1) * (size_t)k);
 }
 

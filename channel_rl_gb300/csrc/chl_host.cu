@@ -502,12 +502,15 @@ static int finish(chl_handle* h) {
 // Non-finite velocities: the CFL pass of every step flags them in the
 // instance's status word (chl_misc.cu: k_minabs).  Checked at the calls that
 // synchronise; the flag stays set until the instance is uploaded again.
-static int check_finite(chl_handle* h) {
+// inst < 0 checks every instance (chl_synchronize); reads of one instance
+// check only that one, so the others of a batch stay usable.
+static int check_finite(chl_handle* h, int inst = -1) {
   for (size_t q = 0; q < h->in.size(); ++q) {
+    if (inst >= 0 && (int)q != inst) continue;
     int st = 0;
     cudaError_t e = cudaMemcpy(&st, h->in[q].dev.status, sizeof(int), cudaMemcpyDeviceToHost);
     if (e != cudaSuccess) { h->err = std::string("CUDA: ") + cudaGetErrorString(e); return CHL_E_CUDA; }
-    if (st & 1) {
+    if (st & CHL_STATUS_NONFINITE) {
       h->err = "non-finite velocity in instance " + std::to_string(q) + " (found by compute_dt); re-upload the fields";
       return CHL_E_NAN;
     }
@@ -659,7 +662,7 @@ int chl_download(chl_handle* h, int inst, double* U, double* V, double* W, doubl
   Inst* I = get_inst(h, inst);
   if (!I) return CHL_E_ARG;
   int rc0 = finish(h);
-  if (rc0 || (rc0 = check_finite(h))) return rc0;
+  if (rc0 || (rc0 = check_finite(h, inst))) return rc0;
   const Consts& c = I->c;
   const int Ny = c.Ny;
   int rc = 0;
@@ -806,6 +809,14 @@ int chl_agent_act(chl_handle* h, int inst, int nagents, const double* action) {
     }
   CK(cudaMemcpyAsync(I->dev.alpha, al.data(), 8 * al.size(), cudaMemcpyHostToDevice, h->st));
   return finish(h);
+}
+
+int chl_status_flags(chl_handle* h, int inst, int* flags) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !flags) return CHL_E_ARG;
+  int rc = finish(h); if (rc) return rc;
+  CK(cudaMemcpy(flags, I->dev.status, sizeof(int), cudaMemcpyDeviceToHost));
+  return CHL_OK;
 }
 
 int chl_get_scalars(chl_handle* h, int inst, double* out4) {
@@ -1153,7 +1164,7 @@ static int run_stats(chl_handle* h, int inst, std::vector<double>& buf) {
 int chl_stats(chl_handle* h, int inst, chl_stats_out* out) {
   if (!out || !h) return CHL_E_ARG;
   int rc0 = finish(h);
-  if (rc0 || (rc0 = check_finite(h))) return rc0;
+  if (rc0 || (rc0 = check_finite(h, inst))) return rc0;
   std::vector<double> buf;
   int rc = run_stats(h, inst, buf); if (rc) return rc;
   const Inst& I = h->in[inst];

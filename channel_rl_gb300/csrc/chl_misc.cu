@@ -123,7 +123,7 @@ k_minabs(ChlMap map, int s) {
     mw = x < mw ? x : mw;
   }
   if (lane == 0) swm[warp] = mw;
-  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(I.status, 1);
+  if (__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(I.status, CHL_STATUS_NONFINITE);
   __syncthreads();
   if (threadIdx.x == 0) {
     unsigned long long m = swm[0];

@@ -70,7 +70,7 @@ EXPORTS = (
     "chl_mlp_eval", "chl_tc_selftest",
     "chl_snapshot_dims", "chl_snapshot_read", "chl_snapshot_write", "chl_io_last_error",
     "chl_read_parameters", "chl_save_snapshot", "chl_load_snapshot",
-    "chl_agent_observe", "chl_agent_act",
+    "chl_agent_observe", "chl_agent_act", "chl_status_flags",
 )
 MLP_NPARAM = 4545
 _F32P = C.POINTER(C.c_float)
@@ -85,7 +85,9 @@ def load(build_if_missing=True):
     global _LIB
     if _LIB is not None:
         return _LIB
-    path = _build.LIB
+    # CHL_LIBRARY selects another build of the same ABI (e.g. the
+    # bounds-checked variant); default: the in-tree library
+    path = os.environ.get("CHL_LIBRARY") or _build.LIB
     if not os.path.exists(path):
         if not build_if_missing:
             raise ChlError(f"{path} missing: run channel_rl_gb300.build.build()")
@@ -138,6 +140,7 @@ def load(build_if_missing=True):
     lib.chl_load_snapshot.argtypes = [H, C.c_int, C.c_char_p]
     lib.chl_agent_observe.argtypes = [H, C.c_int, C.c_int, I, _F64P, _F64P, _F64P]
     lib.chl_agent_act.argtypes = [H, C.c_int, C.c_int, _F64P]
+    lib.chl_status_flags.argtypes = [H, C.c_int, C.POINTER(C.c_int)]
     _LIB = lib
     return lib
 
@@ -315,6 +318,13 @@ class Channel:
         """read_input_data (input_output.f90:390-560) into one instance; the
         file's mesh must be the instance's."""
         self._check(self.lib.chl_load_snapshot(self.h, inst, os.fsencode(path)), "chl_load_snapshot")
+
+    def status_flags(self, inst=0):
+        """Status word of an instance (1: non-finite velocity, 4: field index
+        out of range, bounds-checked build only)."""
+        f = C.c_int(0)
+        self._check(self.lib.chl_status_flags(self.h, inst, C.byref(f)), "chl_status_flags")
+        return f.value
 
     def agent_observe(self, nagents, y_ind, y_rand, inst=0):
         """States [2][nagents][6] and rewards [2][nagents] of the wall agents

@@ -103,6 +103,10 @@ int chl_get_wall_stress(chl_handle* h, int inst, double* alpha_x);
 
 /* scalars: [0] dt, [1] t, [2] dPdx, [3] Qflow_x_0 */
 int chl_get_scalars(chl_handle* h, int inst, double* out4);
+/* Status word of an instance: bit 0 (1) non-finite velocity found by the
+ * CFL pass, bit 2 (4) an out-of-range field index (only the bounds-checked
+ * build checks; it clamps the index and records it here).  Cleared by upload. */
+int chl_status_flags(chl_handle* h, int inst, int* flags);
 int chl_set_scalars(chl_handle* h, int inst, const double* in4);
 
 /* compute_dt (time_integration.f90:102-150), all instances. */

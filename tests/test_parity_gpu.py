@@ -4,6 +4,7 @@ Tolerance: relative max error <= 1e-12 on every velocity and pressure field
 (FIELD_RTOL), <= 1e-10 on nu_t of the dynamic model (NUT_RTOL, see helpers).
 """
 import os
+from dataclasses import replace
 
 import numpy as np
 import pytest
@@ -214,3 +215,34 @@ def test_non_finite_velocity_is_reported():
     ch.synchronize()
     assert np.isfinite(ch.download()["U"]).all()
     ch.close()
+
+
+def test_non_finite_instance_is_isolated_in_a_batch():
+    """One channel of a batch carries a NaN: the batch-wide check names it,
+    the others stay readable and advance exactly as they do alone."""
+    from channel_rl_gb300.host import ChlError
+    batch = [C.smaller(C.c2_wm64(), 32, 16, 16), C.smaller(C.c1_small(), 16, 12, 16),
+             C.smaller(C.c3_roofline(les=C.LES_DSM), 24, 16, 32)]
+    batch = [b if q != 1 else replace(b, wall_model=C.WM_EQLOG, Retau=2000.0, x_mass_cte=1)
+             for q, b in enumerate(batch)]
+    chb = _channel(batch)
+    for q, c in enumerate(batch):
+        U, V, W = C.initial_fields(c)
+        if q == 1:
+            U = U.copy()
+            U[3, 4, 5] = np.inf
+        chb.upload(U, V, W, inst=q)
+    chb.step(3)
+    with pytest.raises(ChlError, match="instance 1"):
+        chb.synchronize()
+    with pytest.raises(ChlError, match="non-finite"):
+        chb.download(inst=1)
+    for q in (0, 2):
+        ch = _channel(batch[q])
+        ch.upload(*C.initial_fields(batch[q]))
+        ch.step(3)
+        a, b = chb.download(inst=q), ch.download()
+        for f in "UVW":
+            assert np.array_equal(a[f], b[f]), (q, f)
+        ch.close()
+    chb.close()
