@@ -124,3 +124,26 @@ __device__ __forceinline__ size_t vidx(const ChlInst& I, int i, int jv, int k) {
 }
 
 #define LDG(p) __ldg(p)
+
+// Programmatic dependent launch inside the step graph: each step kernel is
+// launched with programmatic stream serialisation, so its blocks may be
+// scheduled while the previous kernel drains, and waits here, first thing,
+// until that kernel has finished and its writes are visible.  Without the
+// launch attribute the wait returns at once.
+__device__ __forceinline__ void chl_pdl_wait() {
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 900)
+  cudaGridDependencySynchronize();
+#endif
+}
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t chl_launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                                  Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid; cfg.blockDim = block; cfg.dynamicSmemBytes = smem; cfg.stream = st;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at; cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}

@@ -104,6 +104,7 @@ __device__ __forceinline__ int rows_per_block_x(int Nx) { int cr = 1024 / Nx; re
 //         the pressure BC planes and the BC source terms of pressure.f90:138-139.
 __global__ void __launch_bounds__(256)
 k_div_fftx(ChlMap map, int s_in, int mode) {
+  chl_pdl_wait();
   extern __shared__ double2 sm[];
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
@@ -160,6 +161,7 @@ k_div_fftx(ChlMap map, int s_in, int mode) {
 // ------------------------------------------------------------ z transform of the half spectrum
 __global__ void __launch_bounds__(256)
 k_fftz(ChlMap map, int inv, int zcw) {
+  chl_pdl_wait();
   // zcw kx columns per block (16, fewer for long z lines: chl_fftz_cols)
   extern __shared__ double2 sm[];
   int lb;
@@ -185,6 +187,7 @@ k_fftz(ChlMap map, int inv, int zcw) {
 // ------------------------------------------------------------ tridiagonal per mode
 __global__ void __launch_bounds__(128)
 k_tri(ChlMap map) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
@@ -241,6 +244,7 @@ k_tri(ChlMap map) {
 // ------------------------------------------------------------ inverse x -> pressure field
 __global__ void __launch_bounds__(256)
 k_fftx_inv(ChlMap map, int dst) {
+  chl_pdl_wait();
   extern __shared__ double2 sm[];
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
@@ -278,6 +282,7 @@ k_fftx_inv(ChlMap map, int dst) {
 // project_velocity (projection.f90:192-214) + Dirichlet ghost rows.
 __global__ void __launch_bounds__(256)
 k_project(ChlMap map, int s) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -364,11 +369,11 @@ int chl_fft_setup(size_t smx, size_t smz) {
   cudaError_t e3 = cudaFuncSetAttribute(k_fftz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
   return (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) ? 1 : 0;
 }
-void chl_launch_div_fftx(const ChlMap& m, int nb, size_t smem, int s_in, int mode, cudaStream_t st) { k_div_fftx<<<nb, 256, smem, st>>>(m, s_in, mode); }
-void chl_launch_fftz(const ChlMap& m, int nb, size_t smem, int inv, int zcw, cudaStream_t st) { k_fftz<<<nb, 256, smem, st>>>(m, inv, zcw); }
-void chl_launch_tri(const ChlMap& m, int nb, cudaStream_t st) { k_tri<<<nb, 128, 0, st>>>(m); }
-void chl_launch_fftx_inv(const ChlMap& m, int nb, size_t smem, int dst, cudaStream_t st) { k_fftx_inv<<<nb, 256, smem, st>>>(m, dst); }
-void chl_launch_project(const ChlMap& m, int nb, int s, cudaStream_t st) { k_project<<<nb, 256, 0, st>>>(m, s); }
+void chl_launch_div_fftx(const ChlMap& m, int nb, size_t smem, int s_in, int mode, cudaStream_t st) { chl_launch_pdl(k_div_fftx, dim3(nb), dim3(256), smem, st, m, s_in, mode); }
+void chl_launch_fftz(const ChlMap& m, int nb, size_t smem, int inv, int zcw, cudaStream_t st) { chl_launch_pdl(k_fftz, dim3(nb), dim3(256), smem, st, m, inv, zcw); }
+void chl_launch_tri(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_tri, dim3(nb), dim3(128), 0, st, m); }
+void chl_launch_fftx_inv(const ChlMap& m, int nb, size_t smem, int dst, cudaStream_t st) { chl_launch_pdl(k_fftx_inv, dim3(nb), dim3(256), smem, st, m, dst); }
+void chl_launch_project(const ChlMap& m, int nb, int s, cudaStream_t st) { chl_launch_pdl(k_project, dim3(nb), dim3(256), 0, st, m, s); }
 void chl_launch_pbc(const ChlMap& m, int nb, int s, cudaStream_t st) { k_pbc<<<nb, 256, 0, st>>>(m, s); }
 void chl_launch_pghost(const ChlMap& m, int nb, cudaStream_t st) { k_pghost<<<nb, 256, 0, st>>>(m); }
 }

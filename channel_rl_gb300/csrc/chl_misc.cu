@@ -79,6 +79,7 @@ __device__ __forceinline__ int minabs_chunks(int Ny) { return (Ny + MINABS_ROWS 
 
 __global__ void __launch_bounds__(256)
 k_minabs(ChlMap map, int s) {
+  chl_pdl_wait();
   __shared__ unsigned long long sv[MINABS_ROWS];
   __shared__ unsigned long long swm[8];
   int lb;
@@ -134,6 +135,7 @@ k_minabs(ChlMap map, int s) {
 }
 
 __global__ void k_minabs_init(ChlMap map) {
+  chl_pdl_wait();
   const ChlInst& I = map.inst[blockIdx.x];
   const int n = I.Nx + I.Ny + 1 + I.Nz;
   for (int w = threadIdx.x; w < n; w += blockDim.x) I.minabs[w] = CHL_BIG_BITS;
@@ -141,6 +143,7 @@ __global__ void k_minabs_init(ChlMap map) {
 
 // one block per instance
 __global__ void k_dt(ChlMap map) {
+  chl_pdl_wait();
   const ChlInst& I = map.inst[blockIdx.x];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
   const unsigned long long* g = I.minabs;
@@ -176,6 +179,7 @@ __global__ void k_dt(ChlMap map) {
 // x-z points of rows j_f = 3 and nyg-2, then U += dPdx on the interior
 // (time_integration.f90:89-94); one block per instance for the sum.
 __global__ void k_massflow(ChlMap map, int s, int force) {
+  chl_pdl_wait();
   const ChlInst& I = map.inst[blockIdx.x];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
   if (!I.x_mass_cte && !force) {                 // pressure-gradient forcing: no shift
@@ -204,6 +208,7 @@ __global__ void k_massflow(ChlMap map, int s, int force) {
 
 __global__ void __launch_bounds__(256)
 k_shift(ChlMap map, int s) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -221,6 +226,7 @@ k_shift(ChlMap map, int s) {
 
 // time advance t += dt (compute_time_step_RK3 leaves t = to + rk_t(3)*dt)
 __global__ void k_tadvance(ChlMap map) {
+  chl_pdl_wait();
   const ChlInst& I = map.inst[blockIdx.x];
   if (threadIdx.x == 0) I.scal[CHL_S_T] = I.scal[CHL_S_T] + 1.0 * I.scal[CHL_S_DT];
   // step counter of the wall-model exploration noise (shared by the batch)
@@ -296,13 +302,13 @@ __global__ void k_qflow_final(const ChlInst* inst, int slot) {
 
 extern "C" {
 void chl_launch_minabs(const ChlMap& m, int nb, int s, cudaStream_t st) {
-  k_minabs_init<<<m.n, 128, 0, st>>>(m);
-  k_minabs<<<nb, 256, 0, st>>>(m, s);
+  chl_launch_pdl(k_minabs_init, dim3(m.n), dim3(128), 0, st, m);
+  chl_launch_pdl(k_minabs, dim3(nb), dim3(256), 0, st, m, s);
 }
-void chl_launch_dt(const ChlMap& m, cudaStream_t st) { k_dt<<<m.n, 128, 0, st>>>(m); }
-void chl_launch_massflow(const ChlMap& m, cudaStream_t st, int s, int force) { k_massflow<<<m.n, 256, 0, st>>>(m, s, force); }
-void chl_launch_shift(const ChlMap& m, int nb, int s, cudaStream_t st) { k_shift<<<nb, 256, 0, st>>>(m, s); }
-void chl_launch_tadvance(const ChlMap& m, cudaStream_t st) { k_tadvance<<<m.n, 32, 0, st>>>(m); }
+void chl_launch_dt(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_dt, dim3(m.n), dim3(128), 0, st, m); }
+void chl_launch_massflow(const ChlMap& m, cudaStream_t st, int s, int force) { chl_launch_pdl(k_massflow, dim3(m.n), dim3(256), 0, st, m, s, force); }
+void chl_launch_shift(const ChlMap& m, int nb, int s, cudaStream_t st) { chl_launch_pdl(k_shift, dim3(nb), dim3(256), 0, st, m, s); }
+void chl_launch_tadvance(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_tadvance, dim3(m.n), dim3(32), 0, st, m); }
 void chl_launch_divmax(const ChlMap& m, int s, double* out, cudaStream_t st) { k_divmax<<<m.n, 256, 0, st>>>(m, s, out); }
 void chl_launch_qflow(const ChlInst* inst, int Nz, int s, int slot, cudaStream_t st) {
   k_qflow_part<<<Nz, 256, 0, st>>>(inst, s);

@@ -84,6 +84,7 @@ __device__ __forceinline__ float gauss(unsigned long long seed, unsigned long lo
 
 __global__ void __launch_bounds__(MLP_TILE)
 k_mlp(ChlMap map, MlpArgs A) {
+  chl_pdl_wait();
   extern __shared__ __align__(1024) unsigned char sm[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(sm + S_MISC);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + S_MISC + 16);
@@ -372,13 +373,13 @@ int chl_mlp_setup() {
 }
 void chl_launch_mlp(const ChlMap& m, int nb, int s_in, int stage, int* status, cudaStream_t st) {
   MlpArgs a{nullptr, nullptr, nullptr, nullptr, nullptr, 0, s_in, stage, status};
-  k_mlp<<<nb, MLP_TILE, MLP_SMEM, st>>>(m, a);
+  chl_launch_pdl(k_mlp, dim3(nb), dim3(MLP_TILE), MLP_SMEM, st, m, a);
 }
 void chl_launch_mlp_test(const float* theta, const float* x, const float* g, int P, float* mu, float* trace,
                          int* status, cudaStream_t st) {
   ChlMap m{nullptr, nullptr, 0};
   MlpArgs a{theta, x, g, mu, trace, P, 0, 0, status};
-  k_mlp<<<(P + MLP_TILE - 1) / MLP_TILE, MLP_TILE, MLP_SMEM, st>>>(m, a);
+  chl_launch_pdl(k_mlp, dim3((P + MLP_TILE - 1) / MLP_TILE), dim3(MLP_TILE), MLP_SMEM, st, m, a);
 }
 int chl_tc_selftest_launch(const void* A, const void* B, float* D, int variant, int* status, cudaStream_t st) {
   cudaError_t e = cudaFuncSetAttribute(k_tc_selftest, cudaFuncAttributeMaxDynamicSharedMemorySize, 28672 + 64);

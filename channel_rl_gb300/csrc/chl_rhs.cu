@@ -29,6 +29,7 @@ enum { G_UX = 0, G_VY, G_WZ, G_UZ, G_WX, G_UY, G_VX, G_VZ, G_WY };
 
 __global__ void __launch_bounds__(256)
 k_flux(ChlMap map, int sin) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -106,6 +107,7 @@ struct RhsArgs {
 
 __global__ void __launch_bounds__(256)
 k_rhs_update(ChlMap map, RhsArgs a) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -167,11 +169,11 @@ k_rhs_update(ChlMap map, RhsArgs a) {
 
 extern "C" {
 void chl_launch_flux(const ChlMap& map, int nb_edge, int sin, cudaStream_t st) {
-  k_flux<<<nb_edge, 256, 0, st>>>(map, sin);
+  chl_launch_pdl(k_flux, dim3(nb_edge), dim3(256), 0, st, map, sin);
 }
 void chl_launch_update(const ChlMap& map, int nb_pt, int sbase, int sout, double c1, double c2, int mode,
                        cudaStream_t st) {
   RhsArgs a{sbase, sout, c1, c2, mode};
-  k_rhs_update<<<nb_pt, 256, 0, st>>>(map, a);
+  chl_launch_pdl(k_rhs_update, dim3(nb_pt), dim3(256), 0, st, map, a);
 }
 }

@@ -28,6 +28,7 @@
 // (E13, rows 1..Ny).
 __global__ void __launch_bounds__(256)
 k_edges(ChlMap map, int src) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -85,6 +86,7 @@ __device__ __forceinline__ Strain centre_strain(const ChlInst& I, const double* 
 // q0..2 = 2*(centre velocities), q3..8 = their products, q9..14 = |S|*(d, o).
 __global__ void __launch_bounds__(256)
 k_centre(ChlMap map, int s_in, int dsm) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -124,6 +126,7 @@ __device__ __forceinline__ double fy(const double* f, size_t c, size_t pitch, in
 
 __global__ void __launch_bounds__(256)
 k_filter_y(ChlMap map, int s_in) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -163,6 +166,7 @@ k_filter_y(ChlMap map, int s_in) {
 template <int DIR>
 __global__ void __launch_bounds__(256)
 k_filter_xz(ChlMap map, int from_r) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -204,6 +208,7 @@ k_filter_xz(ChlMap map, int from_r) {
 #define DSM_PPT 4
 __global__ void __launch_bounds__(256)
 k_dsm_final(ChlMap map) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -257,6 +262,7 @@ k_dsm_final(ChlMap map) {
 
 // ------------------------------------------------------------ nu_t coefficient per row
 __global__ void k_coef(ChlMap map) {
+  chl_pdl_wait();
   const ChlInst& I = map.inst[blockIdx.x];
   const int Ny = I.Ny, np = I.npart;
   for (int jc = threadIdx.x; jc < Ny + 2; jc += blockDim.x) {
@@ -319,6 +325,7 @@ __device__ double eqlog_tau(double u, double h, double nu, double guess) {
 }
 
 __global__ void k_eqwm(ChlMap map, int s_in) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -341,6 +348,7 @@ __device__ __forceinline__ double wm_face(const ChlInst& I, const double* U, int
 
 __global__ void __launch_bounds__(256)
 k_nut(ChlMap map, int s_in, int use_wm) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -374,13 +382,13 @@ k_nut(ChlMap map, int s_in, int use_wm) {
 
 // ------------------------------------------------------------ launchers
 extern "C" {
-void chl_launch_edges(const ChlMap& m, int nb, int src, cudaStream_t st) { k_edges<<<nb, 256, 0, st>>>(m, src); }
-void chl_launch_centre(const ChlMap& m, int nb, int s_in, int dsm, cudaStream_t st) { k_centre<<<nb, 256, 0, st>>>(m, s_in, dsm); }
-void chl_launch_filter_y(const ChlMap& m, int nb, int s_in, cudaStream_t st) { k_filter_y<<<nb, 256, 0, st>>>(m, s_in); }
-void chl_launch_filter_x(const ChlMap& m, int nb, cudaStream_t st) { k_filter_xz<0><<<nb, 256, 0, st>>>(m, 1); }
-void chl_launch_filter_z(const ChlMap& m, int nb, cudaStream_t st) { k_filter_xz<1><<<nb, 256, 0, st>>>(m, 0); }
-void chl_launch_dsm_final(const ChlMap& m, int nb, cudaStream_t st) { k_dsm_final<<<nb, 256, 0, st>>>(m); }
-void chl_launch_coef(const ChlMap& m, cudaStream_t st) { k_coef<<<m.n, 128, 0, st>>>(m); }
-void chl_launch_eqwm(const ChlMap& m, int nb, int s_in, cudaStream_t st) { k_eqwm<<<nb, 256, 0, st>>>(m, s_in); }
-void chl_launch_nut(const ChlMap& m, int nb, int s_in, int use_wm, cudaStream_t st) { k_nut<<<nb, 256, 0, st>>>(m, s_in, use_wm); }
+void chl_launch_edges(const ChlMap& m, int nb, int src, cudaStream_t st) { chl_launch_pdl(k_edges, dim3(nb), dim3(256), 0, st, m, src); }
+void chl_launch_centre(const ChlMap& m, int nb, int s_in, int dsm, cudaStream_t st) { chl_launch_pdl(k_centre, dim3(nb), dim3(256), 0, st, m, s_in, dsm); }
+void chl_launch_filter_y(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_filter_y, dim3(nb), dim3(256), 0, st, m, s_in); }
+void chl_launch_filter_x(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<0>, dim3(nb), dim3(256), 0, st, m, 1); }
+void chl_launch_filter_z(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<1>, dim3(nb), dim3(256), 0, st, m, 0); }
+void chl_launch_dsm_final(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_dsm_final, dim3(nb), dim3(256), 0, st, m); }
+void chl_launch_coef(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_coef, dim3(m.n), dim3(128), 0, st, m); }
+void chl_launch_eqwm(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_eqwm, dim3(nb), dim3(256), 0, st, m, s_in); }
+void chl_launch_nut(const ChlMap& m, int nb, int s_in, int use_wm, cudaStream_t st) { chl_launch_pdl(k_nut, dim3(nb), dim3(256), 0, st, m, s_in, use_wm); }
 }

@@ -85,6 +85,7 @@ __device__ __forceinline__ Grad gradients(const ChlInst& I, const double* U, con
 
 __global__ void __launch_bounds__(256)
 k_amd(ChlMap map, int s_in) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -122,6 +123,7 @@ k_amd(ChlMap map, int s_in) {
 
 __global__ void __launch_bounds__(256)
 k_vreman(ChlMap map, int s_in) {
+  chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -155,6 +157,6 @@ k_vreman(ChlMap map, int s_in) {
 }
 
 extern "C" {
-void chl_launch_amd(const ChlMap& m, int nb, int s_in, cudaStream_t st) { k_amd<<<nb, 256, 0, st>>>(m, s_in); }
-void chl_launch_vreman(const ChlMap& m, int nb, int s_in, cudaStream_t st) { k_vreman<<<nb, 256, 0, st>>>(m, s_in); }
+void chl_launch_amd(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_amd, dim3(nb), dim3(256), 0, st, m, s_in); }
+void chl_launch_vreman(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_vreman, dim3(nb), dim3(256), 0, st, m, s_in); }
 }
