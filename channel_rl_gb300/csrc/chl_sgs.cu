@@ -223,13 +223,15 @@ k_dsm_final(ChlMap map) {
     const int i = pidx % Nx, k = pidx / Nx;
     const size_t c = cidx(I, i, jc, k);
     const Strain h = centre_strain(I, R[15], R[16], R[17], i, jc, k);  // 216 x filtered strain
-    const double s4 = 4.0 * h.s;
-    const double M1 = fma(s4, h.d1, -216.0 * LDG(R[9] + c));
-    const double M2 = fma(s4, h.d2, -216.0 * LDG(R[10] + c));
-    const double M3 = fma(s4, h.d3, -216.0 * LDG(R[11] + c));
-    const double M4 = fma(s4, h.o12, -216.0 * LDG(R[12] + c));
-    const double M5 = fma(s4, h.o13, -216.0 * LDG(R[13] + c));
-    const double M6 = fma(s4, h.o23, -216.0 * LDG(R[14] + c));
+    // M_ij / 216: the 216 of the filtered |S| S_ij terms moves into the
+    // strain factor (4/216), and k_coef takes the remaining 1/216
+    const double s4 = h.s * (4.0 / 216.0);
+    const double M1 = fma(s4, h.d1, -LDG(R[9] + c));
+    const double M2 = fma(s4, h.d2, -LDG(R[10] + c));
+    const double M3 = fma(s4, h.d3, -LDG(R[11] + c));
+    const double M4 = fma(s4, h.o12, -LDG(R[12] + c));
+    const double M5 = fma(s4, h.o13, -LDG(R[13] + c));
+    const double M6 = fma(s4, h.o23, -LDG(R[14] + c));
     const double fu = LDG(R[0] + c), fv = LDG(R[1] + c), fw = LDG(R[2] + c);
     const double L1 = fma(216.0, LDG(R[3] + c), -fu * fu);
     const double L2 = fma(216.0, LDG(R[4] + c), -fv * fv);
@@ -274,7 +276,9 @@ __global__ void k_coef(ChlMap map) {
           lm += I.part[(size_t)jc * np + q];
           mm += I.part[(size_t)(Ny + 2) * np + (size_t)jc * np + q];
         }
-        c = -0.125 * (lm / mm);          // -1/2 * <LM>/<MM>, see the scaling note above
+        // -1/2 <LM>/<MM>: the filter and average scales give 1/8 (see the
+        // scaling note above), M is stored / 216, so <LM>/<MM> = 216 lm/mm
+        c = (-0.125 / 216.0) * (lm / mm);
       } else if (I.LES_model == 1) {
         // van Driest: f = 1 - exp(-d/25/(nu/utau)), utau = dPdx^0.5 (subgrid.f90:581-599)
         const double ut = sqrt(I.scal[CHL_S_DPDX]);
