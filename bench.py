@@ -77,6 +77,8 @@ def workload(name):
         return [replace(C.c3_roofline(les=C.LES_DSM), LES_model=C.LES_AMD, name="c3_256x96x192_amd_eqwm")]
     if name == "c3_vreman":
         return [replace(C.c3_roofline(les=C.LES_DSM), LES_model=C.LES_VREMAN, name="c3_256x96x192_vreman_eqwm")]
+    if name == "rl_case":
+        return [C.rl_case()]
     if name == "c3_dsm_small":
         return [C.smaller(C.c3_roofline(les=C.LES_DSM), 128, 96, 96)]
     if name == "c1":

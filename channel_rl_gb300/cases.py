@@ -127,6 +127,15 @@ def c4_ensemble(n=64, seed=4321):
     return out
 
 
+def rl_case(seed=2000):
+    """The size and physics of the reference's own RL cases (its parameter
+    files for Re_tau 2000: 130x41x66 faces = 128x40x64 cells, 2pi x 2 x pi,
+    AMD with Dirichlet nu_t ghosts, pressure-gradient forcing, fixed
+    dt = 1e-2), with the equilibrium wall model setting the wall stress
+    that the reference's agents set."""
+    return replace(wallmodelled("rl_128x40x64_amd", 128, 40, 64, 2000.0, les=LES_AMD, seed=seed), CFL=-1e-2)
+
+
 def c5_learned(n=16, seed=5555):
     """Learned wall model: 16 channels, Re_tau in {2000, 5200, 10000},
     grids 48x48x48 .. 96x64x96."""
