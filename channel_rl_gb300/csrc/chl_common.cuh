@@ -18,6 +18,28 @@
 #include <stdint.h>
 
 #define CHL_NQ 18   // filtered DSM components
+#define CHL_WALL_THREADS 64   // block width of the equilibrium wall-stress solve
+// SMs of a GB300.  The small transforms are cut finer until their grid
+// covers the SMs about four times: with about one block per SM a few SMs
+// run two, and the launch takes twice one block's time.
+#define CHL_SMS 152
+#define CHL_FFT_MIN_BLOCKS (4 * CHL_SMS)
+// complex rows (pairs of real x lines) per x-transform block
+__host__ __device__ inline int chl_fftx_rows(int Nx, int nrow) {
+  int cr = 1024 / Nx;
+  if (cr < 1) cr = 1;
+  while (cr > 1 && (nrow + cr - 1) / cr < CHL_FFT_MIN_BLOCKS) cr >>= 1;
+  return cr;
+}
+// threads of a transform block staging `lines` lines of length n: one
+// radix-4 butterfly each per pass, in whole warps, 64..256
+__host__ __device__ inline int chl_fft_threads(int lines, int n) {
+  int t = (lines * n / 4 + 31) & ~31;
+  return t < 64 ? 64 : (t > 256 ? 256 : t);
+}
+#ifndef CHL_TRI_SMEM_MAX
+#define CHL_TRI_SMEM_MAX (128 * 1024)   // largest staged tridiagonal column block
+#endif
 
 struct ChlInst {
   int Nx, Ny, Nz, Nxh;          // unique cells; Nxh = Nx/2+1

@@ -15,7 +15,8 @@
 //  * y: one thread per mode runs the Thomas elimination with factors
 //    precomputed once per grid (the matrix of a mode never changes between
 //    steps), into which the 1/(Nx*Nz) of the inverse transform and the 2 of
-//    the real-row packing are folded;
+//    the real-row packing are folded; the mode's column is staged in shared
+//    memory by asynchronous copies when it fits;
 //  * the inverse runs the same way back and the x pass writes the pressure.
 #include "chl_common.cuh"
 
@@ -96,7 +97,6 @@ __device__ double2* fft_smem(double2* a, double2* b, int nrows, int rs, int es, 
   return src;
 }
 
-__device__ __forceinline__ int rows_per_block_x(int Nx) { int cr = 1024 / Nx; return cr < 1 ? 1 : cr; }
 
 // ------------------------------------------------------------ divergence + forward x
 // mode 0: div of velocity set s_in (compute_pseudo_pressure_rhs, projection.f90:40-55)
@@ -109,8 +109,8 @@ k_div_fftx(ChlMap map, int s_in, int mode) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
-  const int CR = rows_per_block_x(Nx);
   const int nrow = Ny * (Nz / 2);
+  const int CR = chl_fftx_rows(Nx, nrow);
   const int g0 = lb * CR;
   const int cr_n = min(CR, nrow - g0);
   double2* A = sm;
@@ -162,25 +162,33 @@ k_div_fftx(ChlMap map, int s_in, int mode) {
 __global__ void __launch_bounds__(256)
 k_fftz(ChlMap map, int inv, int zcw) {
   chl_pdl_wait();
-  // zcw kx columns per block (16, fewer for long z lines: chl_fftz_cols)
+  // The Ny x Nxh columns (jc, kx) of an instance are numbered jc-major and
+  // cut into runs of zcw (chl_fftz_cols); a run may cross into the next
+  // jc row, so every column is a full one and only the instance's last
+  // block is short.
   extern __shared__ double2 sm[];
+  __shared__ size_t coff[16];
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nz = I.Nz, Nxh = I.Nxh;
-  const int ncb = (Nxh + zcw - 1) / zcw;
-  const int jc = 1 + lb / ncb, c0 = (lb % ncb) * zcw;
-  const int cw = min(zcw, Nxh - c0);
+  const int q0 = lb * zcw;
+  const int cw = min(zcw, I.Ny * Nxh - q0);
+  if (threadIdx.x < cw) {
+    const int q = q0 + threadIdx.x;
+    coff[threadIdx.x] = (size_t)(1 + q / Nxh) * Nz * Nxh + (q % Nxh);
+  }
+  __syncthreads();
   double2* A = sm;
   double2* B = sm + Nz * zcw;
-  double2* base = I.spec + (size_t)jc * Nz * Nxh + c0;
-  for (int w = threadIdx.x; w < Nz * zcw; w += blockDim.x) {
-    const int k = w / zcw, c = w - k * zcw;
-    A[k * zcw + c] = c < cw ? base[(size_t)k * Nxh + c] : make_double2(0.0, 0.0);
+  double2* spec = I.spec;
+  for (int w = threadIdx.x; w < Nz * cw; w += blockDim.x) {
+    const int k = w / cw, c = w - k * cw;
+    A[k * zcw + c] = spec[coff[c] + (size_t)k * Nxh];
   }
-  double2* res = fft_smem(A, B, zcw, 1, zcw, Nz, I.twz, inv != 0);
-  for (int w = threadIdx.x; w < Nz * zcw; w += blockDim.x) {
-    const int k = w / zcw, c = w - k * zcw;
-    if (c < cw) base[(size_t)k * Nxh + c] = res[k * zcw + c];
+  double2* res = fft_smem(A, B, cw, 1, zcw, Nz, I.twz, inv != 0);
+  for (int w = threadIdx.x; w < Nz * cw; w += blockDim.x) {
+    const int k = w / cw, c = w - k * cw;
+    spec[coff[c] + (size_t)k * Nxh] = res[k * zcw + c];
   }
 }
 
@@ -241,6 +249,72 @@ k_tri(ChlMap map) {
   }
 }
 
+// Staged form, for columns that fit in shared memory.  One warp of TRI_W
+// modes per block.  Each thread copies its own mode's Ny rows of right side
+// and factors into shared memory with cp.async (all rows in flight at once,
+// where the form above waits once per TB rows), runs both sweeps there and
+// writes only the solution.  A thread reads back only what it copied
+// itself, so the copies need a wait but no block barrier.  The arithmetic
+// and its order are those of k_tri.
+#define TRI_W 32
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" :: "r"(s), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* sdst, const void* gsrc) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" :: "r"(s), "l"(gsrc) : "memory");
+}
+
+__global__ void __launch_bounds__(TRI_W)
+k_tri_staged(ChlMap map) {
+  chl_pdl_wait();
+  extern __shared__ double2 smt[];
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
+  const int t = threadIdx.x;
+  const int mode = lb * TRI_W + t;
+  if (mode >= Nz * Nxh) return;
+  const size_t ps = (size_t)Nz * Nxh;
+  double2* __restrict__ s = I.spec + ps + mode;  // row jc = 1
+  // [Ny][TRI_W] right side, then [Ny][TRI_W] x (inv, m, c) as doubles
+  double2* sd = smt;
+  double* sf = reinterpret_cast<double*>(smt + (size_t)Ny * TRI_W);
+  double* si = sf;
+  double* sm = sf + (size_t)Ny * TRI_W;
+  double* sc = sf + (size_t)2 * Ny * TRI_W;
+  for (int j = 0; j < Ny; ++j) {
+    const size_t g = (size_t)j * ps, l = (size_t)j * TRI_W + t;
+    cp_async16(sd + l, s + g);
+    cp_async8(si + l, I.tri_inv + mode + g);
+    cp_async8(sm + l, I.tri_m + mode + g);
+    cp_async8(sc + l, I.tri_c + mode + g);
+  }
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+  double2 prev = make_double2(0.0, 0.0);
+  for (int j = 0; j < Ny; ++j) {
+    const size_t l = (size_t)j * TRI_W + t;
+    double2 d = sd[l];
+    const double iv = si[l], m = sm[l];
+    d.x = fma(d.x, iv, -m * prev.x);   // m = 0 on the first row
+    d.y = fma(d.y, iv, -m * prev.y);
+    prev = d;
+    sd[l] = d;
+  }
+  s[(size_t)(Ny - 1) * ps] = prev;
+  for (int j = Ny - 2; j >= 0; --j) {
+    const size_t l = (size_t)j * TRI_W + t;
+    double2 d = sd[l];
+    const double c = sc[l];
+    d.x = fma(-c, prev.x, d.x);
+    d.y = fma(-c, prev.y, d.y);
+    prev = d;
+    s[(size_t)j * ps] = d;
+  }
+}
+
 // ------------------------------------------------------------ inverse x -> pressure field
 __global__ void __launch_bounds__(256)
 k_fftx_inv(ChlMap map, int dst) {
@@ -249,8 +323,8 @@ k_fftx_inv(ChlMap map, int dst) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
-  const int CR = rows_per_block_x(Nx);
   const int nrow = Ny * (Nz / 2);
+  const int CR = chl_fftx_rows(Nx, nrow);
   const int g0 = lb * CR;
   const int cr_n = min(CR, nrow - g0);
   double2* A = sm;
@@ -354,25 +428,46 @@ __global__ void k_pghost(ChlMap map) {
 }
 
 extern "C" {
-size_t chl_smem_fftx(int maxNx) { int cr = 1024 / maxNx; if (cr < 1) cr = 1; return (size_t)2 * cr * maxNx * sizeof(double2); }
+size_t chl_smem_fftx(int Nx, int nrow) { return (size_t)2 * chl_fftx_rows(Nx, nrow) * Nx * sizeof(double2); }
 size_t chl_smem_fftz(int maxNz, int zcw) { return (size_t)2 * maxNz * zcw * sizeof(double2); }
 // kx columns staged per z-transform block: 16, halved while two Nz x cols
-// complex tiles would exceed the 227 KB a block may use
-int chl_fftz_cols(int maxNz) {
+// complex tiles would exceed the 227 KB a block may use, and halved (down
+// to 2) while the grid over all `ncols` columns would cover the SMs less
+// than about four times
+int chl_fftz_cols(int maxNz, long ncols) {
   int c = 16;
   while (c > 1 && chl_smem_fftz(maxNz, c) > (size_t)227 * 1024) c /= 2;
+  while (c > 2 && (ncols + c - 1) / c < CHL_FFT_MIN_BLOCKS) c /= 2;
   return c;
 }
-int chl_fft_setup(size_t smx, size_t smz) {
+int chl_fft_setup(size_t smx, size_t smz, size_t smt) {
   cudaError_t e1 = cudaFuncSetAttribute(k_div_fftx, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
   cudaError_t e2 = cudaFuncSetAttribute(k_fftx_inv, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smx);
   cudaError_t e3 = cudaFuncSetAttribute(k_fftz, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smz);
-  return (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess) ? 1 : 0;
+  cudaError_t e4 = smt ? cudaFuncSetAttribute(k_tri_staged, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt)
+                       : cudaSuccess;
+  return (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) ? 1 : 0;
 }
-void chl_launch_div_fftx(const ChlMap& m, int nb, size_t smem, int s_in, int mode, cudaStream_t st) { chl_launch_pdl(k_div_fftx, dim3(nb), dim3(256), smem, st, m, s_in, mode); }
-void chl_launch_fftz(const ChlMap& m, int nb, size_t smem, int inv, int zcw, cudaStream_t st) { chl_launch_pdl(k_fftz, dim3(nb), dim3(256), smem, st, m, inv, zcw); }
-void chl_launch_tri(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_tri, dim3(nb), dim3(128), 0, st, m); }
-void chl_launch_fftx_inv(const ChlMap& m, int nb, size_t smem, int dst, cudaStream_t st) { chl_launch_pdl(k_fftx_inv, dim3(nb), dim3(256), smem, st, m, dst); }
+void chl_launch_div_fftx(const ChlMap& m, int nb, int nt, size_t smem, int s_in, int mode, cudaStream_t st) { chl_launch_pdl(k_div_fftx, dim3(nb), dim3(nt), smem, st, m, s_in, mode); }
+void chl_launch_fftz(const ChlMap& m, int nb, int nt, size_t smem, int inv, int zcw, cudaStream_t st) { chl_launch_pdl(k_fftz, dim3(nb), dim3(nt), smem, st, m, inv, zcw); }
+// smem > 0: the staged form with TRI_W-mode blocks (chl_tri_modes_per_block)
+void chl_launch_tri(const ChlMap& m, int nb, size_t smem, cudaStream_t st) {
+  if (smem) chl_launch_pdl(k_tri_staged, dim3(nb), dim3(TRI_W), smem, st, m);
+  else chl_launch_pdl(k_tri, dim3(nb), dim3(128), 0, st, m);
+}
+// Shared memory of the staged form for the tallest column (40 bytes per
+// row and mode), or 0 for the row-batched form.  The staged form has one
+// warp per block, so it pays only while all `modes` fit in one wave of
+// resident blocks; beyond that the row-batched form keeps more warps per SM.
+size_t chl_smem_tri(int maxNy, long modes) {
+  const size_t b = (size_t)maxNy * TRI_W * (sizeof(double2) + 3 * sizeof(double));
+  if (b > (size_t)CHL_TRI_SMEM_MAX) return 0;
+  const long per_sm = (long)((228 * 1024) / (b + 1024));   // + the 1 KB the runtime reserves per block
+  const long blocks = (modes + TRI_W - 1) / TRI_W;
+  return blocks <= per_sm * CHL_SMS ? b : 0;
+}
+int chl_tri_modes_per_block(size_t smem) { return smem ? TRI_W : 128; }
+void chl_launch_fftx_inv(const ChlMap& m, int nb, int nt, size_t smem, int dst, cudaStream_t st) { chl_launch_pdl(k_fftx_inv, dim3(nb), dim3(nt), smem, st, m, dst); }
 void chl_launch_project(const ChlMap& m, int nb, int s, cudaStream_t st) { chl_launch_pdl(k_project, dim3(nb), dim3(256), 0, st, m, s); }
 void chl_launch_pbc(const ChlMap& m, int nb, int s, cudaStream_t st) { k_pbc<<<nb, 256, 0, st>>>(m, s); }
 void chl_launch_pghost(const ChlMap& m, int nb, cudaStream_t st) { k_pghost<<<nb, 256, 0, st>>>(m); }

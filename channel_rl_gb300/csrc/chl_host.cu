@@ -29,14 +29,16 @@ void chl_launch_nut(const ChlMap&, int, int, int, cudaStream_t);
 void chl_launch_amd(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_vreman(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_agent_obs(const ChlInst*, int, int, double, const int*, const double*, double*, double*, cudaStream_t);
-size_t chl_smem_fftx(int);
+size_t chl_smem_fftx(int, int);
 size_t chl_smem_fftz(int, int);
-int chl_fftz_cols(int);
-int chl_fft_setup(size_t, size_t);
-void chl_launch_div_fftx(const ChlMap&, int, size_t, int, int, cudaStream_t);
-void chl_launch_fftz(const ChlMap&, int, size_t, int, int, cudaStream_t);
-void chl_launch_tri(const ChlMap&, int, cudaStream_t);
-void chl_launch_fftx_inv(const ChlMap&, int, size_t, int, cudaStream_t);
+int chl_fftz_cols(int, long);
+int chl_fft_setup(size_t, size_t, size_t);
+size_t chl_smem_tri(int, long);
+int chl_tri_modes_per_block(size_t);
+void chl_launch_div_fftx(const ChlMap&, int, int, size_t, int, int, cudaStream_t);
+void chl_launch_fftz(const ChlMap&, int, int, size_t, int, int, cudaStream_t);
+void chl_launch_tri(const ChlMap&, int, size_t, cudaStream_t);
+void chl_launch_fftx_inv(const ChlMap&, int, int, size_t, int, cudaStream_t);
 void chl_launch_project(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_pbc(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_pghost(const ChlMap&, int, cudaStream_t);
@@ -44,6 +46,7 @@ void chl_launch_unpack(double*, const double*, int, int, int, int, int, int, cud
 void chl_launch_pack(double*, const double*, int, int, int, int, int, int, double, cudaStream_t);
 void chl_launch_pack_unique(double*, const double*, int, int, int, int, int, cudaStream_t);
 void chl_launch_minabs(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_nonfinite(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_dt(const ChlMap&, cudaStream_t);
 void chl_launch_massflow(const ChlMap&, cudaStream_t, int, int);
 void chl_launch_shift(const ChlMap&, int, int, cudaStream_t);
@@ -62,7 +65,7 @@ namespace {
 constexpr double RK_T[3] = {8.0 / 15.0, 2.0 / 3.0, 1.0};
 constexpr double RK_C[3][3] = {{8.0 / 15.0, 0.0, 0.0}, {1.0 / 4.0, 5.0 / 12.0, 0.0}, {1.0 / 4.0, 0.0, 3.0 / 4.0}};
 
-enum { M_PT, M_EDGE, M_FULL, M_DSMF, M_WALL, M_PLANE, M_FFTX, M_FFTZ, M_TRI, M_MINABS, M_ROWS, M_MLP, NMAP };
+enum { M_PT, M_EDGE, M_FULL, M_DSMF, M_WALL, M_PLANE, M_FFTX, M_FFTZ, M_TRI, M_MINABS, M_ROWS, M_MLP, M_WALLN, NMAP };
 constexpr int MLP_NPARAM = 4545;
 
 // Grid constants of one instance (host, FP64), in the device index
@@ -194,7 +197,6 @@ struct Arena {
 };
 
 int dsm_npart(int Nx, int Nz) { return (Nx * Nz + 256 * 4 - 1) / (256 * 4); }
-int fftx_rows(int Nx) { int cr = 1024 / Nx; return cr < 1 ? 1 : cr; }
 
 }  // namespace
 
@@ -211,8 +213,9 @@ struct chl_handle {
   std::string err;
   int* d_off[NMAP] = {};
   int nblk[NMAP] = {};
-  size_t smem_x = 0, smem_z = 0;
+  size_t smem_x = 0, smem_z = 0, smem_t = 0;
   int zcw = 16;                       // kx columns per z-transform block
+  int tx = 256, tz = 256;             // threads of the x and z transform blocks
   int LES_model = 0, wall_model = 0, any_mass = 0;
   float* d_mlp_theta = nullptr;       // learned wall model parameters (shared)
   unsigned int* d_mlp_cfg = nullptr;  // sigma, train, seed lo/hi, evaluation counter
@@ -374,9 +377,22 @@ static int upload_consts(chl_handle* h, Inst& I) {
 static int build_maps(chl_handle* h) {
   const int n = (int)h->in.size();
   auto cdiv = [](long a, long b) { return (int)((a + b - 1) / b); };
-  int mz = 0;
-  for (auto& I : h->in) mz = std::max(mz, I.c.Nz);
-  h->zcw = chl_fftz_cols(mz);
+  int mz = 0, my = 0;
+  long zcols = 0, modes = 0;
+  for (auto& I : h->in) {
+    mz = std::max(mz, I.c.Nz); my = std::max(my, I.c.Ny);
+    zcols += (long)I.c.Ny * I.c.Nxh;
+    modes += (long)I.c.Nz * I.c.Nxh;
+  }
+  h->zcw = chl_fftz_cols(mz, zcols);
+  h->tz = chl_fft_threads(h->zcw, mz);
+  h->tx = 64;
+  for (auto& I : h->in) {
+    const int nrow = I.c.Ny * (I.c.Nz / 2);
+    h->tx = std::max(h->tx, chl_fft_threads(chl_fftx_rows(I.c.Nx, nrow), I.c.Nx));
+  }
+  h->smem_t = chl_smem_tri(my, modes);
+  const int tri_w = chl_tri_modes_per_block(h->smem_t);
   for (int m = 0; m < NMAP; ++m) {
     std::vector<int> off(n + 1, 0);
     for (int q = 0; q < n; ++q) {
@@ -390,12 +406,13 @@ static int build_maps(chl_handle* h) {
         case M_DSMF: b = Ny * dsm_npart(Nx, Nz); break;
         case M_WALL: b = cdiv(2L * Nx * Nz, 256); break;
         case M_PLANE: b = cdiv((long)Nx * Nz, 256); break;
-        case M_FFTX: b = cdiv((long)Ny * (Nz / 2), fftx_rows(Nx)); break;
-        case M_FFTZ: b = Ny * cdiv(Nxh, h->zcw); break;
-        case M_TRI: b = cdiv((long)Nz * Nxh, 128); break;
+        case M_FFTX: b = cdiv((long)Ny * (Nz / 2), chl_fftx_rows(Nx, Ny * (Nz / 2))); break;
+        case M_FFTZ: b = cdiv((long)Ny * Nxh, h->zcw); break;
+        case M_TRI: b = cdiv((long)Nz * Nxh, tri_w); break;
         case M_MINABS: b = Nz * ((Ny + 15) / 16); break;   // planes x 16-row chunks (chl_misc.cu)
         case M_ROWS: b = Ny + 1; break;
         case M_MLP: b = cdiv(2L * Nx * Nz, 128); break;
+        case M_WALLN: b = cdiv(2L * Nx * Nz, CHL_WALL_THREADS); break;
       }
       off[q + 1] = off[q] + b;
     }
@@ -405,12 +422,12 @@ static int build_maps(chl_handle* h) {
   }
   // dynamic shared memory is per launch, so it must hold the largest
   // per-instance need: the x transform of an instance stages
-  // fftx_rows(Nx) rows of Nx, which is not monotonic in Nx
+  // chl_fftx_rows rows of Nx, which is not monotonic in Nx
   size_t sx = 0;
-  for (auto& I : h->in) sx = std::max(sx, chl_smem_fftx(I.c.Nx));
+  for (auto& I : h->in) sx = std::max(sx, chl_smem_fftx(I.c.Nx, I.c.Ny * (I.c.Nz / 2)));
   h->smem_x = sx;
   h->smem_z = chl_smem_fftz(mz, h->zcw);
-  if (chl_fft_setup(h->smem_x, h->smem_z)) { h->err = "FFT shared-memory size not supported"; return CHL_E_ARG; }
+  if (chl_fft_setup(h->smem_x, h->smem_z, h->smem_t)) { h->err = "FFT shared-memory size not supported"; return CHL_E_ARG; }
   if (chl_mlp_setup()) { h->err = "wall-model network shared-memory size not supported"; return CHL_E_ARG; }
   return CHL_OK;
 }
@@ -436,7 +453,7 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
   }
   KL("nut_coef", chl_launch_coef(h->map(M_PT), st));
   if (with_wm && (h->wall_model == CHL_WM_EQLOG || h->wall_model == CHL_WM_MLP))
-    KL("eq_wallmodel", chl_launch_eqwm(h->map(M_WALL), h->nblk[M_WALL], s, st));
+    KL("eq_wallmodel", chl_launch_eqwm(h->map(M_WALLN), h->nblk[M_WALLN], s, st));
   if (with_wm && h->wall_model == CHL_WM_MLP)
     KL("mlp_wallmodel", chl_launch_mlp(h->map(M_MLP), h->nblk[M_MLP], s, stage, h->d_mlp_status, st));
   KL("nut", chl_launch_nut(h->map(M_FULL), h->nblk[M_FULL], s, with_wm ? 1 : 0, st));
@@ -446,18 +463,21 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
 
 static int enqueue_projection(chl_handle* h, int s, int mode) {
   cudaStream_t st = h->st;
-  KL("div_fft_x", chl_launch_div_fftx(h->map(M_FFTX), h->nblk[M_FFTX], h->smem_x, s, mode, st));
-  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 0, h->zcw, st));
-  KL("tridiag", chl_launch_tri(h->map(M_TRI), h->nblk[M_TRI], st));
-  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->smem_z, 1, h->zcw, st));
-  KL("ifft_x", chl_launch_fftx_inv(h->map(M_FFTX), h->nblk[M_FFTX], h->smem_x, mode == 0 ? 0 : 1, st));
+  KL("div_fft_x", chl_launch_div_fftx(h->map(M_FFTX), h->nblk[M_FFTX], h->tx, h->smem_x, s, mode, st));
+  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->tz, h->smem_z, 0, h->zcw, st));
+  KL("tridiag", chl_launch_tri(h->map(M_TRI), h->nblk[M_TRI], h->smem_t, st));
+  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->tz, h->smem_z, 1, h->zcw, st));
+  KL("ifft_x", chl_launch_fftx_inv(h->map(M_FFTX), h->nblk[M_FFTX], h->tx, h->smem_x, mode == 0 ? 0 : 1, st));
   if (mode == 0) KL("project", chl_launch_project(h->map(M_PT), h->nblk[M_PT], s, st));
   LAUNCHED();
   return CHL_OK;
 }
 
 static int enqueue_dt(chl_handle* h) {
-  KL("dt_minabs", chl_launch_minabs(h->map(M_MINABS), h->nblk[M_MINABS], 0, h->st));
+  bool fixed = true;   // every instance on a fixed step: only the non-finite check
+  for (auto& I : h->in) fixed = fixed && I.d.CFL < 0.0;
+  if (fixed) KL("dt_minabs", chl_launch_nonfinite(h->map(M_PT), h->nblk[M_PT], 0, h->st));
+  else KL("dt_minabs", chl_launch_minabs(h->map(M_MINABS), h->nblk[M_MINABS], 0, h->st));
   KL("dt", chl_launch_dt(h->map(M_PT), h->st));
   LAUNCHED();
   return CHL_OK;
@@ -886,7 +906,7 @@ int chl_compute_eddy_viscosity(chl_handle* h) {
 
 int chl_compute_wall_model(chl_handle* h) {
   int rc = check_ready(h); if (rc) return rc;
-  if (h->wall_model >= CHL_WM_EQLOG) chl_launch_eqwm(h->map(M_WALL), h->nblk[M_WALL], 0, h->st);
+  if (h->wall_model >= CHL_WM_EQLOG) chl_launch_eqwm(h->map(M_WALLN), h->nblk[M_WALLN], 0, h->st);
   if (h->wall_model == CHL_WM_MLP) chl_launch_mlp(h->map(M_MLP), h->nblk[M_MLP], 0, 0, h->d_mlp_status, h->st);
   chl_launch_nut(h->map(M_FULL), h->nblk[M_FULL], 0, h->wall_model != CHL_WM_NONE ? 1 : 0, h->st);
   LAUNCHED();

@@ -99,22 +99,31 @@ k_minabs(ChlMap map, int s) {
   for (int i = threadIdx.x; i < nxr; i += blockDim.x) {
     const bool ok = i < Nx;
     unsigned long long mu = CHL_BIG_BITS;
-    for (int jc = j0; jc <= j1; ++jc) {
-      unsigned long long bv = CHL_BIG_BITS;
-      if (ok) {
+    // all rows of the chunk are loaded before any reduction, so the loads
+    // are in flight together (the shared atomics would otherwise order them)
+    unsigned long long bv[MINABS_ROWS];
+#pragma unroll
+    for (int r = 0; r < MINABS_ROWS; ++r) {
+      const int jc = j0 + r;
+      bv[r] = CHL_BIG_BITS;
+      if (ok && jc <= j1) {
         const unsigned long long bu = absbits(U[cidx(I, i, jc, k)]);
         const unsigned long long bw = absbits(W[cidx(I, i, jc, k)]);
-        bv = absbits(V[vidx(I, i, jc, k)]);
+        bv[r] = absbits(V[vidx(I, i, jc, k)]);
         mu = bu < mu ? bu : mu;
         mw = bw < mw ? bw : mw;
-        bad |= (bu >= CHL_BIG_BITS) | (bw >= CHL_BIG_BITS) | (bv >= CHL_BIG_BITS);
+        bad |= (bu >= CHL_BIG_BITS) | (bw >= CHL_BIG_BITS) | (bv[r] >= CHL_BIG_BITS);
       }
+    }
+#pragma unroll
+    for (int r = 0; r < MINABS_ROWS; ++r) {
+      unsigned long long b = bv[r];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long x = __shfl_xor_sync(0xffffffffu, bv, o);
-        bv = x < bv ? x : bv;
+        const unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
+        b = x < b ? x : b;
       }
-      if (lane == 0) atomicMin(sv + (jc - j0), bv);
+      if (lane == 0 && j0 + r <= j1) atomicMin(sv + r, b);
     }
     if (ok) atomicMin(g + i, mu);
   }
@@ -134,6 +143,30 @@ k_minabs(ChlMap map, int s) {
   if (threadIdx.x <= j1 - j0) atomicMin(g + Nx + j0 + threadIdx.x, sv[threadIdx.x]);
 }
 
+// With a fixed time step the minima are not needed (compute_dt reduces them
+// and then replaces dt by -CFL, time_integration.f90:146-148); what the pass
+// must still do is flag non-finite velocities.  One thread per centre
+// (i, jc, k), jc = 1..Ny, reading the same U, V, W entries as k_minabs.
+__global__ void __launch_bounds__(256)
+k_nonfinite(ChlMap map, int s) {
+  chl_pdl_wait();
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const long t = (long)lb * blockDim.x + threadIdx.x;
+  bool bad = false;
+  if (t < (long)Nx * Ny * Nz) {
+    const int i = (int)(t % Nx);
+    const int jc = 1 + (int)((t / Nx) % Ny);
+    const int k = (int)(t / ((long)Nx * Ny));
+    const unsigned long long bu = absbits(I.U[s][cidx(I, i, jc, k)]);
+    const unsigned long long bv = absbits(I.V[s][vidx(I, i, jc, k)]);
+    const unsigned long long bw = absbits(I.W[s][cidx(I, i, jc, k)]);
+    bad = (bu >= CHL_BIG_BITS) | (bv >= CHL_BIG_BITS) | (bw >= CHL_BIG_BITS);
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(I.status, CHL_STATUS_NONFINITE);
+}
+
 __global__ void k_minabs_init(ChlMap map) {
   chl_pdl_wait();
   const ChlInst& I = map.inst[blockIdx.x];
@@ -141,13 +174,27 @@ __global__ void k_minabs_init(ChlMap map) {
   for (int w = threadIdx.x; w < n; w += blockDim.x) I.minabs[w] = CHL_BIG_BITS;
 }
 
-// one block per instance
-__global__ void k_dt(ChlMap map) {
+// One block of 128 threads per instance.  With a fixed time step (CFL < 0)
+// the step is -CFL whatever the velocities, so nothing is reduced.  The
+// maxima are formed by warp shuffles and one pass over the four warps'
+// results (a serial pass over 128 entries costs more than the whole rest).
+__device__ __forceinline__ double warp_fmax(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__global__ void __launch_bounds__(128)
+k_dt(ChlMap map) {
   chl_pdl_wait();
   const ChlInst& I = map.inst[blockIdx.x];
+  if (I.CFL < 0.0) {
+    if (threadIdx.x == 0) I.scal[CHL_S_DT] = -I.CFL;
+    return;
+  }
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
   const unsigned long long* g = I.minabs;
-  __shared__ double r[3][128];
+  __shared__ double r[3][4];
   double lu = 0.0, lv = 0.0, lw = 0.0;
   // U: faces i_f = 2..nxg-1 (my 0..Nx, face Nx is the copy of face 0)
   for (int i = threadIdx.x; i <= Nx; i += blockDim.x)
@@ -158,10 +205,12 @@ __global__ void k_dt(ChlMap map) {
   // W: faces k_f = 2..nzg-1 (my 0..Nz)
   for (int k = threadIdx.x; k <= Nz; k += blockDim.x)
     lw = fmax(lw, I.dzf[k] / __longlong_as_double((long long)g[Nx + Ny + 1 + (k == Nz ? 0 : k)]));
-  r[0][threadIdx.x] = lu; r[1][threadIdx.x] = lv; r[2][threadIdx.x] = lw;
+  lu = warp_fmax(lu); lv = warp_fmax(lv); lw = warp_fmax(lw);
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { r[0][warp] = lu; r[1][warp] = lv; r[2][warp] = lw; }
   __syncthreads();
   if (threadIdx.x == 0) {
-    for (int w = 1; w < blockDim.x; ++w) {
+    for (int w = 1; w < 4; ++w) {
       lu = fmax(lu, r[0][w]); lv = fmax(lv, r[1][w]); lw = fmax(lw, r[2][w]);
     }
     const double C = I.CFL, nu = I.nu;
@@ -169,7 +218,6 @@ __global__ void k_dt(ChlMap map) {
     const double dt_vis = fmin(fmin(C * I.dxmin * I.dxmin / nu, C * I.dymin * I.dymin / nu), C * I.dzmin * I.dzmin / nu);
     double dt = fmin(dt_conv, dt_vis);
     dt = fmin(dt, 1e-3);
-    if (C < 0.0) dt = -C;
     I.scal[CHL_S_DT] = dt;
   }
 }
@@ -304,6 +352,10 @@ extern "C" {
 void chl_launch_minabs(const ChlMap& m, int nb, int s, cudaStream_t st) {
   chl_launch_pdl(k_minabs_init, dim3(m.n), dim3(128), 0, st, m);
   chl_launch_pdl(k_minabs, dim3(nb), dim3(256), 0, st, m, s);
+}
+// nb: blocks of 256 centres (the point map)
+void chl_launch_nonfinite(const ChlMap& m, int nb, int s, cudaStream_t st) {
+  chl_launch_pdl(k_nonfinite, dim3(nb), dim3(256), 0, st, m, s);
 }
 void chl_launch_dt(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_dt, dim3(m.n), dim3(128), 0, st, m); }
 void chl_launch_massflow(const ChlMap& m, cudaStream_t st, int s, int force) { chl_launch_pdl(k_massflow, dim3(m.n), dim3(256), 0, st, m, s, force); }

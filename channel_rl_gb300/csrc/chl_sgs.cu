@@ -299,36 +299,46 @@ __global__ void k_coef(ChlMap map) {
 #define EQWM_B 5.2
 #define EQWM_ITERS 12
 // Newton on f(ut) = ut (ln(h ut/nu)/kappa + B) - |u|.  f is convex and
-// increasing, so from any start right of the root the iterates decrease
-// monotonically; `guess` (the previous stage's u_tau, when it lies right of
-// the root) saves most iterations.  The iteration stops when the update is
-// below 4 ulp; the root agrees with a fixed-count solve to rounding.
+// increasing, so Newton converges from either side of the root (from the
+// left the first step lands right of it, then the iterates decrease).  The
+// start is `guess` (the previous stage's u_tau) when it lies above the
+// laminar estimate, which the root always does.  Convergence is quadratic
+// with relative constant 1/(2 kappa f') < 0.1, so once a correction is below
+// 1e-9 of ut the next one would be below 1e-19: the iteration stops there
+// and the root agrees with a fixed-count solve to rounding.  The log of the
+// branch test is reused as the first iterate's when the start is laminar.
+// FP64 is the scarce pipe here: h/nu is formed once, 1/kappa is a constant
+// multiplier, and each iteration holds one log and one division.
 __device__ double eqlog_tau(double u, double h, double nu, double guess) {
+  const double inv_k = 1.0 / EQWM_KAPPA;   // folded at compile time
   const double au = fabs(u);
-  const double ut_lam = sqrt(nu * au / h);
-  const double yp_lam = h * ut_lam / nu;
-  const double f0 = ut_lam * (log(yp_lam) / EQWM_KAPPA + EQWM_B) - au;
+  const double hn = h / nu;
+  const double ut_lam = sqrt(au / hn);
+  const double yp_lam = hn * ut_lam;
+  const double l0 = log(yp_lam);
+  const double f0 = ut_lam * fma(l0, inv_k, EQWM_B) - au;
   double ut = ut_lam;
   // log law only above its upper crossing with u+ = y+ (y+ ~ 11)
   if (f0 < 0.0 && yp_lam >= 1.0) {
-    if (guess > ut_lam) {
-      const double fg = guess * (log(h * guess / nu) / EQWM_KAPPA + EQWM_B) - au;
-      if (fg >= 0.0) ut = guess;
-    }
+    const bool warm = guess > ut_lam;
+    if (warm) ut = guess;
     for (int it = 0; it < 2 * EQWM_ITERS; ++it) {
-      const double lg = log(h * ut / nu);
-      const double f = ut * (lg / EQWM_KAPPA + EQWM_B) - au;
-      const double fp = lg / EQWM_KAPPA + EQWM_B + 1.0 / EQWM_KAPPA;
-      const double d = f / fp;
+      const double lg = (it == 0 && !warm) ? l0 : log(hn * ut);
+      const double g = fma(lg, inv_k, EQWM_B);          // u+ at ut
+      const double d = fma(ut, g, -au) / (g + inv_k);   // f / f'
       ut = ut - d;
-      if (fabs(d) <= 9e-16 * ut) break;
+      if (fabs(d) <= 1e-9 * ut) break;
     }
   }
   const double tau = ut * ut;
   return u < 0.0 ? -tau : (u > 0.0 ? tau : 0.0);
 }
 
-__global__ void k_eqwm(ChlMap map, int s_in) {
+// CHL_WALL_THREADS-wide blocks: the 2 Nx Nz wall points of a small channel
+// are few, and the serial Newton chains are FP64-issue bound, so they are
+// spread over as many SMs as there are blocks.
+__global__ void __launch_bounds__(CHL_WALL_THREADS)
+k_eqwm(ChlMap map, int s_in) {
   chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
@@ -393,6 +403,6 @@ void chl_launch_filter_x(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_
 void chl_launch_filter_z(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<1>, dim3(nb), dim3(256), 0, st, m, 0); }
 void chl_launch_dsm_final(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_dsm_final, dim3(nb), dim3(256), 0, st, m); }
 void chl_launch_coef(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_coef, dim3(m.n), dim3(128), 0, st, m); }
-void chl_launch_eqwm(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_eqwm, dim3(nb), dim3(256), 0, st, m, s_in); }
+void chl_launch_eqwm(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_eqwm, dim3(nb), dim3(CHL_WALL_THREADS), 0, st, m, s_in); }
 void chl_launch_nut(const ChlMap& m, int nb, int s_in, int use_wm, cudaStream_t st) { chl_launch_pdl(k_nut, dim3(nb), dim3(256), 0, st, m, s_in, use_wm); }
 }

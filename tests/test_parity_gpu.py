@@ -194,12 +194,14 @@ def test_calls_out_of_order_report_errors():
     ch.close()
 
 
-def test_non_finite_velocity_is_reported():
+@pytest.mark.parametrize("cfl", [0.5, -1e-3], ids=["cfl", "fixed_dt"])
+def test_non_finite_velocity_is_reported(cfl):
     """A NaN in the uploaded field (made on the host) is found by the next
-    step's CFL pass and reported as CHL_E_NAN at the synchronising calls,
-    until clean fields are uploaded again."""
+    step's CFL pass (with a fixed step, by its non-finite check alone) and
+    reported as CHL_E_NAN at the synchronising calls, until clean fields are
+    uploaded again."""
     from channel_rl_gb300.host import ChlError
-    case = C.smaller(C.c1_small(), 16, 12, 16)
+    case = replace(C.smaller(C.c1_small(), 16, 12, 16), CFL=cfl)
     U, V, W = C.initial_fields(case)
     ch = _channel(case)
     bad = U.copy()
