@@ -255,6 +255,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   size_t o_rdyc = A.take(8 * (Ny + 2)), o_rdyf = A.take(8 * (Ny + 2)), o_dyf = A.take(8 * (Ny + 2));
   size_t o_hx2 = A.take(8 * (Nx + 3)), o_hz2 = A.take(8 * (Nz + 3)), o_hy2 = A.take(8 * (Ny + 2));
   size_t o_w0 = A.take(8 * (Ny + 2)), o_w1 = A.take(8 * (Ny + 2)), o_ygc = A.take(8 * (Ny + 2));
+  size_t o_rdxc4 = A.take(8 * (Nx + 3)), o_rdyc4 = A.take(8 * (Ny + 2)), o_rdzc4 = A.take(8 * (Nz + 3));
   size_t o_csd = A.take(8 * (Ny + 2)), o_dw = A.take(8 * (Ny + 2));
   size_t o_twx = A.take(16 * Nx), o_twz = A.take(16 * Nz);
   size_t o_ti = A.take(8 * ntri), o_tm = A.take(8 * ntri), o_tc = A.take(8 * ntri);
@@ -307,7 +308,8 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.rdxc = P(o_rdxc) + 1; D.rdxf = P(o_rdxf) + 1; D.dxf = P(o_dxf) + 1;
   D.rdzc = P(o_rdzc) + 1; D.rdzf = P(o_rdzf) + 1; D.dzf = P(o_dzf) + 1;
   D.hx2 = P(o_hx2) + 1; D.hz2 = P(o_hz2) + 1; D.hy2 = P(o_hy2);
-  D.rdyc = P(o_rdyc); D.rdyf = P(o_rdyf); D.dyf = P(o_dyf); D.w0 = P(o_w0); D.w1 = P(o_w1); D.ygc = P(o_ygc);
+  D.rdyc = P(o_rdyc); D.rdyf = P(o_rdyf); D.dyf = P(o_dyf); D.w0x2 = P(o_w0); D.w1x2 = P(o_w1); D.ygc = P(o_ygc);
+  D.rdxc4 = P(o_rdxc4) + 1; D.rdyc4 = P(o_rdyc4); D.rdzc4 = P(o_rdzc4) + 1;
   D.smag_csdelta = P(o_csd); D.smag_dwall = P(o_dw);
   D.twx = (const double2*)(base + o_twx); D.twz = (const double2*)(base + o_twz);
   D.tri_inv = P(o_ti); D.tri_m = P(o_tm); D.tri_c = P(o_tc);
@@ -333,7 +335,19 @@ static int upload_consts(chl_handle* h, Inst& I) {
   CK(put(o_hx2, c.hx2)); CK(put(o_hz2, c.hz2)); CK(put(o_hy2, c.hy2));
   const std::vector<double> ygc(c.yg.begin() + 1, c.yg.begin() + 1 + c.nyg);
   CK(put(o_ygc, ygc));
-  CK(put(o_w0, c.w0)); CK(put(o_w1, c.w1)); CK(put(o_csd, c.csdelta)); CK(put(o_dw, c.dwall));
+  // the flux kernel keeps its face fluxes 4 x (chl_rhs.cu): doubled y
+  // weights and quadrupled centre reciprocals, exact power-of-two scalings
+  // (kept in `scaled` for the rest of this function)
+  std::vector<std::vector<double>> scaled;
+  auto times = [&scaled](const std::vector<double>& v, double f) -> const std::vector<double>& {
+    scaled.emplace_back(v);
+    for (auto& x : scaled.back()) x *= f;
+    return scaled.back();
+  };
+  scaled.reserve(5);
+  CK(put(o_w0, times(c.w0, 2.0))); CK(put(o_w1, times(c.w1, 2.0)));
+  CK(put(o_rdxc4, times(c.rdxc, 4.0))); CK(put(o_rdyc4, times(c.rdyc, 4.0))); CK(put(o_rdzc4, times(c.rdzc, 4.0)));
+  CK(put(o_csd, c.csdelta)); CK(put(o_dw, c.dwall));
   const double pi = 4.0 * std::atan(1.0);
   std::vector<double> tw(2 * (size_t)std::max(Nx, Nz));
   for (int m = 0; m < Nx; ++m) { tw[2 * m] = std::cos(2.0 * pi * m / Nx); tw[2 * m + 1] = -std::sin(2.0 * pi * m / Nx); }

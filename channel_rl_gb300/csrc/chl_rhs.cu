@@ -21,6 +21,14 @@
 // writes the nine face fluxes, the second takes their divergence and
 // updates the stage: the FP64 pipe, not HBM, bounds this code, and each
 // flux is computed once instead of twice.
+//
+// The face fluxes are kept 4 x their value: the quarter of the x-z edge
+// averages and of the centre products -(u+u)^2/4 is then never formed, the
+// y weights come doubled (w0x2, w1x2) in place of halved per thread, and the
+// centre reciprocals quadrupled (rdxc4 ...).  The stage update takes the
+// quarter in its RK coefficients.  Scalings by powers of two are exact, so
+// the results are bit-for-bit those of the unscaled form, with 7 fewer FP64
+// instructions per face point.
 #include "chl_common.cuh"
 
 // flux fields: centre-like (rows 1..Ny): 0 GUx, 1 GVy, 2 GWz, 3 GUz, 4 GWx;
@@ -50,26 +58,26 @@ k_flux(ChlMap map, int sin) {
 #define VV(ii, jj, kk) LDG(V + vidx(I, ii, jj, kk))
 #define NT(ii, jj, kk) LDG(nt + cidx(I, ii, jj, kk))
   const double rxf = LDG(I.rdxf + i), rzf = LDG(I.rdzf + k), ryf = LDG(I.rdyf + j);
-  const double hw0 = 0.5 * LDG(I.w0 + j), hw1 = 0.5 * LDG(I.w1 + j);
+  const double qw0 = LDG(I.w0x2 + j), qw1 = LDG(I.w1x2 + j);   // 2 w0, 2 w1
   // row j and j+1 values shared by the xy and yz edges (y-face jv = j)
   const double u_a = UC(i, j, k), u_b = UC(i, j + 1, k);
   const double w_a = WC(i, j, k), w_b = WC(i, j + 1, k);
   const double v_0 = VV(i, j, k);
   const double n_a = NT(i, j, k), n_b = NT(i, j + 1, k);
-  {  // xy edge (x-face i, y-face j, z-centre k): uv, nu -> GUy, GVx
+  {  // xy edge (x-face i, y-face j, z-centre k): uv, nu -> GUy, GVx (all 4 x)
     const double v_p = VV(ip, j, k);
-    const double uy = fma(hw0, u_a, hw1 * u_b);          // 0.5 * u on the y-face
-    const double uv = uy * (v_0 + v_p);                  // u * v (v = 0.5 (v0+vp))
-    const double nxy = fma(hw0, n_a + NT(ip, j, k), hw1 * (n_b + NT(ip, j + 1, k)));
+    const double uy = fma(qw0, u_a, qw1 * u_b);          // 2 u on the y-face
+    const double uv = uy * (v_0 + v_p);                  // 4 u v (v = 0.5 (v0+vp))
+    const double nxy = fma(qw0, n_a + NT(ip, j, k), qw1 * (n_b + NT(ip, j + 1, k)));
     const size_t e = vidx(I, i, j, k);
     G[G_UY][e] = fma(nxy, (u_b - u_a) * ryf, -uv);
     G[G_VX][e] = fma(nxy, (v_p - v_0) * rxf, -uv);
   }
   {  // yz edge (x-centre i, y-face j, z-face k): vw, nu -> GVz, GWy
     const double v_z = VV(i, j, kp);
-    const double wy = fma(hw0, w_a, hw1 * w_b);
+    const double wy = fma(qw0, w_a, qw1 * w_b);
     const double vw = wy * (v_0 + v_z);
-    const double nyz = fma(hw0, n_a + NT(i, j, kp), hw1 * (n_b + NT(i, j + 1, kp)));
+    const double nyz = fma(qw0, n_a + NT(i, j, kp), qw1 * (n_b + NT(i, j + 1, kp)));
     const size_t e = vidx(I, i, j, k);
     G[G_VZ][e] = fma(nyz, (v_z - v_0) * rzf, -vw);
     G[G_WY][e] = fma(nyz, (w_b - w_a) * ryf, -vw);
@@ -77,17 +85,17 @@ k_flux(ChlMap map, int sin) {
   if (j >= 1 && j <= Ny) {
     const int jc = j;
     const size_t c = cidx(I, i, jc, k);
-    {  // cell centre: diagonal fluxes
+    {  // cell centre: diagonal fluxes, 4 x (nu du/dx - ((u+u)/2)^2)
       const double um = UC(im, jc, k), vm = VV(i, jc - 1, k), wm = WC(i, jc, km);
       const double su = um + u_a, sv = vm + v_0, sw = wm + w_a;
-      G[G_UX][c] = fma(-0.25 * su, su, n_a * LDG(I.rdxc + i) * (u_a - um));
-      G[G_VY][c] = fma(-0.25 * sv, sv, n_a * LDG(I.rdyc + jc) * (v_0 - vm));
-      G[G_WZ][c] = fma(-0.25 * sw, sw, n_a * LDG(I.rdzc + k) * (w_a - wm));
+      G[G_UX][c] = fma(-su, su, n_a * LDG(I.rdxc4 + i) * (u_a - um));
+      G[G_VY][c] = fma(-sv, sv, n_a * LDG(I.rdyc4 + jc) * (v_0 - vm));
+      G[G_WZ][c] = fma(-sw, sw, n_a * LDG(I.rdzc4 + k) * (w_a - wm));
     }
-    {  // xz edge (x-face i, y-centre jc, z-face k): uw, nu -> GUz, GWx
+    {  // xz edge (x-face i, y-centre jc, z-face k): uw, nu -> GUz, GWx (all 4 x)
       const double u_z = UC(i, jc, kp), w_p = WC(ip, jc, k);
-      const double uw = 0.25 * (u_a + u_z) * (w_a + w_p);
-      const double nxz = 0.25 * ((n_a + NT(ip, jc, k)) + (NT(i, jc, kp) + NT(ip, jc, kp)));
+      const double uw = (u_a + u_z) * (w_a + w_p);
+      const double nxz = (n_a + NT(ip, jc, k)) + (NT(i, jc, kp) + NT(ip, jc, kp));
       G[G_UZ][c] = fma(nxz, (u_z - u_a) * rzf, -uw);
       G[G_WX][c] = fma(nxz, (w_p - w_a) * rxf, -uw);
     }
@@ -101,7 +109,7 @@ k_flux(ChlMap map, int sin) {
 
 struct RhsArgs {
   int sbase, sout;        // velocity sets: stage base (U^n), output
-  double c1, c2;          // out = base + dt*(c1*F1 + c2*F)
+  double c1, c2;          // out = base + dt*(c1*F1 + c2*F), both passed / 4 (F1, F are 4 x)
   int mode;               // 0: stage 1 (store F1), 1: stages 2/3, 2: actual-pressure RHS only
 };
 
@@ -128,7 +136,7 @@ k_rhs_update(ChlMap map, RhsArgs a) {
   double Fu = (LDG(G[G_UX] + cidx(I, ip, jc, k)) - LDG(G[G_UX] + c)) * rxf;
   Fu = fma(LDG(G[G_UY] + e) - LDG(G[G_UY] + em), ryc, Fu);
   Fu = fma(LDG(G[G_UZ] + c) - LDG(G[G_UZ] + cidx(I, i, jc, km)), rzc, Fu);
-  Fu += I.scal[CHL_S_DPDX];
+  Fu += 4.0 * I.scal[CHL_S_DPDX];   // the fluxes, so F, are 4 x
   // w at (x-centre i, row jc, z-face k)
   double Fw = (LDG(G[G_WX] + c) - LDG(G[G_WX] + cidx(I, im, jc, k))) * rxc;
   Fw = fma(LDG(G[G_WY] + e) - LDG(G[G_WY] + em), ryc, Fw);
@@ -141,9 +149,9 @@ k_rhs_update(ChlMap map, RhsArgs a) {
     Fv = fma(LDG(G[G_VY] + cidx(I, i, jc + 1, k)) - LDG(G[G_VY] + c), LDG(I.rdyf + jc), Fv);
     Fv = fma(LDG(G[G_VZ] + e) - LDG(G[G_VZ] + vidx(I, i, jc, km)), rzc, Fv);
   }
-  if (a.mode == 2) {           // actual-pressure RHS: keep F only
-    I.Fp[0][c] = Fu; I.Fp[2][c] = Fw;
-    if (hasv) I.Fp[1][e] = Fv;
+  if (a.mode == 2) {           // actual-pressure RHS: keep F only, at its own scale
+    I.Fp[0][c] = 0.25 * Fu; I.Fp[2][c] = 0.25 * Fw;
+    if (hasv) I.Fp[1][e] = 0.25 * Fv;
     return;
   }
   const double dt = I.scal[CHL_S_DT];
@@ -173,7 +181,7 @@ void chl_launch_flux(const ChlMap& map, int nb_edge, int sin, cudaStream_t st) {
 }
 void chl_launch_update(const ChlMap& map, int nb_pt, int sbase, int sout, double c1, double c2, int mode,
                        cudaStream_t st) {
-  RhsArgs a{sbase, sout, c1, c2, mode};
+  RhsArgs a{sbase, sout, 0.25 * c1, 0.25 * c2, mode};
   chl_launch_pdl(k_rhs_update, dim3(nb_pt), dim3(256), 0, st, map, a);
 }
 }

@@ -353,26 +353,43 @@ k_eqwm(ChlMap map, int s_in) {
 }
 
 // ------------------------------------------------------------ nu_t (+ wall model rows)
+// wall-model eddy viscosity at the x face a of a wall: tau / (dU/dy) - nu
+// with dU/dy = (U(wall row) - U(ghost row)) / dyw (one division)
 __device__ __forceinline__ double wm_face(const ChlInst& I, const double* U, int a, int k, int wall) {
   const double al = I.alpha[(size_t)wall * I.Nx * I.Nz + (size_t)k * I.Nx + a];
   const double du = wall == 0 ? U[cidx(I, a, 1, k)] - U[cidx(I, a, 0, k)]
                               : U[cidx(I, a, I.Ny, k)] - U[cidx(I, a, I.Ny + 1, k)];
-  return al / (du / I.dyw) - I.nu;
+  return al * I.dyw / du - I.nu;
 }
 
+// One thread per centre (i, jc, k), jc = 0..Ny+1.  On the wall-model rows
+// (jc = 0, 1 and Ny, Ny+1) nu_t is the mean of the face values at x faces
+// i-1 and i: each thread forms face i and takes face i-1 from the lane to
+// its left when that lane is on the same row (i > 0), so no thread returns
+// before the shuffle.
 __global__ void __launch_bounds__(256)
 k_nut(ChlMap map, int s_in, int use_wm) {
   chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
-  if (t >= (long)Nx * (Ny + 2) * Nz) return;
-  const int i = (int)(t % Nx);
-  const int jc = (int)((t / Nx) % (Ny + 2));
-  const int k = (int)(t / ((long)Nx * (Ny + 2)));
+  const long t = (long)lb * blockDim.x + threadIdx.x;
+  const bool valid = t < (long)Nx * (Ny + 2) * Nz;
+  const long tv = valid ? t : 0;
+  const int i = (int)(tv % Nx);
+  const int jc = (int)((tv / Nx) % (Ny + 2));
+  const int k = (int)(tv / ((long)Nx * (Ny + 2)));
+  const bool wmrow = valid && use_wm && I.wall_model != 0 && (jc <= 1 || jc >= Ny);
+  const int wall = jc <= 1 ? 0 : 1;
+  const double* U = I.U[s_in];
+  const double f = wmrow ? wm_face(I, U, i, k, wall) : 0.0;
+  const double f_left = __shfl_up_sync(0xffffffffu, f, 1);
+  if (!valid) return;
   double v = 0.0;
-  if (I.LES_model != 0) {
+  if (wmrow) {
+    const double fl = ((threadIdx.x & 31) > 0 && i > 0) ? f_left : wm_face(I, U, wrap(i - 1, Nx), k, wall);
+    v = 0.5 * (fl + f);
+  } else if (I.LES_model != 0) {
     const bool ghost = jc == 0 || jc == Ny + 1;
     const int js = jc == 0 ? 1 : (jc == Ny + 1 ? Ny : jc);
     v = fmax(I.coef[js] * I.S[cidx(I, i, js, k)], 0.0);
@@ -384,11 +401,6 @@ k_nut(ChlMap map, int s_in, int use_wm) {
         v = -v + 2.0 * 0.38 * sqrt(I.scal[CHL_S_DPDX]) * I.dy1 / 2.0;
       }
     }
-  }
-  if (use_wm && I.wall_model != 0 && (jc <= 1 || jc >= Ny)) {
-    const int wall = jc <= 1 ? 0 : 1;
-    const double* U = I.U[s_in];
-    v = 0.5 * (wm_face(I, U, wrap(i - 1, Nx), k, wall) + wm_face(I, U, i, k, wall));
   }
   // stored as nu + nu_t: every consumer adds nu (equations.f90:139-155)
   I.nut[cidx(I, i, jc, k)] = I.nu + v;

@@ -19,7 +19,7 @@ k_stats_rows(ChlMap map, int s, double* out, int pitch) {
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
   const int r = lb;
   const double *U = I.U[s], *V = I.V[s], *W = I.W[s];
-  const double w0 = I.w0[r], w1 = I.w1[r];
+  const double w0 = 0.5 * I.w0x2[r], w1 = 0.5 * I.w1x2[r];   // exact halvings
   double acc[NST] = {0, 0, 0, 0, 0, 0, 0};
   for (int w = threadIdx.x; w < Nx * Nz; w += blockDim.x) {
     const int i = w % Nx, k = w / Nx;
@@ -62,7 +62,7 @@ k_stats_wall(ChlMap map, int s, double* out, int pitch) {
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
   const double *U = I.U[s], *V = I.V[s], *nt = I.nut;
   double tau = 0.0, qx = 0.0, nx_ = 0.0, qy = 0.0, ny_ = 0.0;
-  const double w0 = I.w0[0], w1 = I.w1[0];
+  const double w0 = 0.5 * I.w0x2[0], w1 = 0.5 * I.w1x2[0];
   for (long w = threadIdx.x; w < (long)Nx * Nz; w += blockDim.x) {
     const int i = (int)(w % Nx), k = (int)(w / Nx), ip = wrap(i + 1, Nx);
     const double ntf0 = 0.5 * (nt[cidx(I, i, 0, k)] + nt[cidx(I, ip, 0, k)]);
