@@ -363,10 +363,7 @@ def run_ours(args):
             "profiled_step_ms": tot_prof}
     if args.workload in ("c3_dsm", "c3_smag") and not args.no_batched:
         line["batched_mlp"] = batched_mlp_rate(args)
-    if rank == 0 and args.gpus == 1 and not args.no_cpu_baseline and cases_[0].LES_model > C.LES_DSM:
-        line["cpu_baseline"] = {"value": None, "unit": UNIT,
-                                "note": "the host restatement covers the none/static/dynamic SGS models only"}
-    elif rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
+    if rank == 0 and args.gpus == 1 and not args.no_cpu_baseline:
         rate, nsteps, secs, cores = host_step_rate(cases_, args.cpu_budget, 50)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": host_sample_text(nsteps, cases_, args, secs, cores),

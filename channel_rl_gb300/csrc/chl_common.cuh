@@ -18,7 +18,7 @@
 #include <stdint.h>
 
 #define CHL_NQ 18   // filtered DSM components
-#define CHL_WALL_THREADS 64   // block width of the equilibrium wall-stress solve
+#define CHL_WALL_THREADS 32   // block width of the equilibrium wall-stress solve (one warp)
 // SMs of a GB300.  The small transforms are cut finer until their grid
 // covers the SMs about four times: with about one block per SM a few SMs
 // run two, and the launch takes twice one block's time.

@@ -465,7 +465,10 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
   } else if (h->LES_model == CHL_LES_VREMAN) {
     KL("vreman", chl_launch_vreman(h->map(M_PT), h->nblk[M_PT], s, st));
   }
-  KL("nut_coef", chl_launch_coef(h->map(M_PT), st));
+  // the row coefficient exists for the Smagorinsky models only (k_nut
+  // takes AMD's and Vreman's S as nu_t, and no model leaves nu_t = 0)
+  if (h->LES_model == CHL_LES_DYNAMIC || h->LES_model == CHL_LES_SMAGORINSKY)
+    KL("nut_coef", chl_launch_coef(h->map(M_PT), st));
   if (with_wm && (h->wall_model == CHL_WM_EQLOG || h->wall_model == CHL_WM_MLP))
     KL("eq_wallmodel", chl_launch_eqwm(h->map(M_WALLN), h->nblk[M_WALLN], s, st));
   if (with_wm && h->wall_model == CHL_WM_MLP)

@@ -99,31 +99,22 @@ k_minabs(ChlMap map, int s) {
   for (int i = threadIdx.x; i < nxr; i += blockDim.x) {
     const bool ok = i < Nx;
     unsigned long long mu = CHL_BIG_BITS;
-    // all rows of the chunk are loaded before any reduction, so the loads
-    // are in flight together (the shared atomics would otherwise order them)
-    unsigned long long bv[MINABS_ROWS];
-#pragma unroll
-    for (int r = 0; r < MINABS_ROWS; ++r) {
-      const int jc = j0 + r;
-      bv[r] = CHL_BIG_BITS;
-      if (ok && jc <= j1) {
+    for (int jc = j0; jc <= j1; ++jc) {
+      unsigned long long bv = CHL_BIG_BITS;
+      if (ok) {
         const unsigned long long bu = absbits(U[cidx(I, i, jc, k)]);
         const unsigned long long bw = absbits(W[cidx(I, i, jc, k)]);
-        bv[r] = absbits(V[vidx(I, i, jc, k)]);
+        bv = absbits(V[vidx(I, i, jc, k)]);
         mu = bu < mu ? bu : mu;
         mw = bw < mw ? bw : mw;
-        bad |= (bu >= CHL_BIG_BITS) | (bw >= CHL_BIG_BITS) | (bv[r] >= CHL_BIG_BITS);
+        bad |= (bu >= CHL_BIG_BITS) | (bw >= CHL_BIG_BITS) | (bv >= CHL_BIG_BITS);
       }
-    }
-#pragma unroll
-    for (int r = 0; r < MINABS_ROWS; ++r) {
-      unsigned long long b = bv[r];
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long x = __shfl_xor_sync(0xffffffffu, b, o);
-        b = x < b ? x : b;
+        const unsigned long long x = __shfl_xor_sync(0xffffffffu, bv, o);
+        bv = x < bv ? x : bv;
       }
-      if (lane == 0 && j0 + r <= j1) atomicMin(sv + r, b);
+      if (lane == 0) atomicMin(sv + (jc - j0), bv);
     }
     if (ok) atomicMin(g + i, mu);
   }

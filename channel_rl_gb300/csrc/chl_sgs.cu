@@ -287,7 +287,7 @@ __global__ void k_coef(ChlMap map) {
         const double cd = I.smag_csdelta[jc] * f;   // Cs*Delta_j*f
         c = cd * cd;
       } else if (I.LES_model >= 3) {
-        c = 1.0;                           // AMD, Vreman: S holds nu_t itself
+        c = 1.0;                           // AMD, Vreman: S holds nu_t itself (not launched for them)
       }
     }
     I.coef[jc] = c;
@@ -392,7 +392,9 @@ k_nut(ChlMap map, int s_in, int use_wm) {
   } else if (I.LES_model != 0) {
     const bool ghost = jc == 0 || jc == Ny + 1;
     const int js = jc == 0 ? 1 : (jc == Ny + 1 ? Ny : jc);
-    v = fmax(I.coef[js] * I.S[cidx(I, i, js, k)], 0.0);
+    // AMD and Vreman store nu_t itself in S (row coefficient 1)
+    const double sv = I.S[cidx(I, i, js, k)];
+    v = fmax(I.LES_model >= 3 ? sv : I.coef[js] * sv, 0.0);
     if (ghost) {
       if (I.Dirichlet_nu_t == 1) {
         v = -v;

@@ -9,6 +9,7 @@
 //   compute_time_step_RK3          time_integration.f90:24-96
 //   sgs_dynamic_Smagorinsky        subgrid.f90:379-537 (filter_xzy :140-190, compute_Sij :1014-1072)
 //   sgs_Smagorinsky                subgrid.f90:563-612 (from its formula, Cs from the caller)
+//   AMD, Vreman                    subgrid.f90:632-874, 897-1004 (ghost rows :858-871, 991-1002)
 //   compute_wall_model             wallmodel.f90:23-46 (+ the equilibrium log law of the build)
 //   compute_rhs_u/v/w              equations.f90:24-468
 //   apply_boundary_conditions      boundary_conditions.f90:20-254 (P>=2 semantics)
@@ -333,6 +334,153 @@ struct Ref {
     finish_nut();
   }
 
+  // Grid-scaled differences of one velocity component interpolated to a
+  // centre the way the reference's interpolate_* pairs do it: a0/b0 at the
+  // near and a1/b1 at the far face in the derivative direction (a, b the two
+  // faces in the other direction), h0/h1 the derivative spacings there.
+  // Returns the centre derivative (d), the centre difference (d^) and the
+  // two face averages of the difference (s1[0], s1[1]).
+  struct Cavg { double der, dif, s1[2]; };
+  static Cavg cavg(double a0, double b0, double a1, double b1, double h0, double h1) {
+    Cavg c;
+    const double t20 = 0.5 * (a0 / h0 + b0 / h0), t21 = 0.5 * (a1 / h1 + b1 / h1);
+    c.der = 0.5 * (t20 + t21);
+    c.s1[0] = 0.5 * (a0 + b0); c.s1[1] = 0.5 * (a1 + b1);
+    c.dif = 0.5 * (c.s1[0] + c.s1[1]);
+    return c;
+  }
+
+  // sgs_AMD (subgrid.f90:632-874): nu_t = max(0, -C N / D), C = 0.3, with
+  // N = sum (d^_k u_i)(d^_k u_j) S_ij and D = sum (d_k u_l)^2, the terms in
+  // the reference's order (U, V, W blocks, then the S12, S13, S23 cross
+  // terms), one fused pass over the interior centres.
+  void amd() {
+    sij(U, V, W, sc_Sr, sc_S);
+    const A3* S6 = sc_Sr;
+    std::fill(nut.v.begin(), nut.v.end(), 0.0);
+    const double Cp = 0.3;
+#pragma omp parallel for
+    for (int k = 2; k <= nzg - 1; ++k)
+      for (int j = 2; j <= nyg - 1; ++j)
+        for (int i = 2; i <= nxg - 1; ++i) {
+          const double S11 = S6[0](i, j, k), S22 = S6[1](i, j, k), S33 = S6[2](i, j, k);
+          const double S12 = S6[3](i, j, k), S13 = S6[4](i, j, k), S23 = S6[5](i, j, k);
+          const double dy0 = yg[j] - yg[j - 1], dy1 = yg[j + 1] - yg[j];
+          const double dz0 = zg[k] - zg[k - 1], dz1 = zg[k + 1] - zg[k];
+          const double dx0 = xg[i] - xg[i - 1], dx1 = xg[i + 1] - xg[i];
+          // U: x, y (faces j, j+1; x faces i-1, i), z
+          const double dUx = U(i, j, k) - U(i - 1, j, k);
+          const double hx = x[i] - x[i - 1];
+          double t4 = dUx * dUx / (hx * hx);
+          double nv = dUx * dUx * S11;
+          const Cavg Uy = cavg(U(i - 1, j, k) - U(i - 1, j - 1, k), U(i, j, k) - U(i, j - 1, k),
+                               U(i - 1, j + 1, k) - U(i - 1, j, k), U(i, j + 1, k) - U(i, j, k), dy0, dy1);
+          t4 = t4 + Uy.der * Uy.der; nv = nv + Uy.dif * Uy.dif * S11;
+          const Cavg Uz = cavg(U(i - 1, j, k) - U(i - 1, j, k - 1), U(i, j, k) - U(i, j, k - 1),
+                               U(i - 1, j, k + 1) - U(i - 1, j, k), U(i, j, k + 1) - U(i, j, k), dz0, dz1);
+          t4 = t4 + Uz.der * Uz.der; nv = nv + Uz.dif * Uz.dif * S11;
+          // V: y, x (faces i, i+1; y faces j-1, j), z
+          const double dVy = V(i, j, k) - V(i, j - 1, k);
+          const double hy = y[j] - y[j - 1];
+          t4 = t4 + dVy * dVy / (hy * hy);
+          nv = nv + dVy * dVy * S22;
+          const Cavg Vx = cavg(V(i, j - 1, k) - V(i - 1, j - 1, k), V(i, j, k) - V(i - 1, j, k),
+                               V(i + 1, j - 1, k) - V(i, j - 1, k), V(i + 1, j, k) - V(i, j, k), dx0, dx1);
+          t4 = t4 + Vx.der * Vx.der; nv = nv + Vx.dif * Vx.dif * S22;
+          const Cavg Vz = cavg(V(i, j - 1, k) - V(i, j - 1, k - 1), V(i, j, k) - V(i, j, k - 1),
+                               V(i, j - 1, k + 1) - V(i, j - 1, k), V(i, j, k + 1) - V(i, j, k), dz0, dz1);
+          t4 = t4 + Vz.der * Vz.der; nv = nv + Vz.dif * Vz.dif * S22;
+          // W: z, x (faces i, i+1; z faces k-1, k), y (faces j, j+1; z faces k-1, k)
+          const double dWz = W(i, j, k) - W(i, j, k - 1);
+          const double hz = z[k] - z[k - 1];
+          const double dWz2 = dWz * dWz;
+          t4 = t4 + dWz2 / (hz * hz);
+          nv = nv + dWz2 * S33;
+          const Cavg Wx = cavg(W(i, j, k - 1) - W(i - 1, j, k - 1), W(i, j, k) - W(i - 1, j, k),
+                               W(i + 1, j, k - 1) - W(i, j, k - 1), W(i + 1, j, k) - W(i, j, k), dx0, dx1);
+          t4 = t4 + Wx.der * Wx.der; nv = nv + Wx.dif * Wx.dif * S33;
+          const Cavg Wy = cavg(W(i, j, k - 1) - W(i, j - 1, k - 1), W(i, j, k) - W(i, j - 1, k),
+                               W(i, j + 1, k - 1) - W(i, j, k - 1), W(i, j + 1, k) - W(i, j, k), dy0, dy1);
+          t4 = t4 + Wy.der * Wy.der; nv = nv + Wy.dif * Wy.dif * S33;
+          // cross terms 2 (d^_k u_i)(d^_k u_j) S_ij, i != j (subgrid.f90:751-851)
+          nv = nv + 2.0 * (Vx.dif * dUx) * S12;
+          nv = nv + 2.0 * (Uy.dif * dVy) * S12;
+          nv = nv + 2.0 * (0.5 * (Uz.s1[0] * Vz.s1[0] + Uz.s1[1] * Vz.s1[1])) * S12;
+          nv = nv + 2.0 * (Wx.dif * dUx) * S13;
+          nv = nv + 2.0 * (Uz.dif * dWz) * S13;
+          nv = nv + 2.0 * (0.5 * (Uy.s1[0] * Wy.s1[0] + Uy.s1[1] * Wy.s1[1])) * S13;
+          nv = nv + 2.0 * (Wy.dif * dVy) * S23;
+          nv = nv + 2.0 * (Vz.dif * dWz) * S23;
+          nv = nv + 2.0 * (0.5 * (Vx.s1[0] * Wx.s1[0] + Vx.s1[1] * Wx.s1[1])) * S23;
+          nut(i, j, k) = -Cp * nv / t4;
+        }
+    finish_nut_amd_vreman(true);
+  }
+
+  // sgs_Vreman (subgrid.f90:897-1004): nu_t = C sqrt(B_b / a_ij a_ij),
+  // C = 2.5 (0.1)^2, b_ij = sum_m dx_m^2 a_mi a_mj, a_ij = du_j/dx_i at the
+  // centre (reference layout 1 4 5 / 7 2 6 / 8 9 3; off-diagonals the mean of
+  // the four surrounding edge derivatives).  Not clipped, as written.
+  void vreman() {
+    std::fill(nut.v.begin(), nut.v.end(), 0.0);
+    const double C = 2.5 * std::pow(0.1, 2.0);
+#pragma omp parallel for
+    for (int k = 2; k <= nzg - 1; ++k)
+      for (int j = 2; j <= nyg - 1; ++j)
+        for (int i = 2; i <= nxg - 1; ++i) {
+          const double dxl = xg[i] - xg[i - 1], dxr = xg[i + 1] - xg[i];
+          const double dyl = yg[j] - yg[j - 1], dyr = yg[j + 1] - yg[j];
+          const double dzl = zg[k] - zg[k - 1], dzr = zg[k + 1] - zg[k];
+          double a[10];
+          a[1] = (U(i, j, k) - U(i - 1, j, k)) / (x[i] - x[i - 1]);
+          a[4] = 0.25 * (V(i, j, k) - V(i - 1, j, k)) / dxl + 0.25 * (V(i, j - 1, k) - V(i - 1, j - 1, k)) / dxl
+               + 0.25 * (V(i + 1, j, k) - V(i, j, k)) / dxr + 0.25 * (V(i + 1, j - 1, k) - V(i, j - 1, k)) / dxr;
+          a[5] = 0.25 * (W(i, j, k) - W(i - 1, j, k)) / dxl + 0.25 * (W(i, j, k - 1) - W(i - 1, j, k - 1)) / dxl
+               + 0.25 * (W(i + 1, j, k) - W(i, j, k)) / dxr + 0.25 * (W(i + 1, j, k - 1) - W(i, j, k - 1)) / dxr;
+          a[2] = (V(i, j, k) - V(i, j - 1, k)) / (y[j] - y[j - 1]);
+          a[7] = 0.25 * (U(i, j, k) - U(i, j - 1, k)) / dyl + 0.25 * (U(i - 1, j, k) - U(i - 1, j - 1, k)) / dyl
+               + 0.25 * (U(i, j + 1, k) - U(i, j, k)) / dyr + 0.25 * (U(i - 1, j + 1, k) - U(i - 1, j, k)) / dyr;
+          a[6] = 0.25 * (W(i, j, k) - W(i, j - 1, k)) / dyl + 0.25 * (W(i, j, k - 1) - W(i, j - 1, k - 1)) / dyl
+               + 0.25 * (W(i, j + 1, k) - W(i, j, k)) / dyr + 0.25 * (W(i, j + 1, k - 1) - W(i, j, k - 1)) / dyr;
+          a[3] = (W(i, j, k) - W(i, j, k - 1)) / (z[k] - z[k - 1]);
+          a[8] = 0.25 * (U(i, j, k) - U(i, j, k - 1)) / dzl + 0.25 * (U(i - 1, j, k) - U(i - 1, j, k - 1)) / dzl
+               + 0.25 * (U(i, j, k + 1) - U(i, j, k)) / dzr + 0.25 * (U(i - 1, j, k + 1) - U(i - 1, j, k)) / dzr;
+          a[9] = 0.25 * (V(i, j, k) - V(i, j, k - 1)) / dzl + 0.25 * (V(i, j - 1, k) - V(i, j - 1, k - 1)) / dzl
+               + 0.25 * (V(i, j, k + 1) - V(i, j, k)) / dzr + 0.25 * (V(i, j - 1, k + 1) - V(i, j - 1, k)) / dzr;
+          const double ddx = (x[i] - x[i - 1]) * (x[i] - x[i - 1]);
+          const double ddy = (y[j] - y[j - 1]) * (y[j] - y[j - 1]);
+          const double ddz = (z[k] - z[k - 1]) * (z[k] - z[k - 1]);
+          // b_ij, (11, 22, 33, 12, 13, 23) = 1..6
+          static const int px[7][2] = {{0, 0}, {1, 1}, {4, 4}, {5, 5}, {1, 4}, {1, 5}, {4, 5}};
+          static const int py[7][2] = {{0, 0}, {7, 7}, {2, 2}, {6, 6}, {7, 2}, {7, 6}, {2, 6}};
+          static const int pz[7][2] = {{0, 0}, {8, 8}, {9, 9}, {3, 3}, {8, 9}, {8, 3}, {9, 3}};
+          double b[7];
+          for (int m = 1; m <= 6; ++m) {
+            b[m] = 0.0 + ddx * a[px[m][0]] * a[px[m][1]];
+            b[m] = b[m] + ddy * a[py[m][0]] * a[py[m][1]];
+            b[m] = b[m] + ddz * a[pz[m][0]] * a[pz[m][1]];
+          }
+          const double Bb = b[1] * b[2] - b[4] * b[4] + b[1] * b[3] - b[5] * b[5] + b[2] * b[3] - b[6] * b[6];
+          double Ab = a[1] * a[1];
+          for (int m = 2; m <= 9; ++m) Ab = Ab + a[m] * a[m];
+          nut(i, j, k) = C * std::pow(Bb / Ab, 0.5);
+        }
+    finish_nut_amd_vreman(false);
+  }
+
+  // ghost rows of the AMD and Vreman models (subgrid.f90:858-871, 991-1002)
+  void finish_nut_amd_vreman(bool clip) {
+    per_x(nut, 2); per_z(nut, 4);
+    if (clip) for (auto& v : nut.v) v = std::max(v, 0.0);
+    if (Dirichlet_nu_t == 1) dir_y(nut, 2);
+    else if (Dirichlet_nu_t == 0) {
+      for (int k = 1; k <= nzg; ++k) for (int i = 1; i <= nxg; ++i) { nut(i, 1, k) = nut(i, 2, k); nut(i, nyg, k) = nut(i, nyg - 1, k); }
+    } else {
+      const double c = 2.0 * 0.38 * std::pow(dPdx, 0.5) * (y[2] - y[1]) / 2.0;
+      for (int k = 1; k <= nzg; ++k) for (int i = 1; i <= nxg; ++i) { nut(i, 1, k) = -nut(i, 2, k) + c; nut(i, nyg, k) = -nut(i, nyg - 1, k) + c; }
+    }
+  }
+
   void finish_nut() {
     per_x(nut, 2); per_z(nut, 4);
     for (auto& v : nut.v) v = std::max(v, 0.0);
@@ -528,6 +676,8 @@ struct Ref {
     for (int s = 0; s < 3; ++s) {
       if (LES_model == 2) dsm();
       else if (LES_model == 1) smag();
+      else if (LES_model == 3) amd();
+      else if (LES_model == 4) vreman();
       else std::fill(nut.v.begin(), nut.v.end(), 0.0);
       if (wall_model != 0) compute_wall_model();
       rhs_u(F[s][0]); rhs_v(F[s][1]); rhs_w(F[s][2]);

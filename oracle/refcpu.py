@@ -56,8 +56,8 @@ class RefCPU:
         wm = case.wall_model
         if wm not in (C.WM_NONE, C.WM_STRESS, C.WM_EQLOG):
             raise ValueError("RefCPU covers the no/stress/equilibrium wall models only")
-        if case.LES_model not in (C.LES_NONE, C.LES_SMAG, C.LES_DSM):
-            raise ValueError("RefCPU covers the none/static/dynamic Smagorinsky models only")
+        if case.LES_model not in (C.LES_NONE, C.LES_SMAG, C.LES_DSM, C.LES_AMD, C.LES_VREMAN):
+            raise ValueError("unsupported LES model")
         self.h = lib.refcpu_create(case.nx, case.ny, case.nz, _p(x), _p(y), _p(z), case.nu, case.CFL,
                                    case.dPdx, case.x_mass_cte, case.LES_model, case.Dirichlet_nu_t,
                                    wm, case.Cs)

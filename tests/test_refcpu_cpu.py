@@ -1,5 +1,7 @@
 """The multi-core C++ restatement (oracle/refcpu.cpp, the host-core baseline)
 against the NumPy oracle: same step, same inputs, every physics switch."""
+from dataclasses import replace
+
 import numpy as np
 import pytest
 
@@ -15,6 +17,11 @@ CASES = {
     "dsm_eqwm": lambda: C.smaller(C.c3_roofline(C.LES_DSM), 16, 12, 24),
     "smag_eqwm": lambda: C.smaller(C.c3_roofline(C.LES_SMAG), 24, 16, 16),
     "dsm_eqwm_massflow_ragged": lambda: C.smaller(C.c2_wm64(), 18, 10, 12),
+    # the reference's RL cases: AMD, ghost rule 2, fixed dt (as rl_case)
+    "amd_eqwm_rule2_fixed_dt": lambda: replace(C.smaller(C.rl_case(), 16, 10, 12), Dirichlet_nu_t=2),
+    "amd_rule1_massflow": lambda: replace(C.smaller(C.c1_small(), 18, 12, 12), LES_model=C.LES_AMD),
+    "vreman_eqwm_rule0": lambda: replace(C.smaller(C.c3_roofline(C.LES_DSM), 12, 14, 18),
+                                         LES_model=C.LES_VREMAN, Dirichlet_nu_t=0),
 }
 
 
@@ -39,8 +46,6 @@ def test_refcpu_matches_oracle(name):
 
 
 def test_refcpu_rejects_learned_wall_model():
-    from dataclasses import replace
-
     from oracle.refcpu import RefCPU
     case = replace(C.smaller(C.c1_small(), 16, 12, 16), wall_model=C.WM_MLP)
     with pytest.raises(ValueError):
