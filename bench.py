@@ -299,6 +299,13 @@ def run_ours(args):
         ch.upload(*C.initial_fields(case), inst=q)
     if cases_[0].wall_model == C.WM_MLP:
         ch.mlp_set_params(mlp_params()[0])
+    # tile shapes picked by the library's tuner, or given (results are
+    # bit-identical for every candidate; untimed)
+    if args.tile_shapes:
+        ch.set_tile_shapes(*(int(v) for v in args.tile_shapes.split(",")))
+        tune_report = f"given: {args.tile_shapes}"
+    else:
+        tune_report = None if args.no_autotune else ch.autotune()
     points = sum(c.points for c in cases_)
     # warm-up (builds the graph on the first call)
     ch.step(max(args.warmup, 1))
@@ -358,6 +365,7 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config_of(args, cases_), "e2e": e2e, "roofline": roof,
             "gpu_launches": nker * args.steps, "clocks": clk.summary(),
+            "tile_shapes": dict(ch.tile_shapes(), tuner=tune_report or "off (defaults)"),
             "host_wall_s": wall,
             "kernels_ms_per_step": {k: round(v[0], 4) for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])},
             "profiled_step_ms": tot_prof}
@@ -390,6 +398,8 @@ def timed_rate(cases_, args, steps, setup=None):
         ch.upload(*C.initial_fields(c), inst=q)
     if setup:
         setup(ch)
+    if not args.no_autotune:
+        ch.autotune()
     ch.step(max(args.warmup, 3))
     ch.synchronize()
     ms = ch.time_steps(steps)
@@ -474,6 +484,10 @@ def main():
     ap.add_argument("--workload", default="c3_dsm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default tile shapes")
+    ap.add_argument("--tile-shapes", default="",
+                    help="x_min_blocks,z_min_blocks,tri_mode,point_threads instead of tuning (e.g. to profile the "
+                         "tuned shapes without the tuner's own launches)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched learned-wall-model line")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--prof-reps", type=int, default=3)

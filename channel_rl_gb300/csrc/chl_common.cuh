@@ -23,12 +23,27 @@
 // covers the SMs about four times: with about one block per SM a few SMs
 // run two, and the launch takes twice one block's time.
 #define CHL_SMS 152
-#define CHL_FFT_MIN_BLOCKS (4 * CHL_SMS)
-// complex rows (pairs of real x lines) per x-transform block
-__host__ __device__ inline int chl_fftx_rows(int Nx, int nrow) {
+#define CHL_MIN_BLOCKS (4 * CHL_SMS)
+#define CHL_FFT_MIN_BLOCKS CHL_MIN_BLOCKS
+// x-z points per thread of the DSM plane sums (k_dsm_final): 4, halved
+// while the instance's Ny x chunks grid would have fewer blocks than SMs.
+// (Each block ends in a shared-memory reduction tree, so cutting finer than
+// one block per SM costs more than it spreads; in a batch the other
+// instances fill the GPU anyway.)  A function of the instance's own extents
+// only, so an instance sums its planes in the same order alone and in a
+// batch.
+__host__ __device__ inline int chl_dsm_ppt(int Nx, int Ny, int Nz) {
+  int ppt = 4;
+  while (ppt > 1 && (long)Ny * ((Nx * Nz + 256 * ppt - 1) / (256 * ppt)) < CHL_SMS) ppt >>= 1;
+  return ppt;
+}
+// complex rows (pairs of real x lines) per x-transform block: up to
+// 1024/Nx, halved while the instance's grid would have fewer than
+// min_blocks blocks (CHL_FFT_MIN_BLOCKS unless the tuner chose another)
+__host__ __device__ inline int chl_fftx_rows(int Nx, int nrow, int min_blocks) {
   int cr = 1024 / Nx;
   if (cr < 1) cr = 1;
-  while (cr > 1 && (nrow + cr - 1) / cr < CHL_FFT_MIN_BLOCKS) cr >>= 1;
+  while (cr > 1 && (nrow + cr - 1) / cr < min_blocks) cr >>= 1;
   return cr;
 }
 // threads of a transform block staging `lines` lines of length n: one
@@ -80,7 +95,7 @@ struct ChlInst {
   double *alpha;                  // wall stress [2][Nz][Nx]
   double *bc;                     // pressure BC planes [2][Nz][Nx]
   double *part;                   // DSM plane partial sums [2][Ny+2][npart]
-  int npart;
+  int npart, dsm_ppt;             // chunks per plane, points per thread (chl_dsm_ppt)
   double *coef;                   // nu_t coefficient per centre row [Ny+2]
   double *scal;                   // device scalars (CHL_S_*)
   unsigned long long *minabs;     // [Nx+1 | Nz] min |u| bit patterns (dt)
@@ -104,6 +119,7 @@ struct ChlMap {
   const ChlInst* inst;   // device array of instances
   const int* off;        // prefix sum of blocks per instance, off[n] = total
   int n;
+  int tb;                // threads per block of the one-thread-per-point maps (tuned)
 };
 
 __device__ __forceinline__ int chl_find(const ChlMap& m, int b, int& local) {

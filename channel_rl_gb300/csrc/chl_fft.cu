@@ -103,14 +103,14 @@ __device__ double2* fft_smem(double2* a, double2* b, int nrows, int rs, int es, 
 // mode 1: div of the actual-pressure RHS Fp with the wall rows of Fv set to
 //         the pressure BC planes and the BC source terms of pressure.f90:138-139.
 __global__ void __launch_bounds__(256)
-k_div_fftx(ChlMap map, int s_in, int mode) {
+k_div_fftx(ChlMap map, int s_in, int mode, int xmb) {
   chl_pdl_wait();
   extern __shared__ double2 sm[];
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
   const int nrow = Ny * (Nz / 2);
-  const int CR = chl_fftx_rows(Nx, nrow);
+  const int CR = chl_fftx_rows(Nx, nrow, xmb);
   const int g0 = lb * CR;
   const int cr_n = min(CR, nrow - g0);
   double2* A = sm;
@@ -317,14 +317,14 @@ k_tri_staged(ChlMap map) {
 
 // ------------------------------------------------------------ inverse x -> pressure field
 __global__ void __launch_bounds__(256)
-k_fftx_inv(ChlMap map, int dst) {
+k_fftx_inv(ChlMap map, int dst, int xmb) {
   chl_pdl_wait();
   extern __shared__ double2 sm[];
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
   const int nrow = Ny * (Nz / 2);
-  const int CR = chl_fftx_rows(Nx, nrow);
+  const int CR = chl_fftx_rows(Nx, nrow, xmb);
   const int g0 = lb * CR;
   const int cr_n = min(CR, nrow - g0);
   double2* A = sm;
@@ -428,16 +428,17 @@ __global__ void k_pghost(ChlMap map) {
 }
 
 extern "C" {
-size_t chl_smem_fftx(int Nx, int nrow) { return (size_t)2 * chl_fftx_rows(Nx, nrow) * Nx * sizeof(double2); }
+size_t chl_smem_fftx(int Nx, int nrow, int xmb) { return (size_t)2 * chl_fftx_rows(Nx, nrow, xmb) * Nx * sizeof(double2); }
 size_t chl_smem_fftz(int maxNz, int zcw) { return (size_t)2 * maxNz * zcw * sizeof(double2); }
 // kx columns staged per z-transform block: 16, halved while two Nz x cols
 // complex tiles would exceed the 227 KB a block may use, and halved (down
-// to 2) while the grid over all `ncols` columns would cover the SMs less
-// than about four times
-int chl_fftz_cols(int maxNz, long ncols) {
+// to 2) while the grid over all `ncols` columns would have fewer than
+// min_blocks blocks (CHL_FFT_MIN_BLOCKS, about four per SM, unless the
+// tuner chose another)
+int chl_fftz_cols(int maxNz, long ncols, int min_blocks) {
   int c = 16;
   while (c > 1 && chl_smem_fftz(maxNz, c) > (size_t)227 * 1024) c /= 2;
-  while (c > 2 && (ncols + c - 1) / c < CHL_FFT_MIN_BLOCKS) c /= 2;
+  while (c > 2 && (ncols + c - 1) / c < min_blocks) c /= 2;
   return c;
 }
 int chl_fft_setup(size_t smx, size_t smz, size_t smt) {
@@ -448,7 +449,7 @@ int chl_fft_setup(size_t smx, size_t smz, size_t smt) {
                        : cudaSuccess;
   return (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) ? 1 : 0;
 }
-void chl_launch_div_fftx(const ChlMap& m, int nb, int nt, size_t smem, int s_in, int mode, cudaStream_t st) { chl_launch_pdl(k_div_fftx, dim3(nb), dim3(nt), smem, st, m, s_in, mode); }
+void chl_launch_div_fftx(const ChlMap& m, int nb, int nt, size_t smem, int s_in, int mode, int xmb, cudaStream_t st) { chl_launch_pdl(k_div_fftx, dim3(nb), dim3(nt), smem, st, m, s_in, mode, xmb); }
 void chl_launch_fftz(const ChlMap& m, int nb, int nt, size_t smem, int inv, int zcw, cudaStream_t st) { chl_launch_pdl(k_fftz, dim3(nb), dim3(nt), smem, st, m, inv, zcw); }
 // smem > 0: the staged form with TRI_W-mode blocks (chl_tri_modes_per_block)
 void chl_launch_tri(const ChlMap& m, int nb, size_t smem, cudaStream_t st) {
@@ -456,19 +457,21 @@ void chl_launch_tri(const ChlMap& m, int nb, size_t smem, cudaStream_t st) {
   else chl_launch_pdl(k_tri, dim3(nb), dim3(128), 0, st, m);
 }
 // Shared memory of the staged form for the tallest column (40 bytes per
-// row and mode), or 0 for the row-batched form.  The staged form has one
-// warp per block, so it pays only while all `modes` fit in one wave of
-// resident blocks; beyond that the row-batched form keeps more warps per SM.
-size_t chl_smem_tri(int maxNy, long modes) {
+// row and mode), or 0 for the row-batched form.  mode 0: row-batched;
+// 1: staged whenever it fits; 2 (default): staged only while all `modes`
+// fit in one wave of resident blocks - the staged form has one warp per
+// block, and beyond one wave the row-batched form keeps more warps per SM.
+size_t chl_smem_tri(int maxNy, long modes, int mode) {
   const size_t b = (size_t)maxNy * TRI_W * (sizeof(double2) + 3 * sizeof(double));
-  if (b > (size_t)CHL_TRI_SMEM_MAX) return 0;
+  if (mode == 0 || b > (size_t)CHL_TRI_SMEM_MAX) return 0;
+  if (mode == 1) return b;
   const long per_sm = (long)((228 * 1024) / (b + 1024));   // + the 1 KB the runtime reserves per block
   const long blocks = (modes + TRI_W - 1) / TRI_W;
   return blocks <= per_sm * CHL_SMS ? b : 0;
 }
 int chl_tri_modes_per_block(size_t smem) { return smem ? TRI_W : 128; }
-void chl_launch_fftx_inv(const ChlMap& m, int nb, int nt, size_t smem, int dst, cudaStream_t st) { chl_launch_pdl(k_fftx_inv, dim3(nb), dim3(nt), smem, st, m, dst); }
-void chl_launch_project(const ChlMap& m, int nb, int s, cudaStream_t st) { chl_launch_pdl(k_project, dim3(nb), dim3(256), 0, st, m, s); }
+void chl_launch_fftx_inv(const ChlMap& m, int nb, int nt, size_t smem, int dst, int xmb, cudaStream_t st) { chl_launch_pdl(k_fftx_inv, dim3(nb), dim3(nt), smem, st, m, dst, xmb); }
+void chl_launch_project(const ChlMap& m, int nb, int s, cudaStream_t st) { chl_launch_pdl(k_project, dim3(nb), dim3(m.tb), 0, st, m, s); }
 void chl_launch_pbc(const ChlMap& m, int nb, int s, cudaStream_t st) { k_pbc<<<nb, 256, 0, st>>>(m, s); }
 void chl_launch_pghost(const ChlMap& m, int nb, cudaStream_t st) { k_pghost<<<nb, 256, 0, st>>>(m); }
 }

@@ -29,16 +29,16 @@ void chl_launch_nut(const ChlMap&, int, int, int, cudaStream_t);
 void chl_launch_amd(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_vreman(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_agent_obs(const ChlInst*, int, int, double, const int*, const double*, double*, double*, cudaStream_t);
-size_t chl_smem_fftx(int, int);
+size_t chl_smem_fftx(int, int, int);
 size_t chl_smem_fftz(int, int);
-int chl_fftz_cols(int, long);
+int chl_fftz_cols(int, long, int);
 int chl_fft_setup(size_t, size_t, size_t);
-size_t chl_smem_tri(int, long);
+size_t chl_smem_tri(int, long, int);
 int chl_tri_modes_per_block(size_t);
-void chl_launch_div_fftx(const ChlMap&, int, int, size_t, int, int, cudaStream_t);
+void chl_launch_div_fftx(const ChlMap&, int, int, size_t, int, int, int, cudaStream_t);
 void chl_launch_fftz(const ChlMap&, int, int, size_t, int, int, cudaStream_t);
 void chl_launch_tri(const ChlMap&, int, size_t, cudaStream_t);
-void chl_launch_fftx_inv(const ChlMap&, int, int, size_t, int, cudaStream_t);
+void chl_launch_fftx_inv(const ChlMap&, int, int, size_t, int, int, cudaStream_t);
 void chl_launch_project(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_pbc(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_pghost(const ChlMap&, int, cudaStream_t);
@@ -196,7 +196,7 @@ struct Arena {
   size_t take(size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; }
 };
 
-int dsm_npart(int Nx, int Nz) { return (Nx * Nz + 256 * 4 - 1) / (256 * 4); }
+int dsm_npart(int Nx, int Ny, int Nz) { const int p = chl_dsm_ppt(Nx, Ny, Nz); return (Nx * Nz + 256 * p - 1) / (256 * p); }
 
 }  // namespace
 
@@ -216,6 +216,10 @@ struct chl_handle {
   size_t smem_x = 0, smem_z = 0, smem_t = 0;
   int zcw = 16;                       // kx columns per z-transform block
   int tx = 256, tz = 256;             // threads of the x and z transform blocks
+  // projection tile shapes (chl_autotune): block-count targets of the x and
+  // z transforms and the tridiagonal form (chl_smem_tri's mode)
+  int x_min_blocks = CHL_FFT_MIN_BLOCKS, z_min_blocks = CHL_FFT_MIN_BLOCKS, tri_mode = 2;
+  int tb_pt = 256;                    // threads per block of the point maps (stencils, updates)
   int LES_model = 0, wall_model = 0, any_mass = 0;
   float* d_mlp_theta = nullptr;       // learned wall model parameters (shared)
   unsigned int* d_mlp_cfg = nullptr;  // sigma, train, seed lo/hi, evaluation counter
@@ -227,7 +231,10 @@ struct chl_handle {
   int stats_pitch = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
-  ChlMap map(int which) const { return ChlMap{d_inst, d_off[which], (int)in.size()}; }
+  ChlMap map(int which) const {
+    const bool pt = which == M_PT || which == M_EDGE || which == M_FULL;
+    return ChlMap{d_inst, d_off[which], (int)in.size(), pt ? tb_pt : 256};
+  }
 };
 
 #define CK(call) do { cudaError_t e_ = (call); if (e_ != cudaSuccess) { \
@@ -247,7 +254,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   const size_t nc = (size_t)Nx * (Ny + 2) * Nz, nv = (size_t)Nx * (Ny + 1) * Nz;
   const size_t nspec = (size_t)(Ny + 2) * Nz * Nxh, ntri = (size_t)Ny * Nz * Nxh;
   const bool dsm = I.d.LES_model == CHL_LES_DYNAMIC;
-  const int npart = dsm_npart(Nx, Nz);
+  const int npart = dsm_npart(Nx, Ny, Nz);
   Arena A;
   // constants
   size_t o_rdxc = A.take(8 * (Nx + 3)), o_rdxf = A.take(8 * (Nx + 3)), o_dxf = A.take(8 * (Nx + 3));
@@ -319,7 +326,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   for (int m = 0; m < CHL_NQ; ++m) { D.q[m] = dsm ? P(o_q[m]) : nullptr; D.r[m] = dsm ? P(o_r[m]) : nullptr; }
   for (int m = 0; m < 3; ++m) D.E[m] = P(o_E[m]);
   D.spec = (double2*)(base + o_spec); D.p = P(o_p); D.P = P(o_P);
-  D.alpha = P(o_alpha); D.bc = P(o_bc); D.part = P(o_part); D.npart = npart;
+  D.alpha = P(o_alpha); D.bc = P(o_bc); D.part = P(o_part); D.npart = npart; D.dsm_ppt = chl_dsm_ppt(Nx, Ny, Nz);
   D.coef = P(o_coef); D.scal = P(o_scal);
   D.minabs = (unsigned long long*)(base + o_min); D.red = P(o_red); D.status = (int*)(base + o_status);
   D.retau = I.d.Re_tau;
@@ -398,14 +405,14 @@ static int build_maps(chl_handle* h) {
     zcols += (long)I.c.Ny * I.c.Nxh;
     modes += (long)I.c.Nz * I.c.Nxh;
   }
-  h->zcw = chl_fftz_cols(mz, zcols);
+  h->zcw = chl_fftz_cols(mz, zcols, h->z_min_blocks);
   h->tz = chl_fft_threads(h->zcw, mz);
   h->tx = 64;
   for (auto& I : h->in) {
     const int nrow = I.c.Ny * (I.c.Nz / 2);
-    h->tx = std::max(h->tx, chl_fft_threads(chl_fftx_rows(I.c.Nx, nrow), I.c.Nx));
+    h->tx = std::max(h->tx, chl_fft_threads(chl_fftx_rows(I.c.Nx, nrow, h->x_min_blocks), I.c.Nx));
   }
-  h->smem_t = chl_smem_tri(my, modes);
+  h->smem_t = chl_smem_tri(my, modes, h->tri_mode);
   const int tri_w = chl_tri_modes_per_block(h->smem_t);
   for (int m = 0; m < NMAP; ++m) {
     std::vector<int> off(n + 1, 0);
@@ -414,13 +421,13 @@ static int build_maps(chl_handle* h) {
       const int Nx = c.Nx, Ny = c.Ny, Nz = c.Nz, Nxh = c.Nxh;
       int b = 0;
       switch (m) {
-        case M_PT: b = cdiv((long)Nx * Ny * Nz, 256); break;
-        case M_EDGE: b = cdiv((long)Nx * (Ny + 1) * Nz, 256); break;
-        case M_FULL: b = cdiv((long)Nx * (Ny + 2) * Nz, 256); break;
-        case M_DSMF: b = Ny * dsm_npart(Nx, Nz); break;
+        case M_PT: b = cdiv((long)Nx * Ny * Nz, h->tb_pt); break;
+        case M_EDGE: b = cdiv((long)Nx * (Ny + 1) * Nz, h->tb_pt); break;
+        case M_FULL: b = cdiv((long)Nx * (Ny + 2) * Nz, h->tb_pt); break;
+        case M_DSMF: b = Ny * dsm_npart(Nx, Ny, Nz); break;
         case M_WALL: b = cdiv(2L * Nx * Nz, 256); break;
         case M_PLANE: b = cdiv((long)Nx * Nz, 256); break;
-        case M_FFTX: b = cdiv((long)Ny * (Nz / 2), chl_fftx_rows(Nx, Ny * (Nz / 2))); break;
+        case M_FFTX: b = cdiv((long)Ny * (Nz / 2), chl_fftx_rows(Nx, Ny * (Nz / 2), h->x_min_blocks)); break;
         case M_FFTZ: b = cdiv((long)Ny * Nxh, h->zcw); break;
         case M_TRI: b = cdiv((long)Nz * Nxh, tri_w); break;
         case M_MINABS: b = Nz * ((Ny + 15) / 16); break;   // planes x 16-row chunks (chl_misc.cu)
@@ -431,14 +438,14 @@ static int build_maps(chl_handle* h) {
       off[q + 1] = off[q] + b;
     }
     h->nblk[m] = off[n];
-    CK(cudaMalloc(&h->d_off[m], sizeof(int) * (n + 1)));
+    if (!h->d_off[m]) CK(cudaMalloc(&h->d_off[m], sizeof(int) * (n + 1)));   // rebuilt by chl_autotune
     CK(cudaMemcpy(h->d_off[m], off.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
   }
   // dynamic shared memory is per launch, so it must hold the largest
   // per-instance need: the x transform of an instance stages
   // chl_fftx_rows rows of Nx, which is not monotonic in Nx
   size_t sx = 0;
-  for (auto& I : h->in) sx = std::max(sx, chl_smem_fftx(I.c.Nx, I.c.Ny * (I.c.Nz / 2)));
+  for (auto& I : h->in) sx = std::max(sx, chl_smem_fftx(I.c.Nx, I.c.Ny * (I.c.Nz / 2), h->x_min_blocks));
   h->smem_x = sx;
   h->smem_z = chl_smem_fftz(mz, h->zcw);
   if (chl_fft_setup(h->smem_x, h->smem_z, h->smem_t)) { h->err = "FFT shared-memory size not supported"; return CHL_E_ARG; }
@@ -478,14 +485,19 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
   return CHL_OK;
 }
 
+// mode 0: pseudo-pressure and the velocity correction of set s; 1: the
+// actual pressure; 2: mode 0's transforms and solve without the correction
+// (writes only the spectrum and the pseudo-pressure scratch; chl_autotune)
 static int enqueue_projection(chl_handle* h, int s, int mode) {
   cudaStream_t st = h->st;
-  KL("div_fft_x", chl_launch_div_fftx(h->map(M_FFTX), h->nblk[M_FFTX], h->tx, h->smem_x, s, mode, st));
+  const bool correct = mode == 0;
+  if (mode == 2) mode = 0;
+  KL("div_fft_x", chl_launch_div_fftx(h->map(M_FFTX), h->nblk[M_FFTX], h->tx, h->smem_x, s, mode, h->x_min_blocks, st));
   KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->tz, h->smem_z, 0, h->zcw, st));
   KL("tridiag", chl_launch_tri(h->map(M_TRI), h->nblk[M_TRI], h->smem_t, st));
   KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->tz, h->smem_z, 1, h->zcw, st));
-  KL("ifft_x", chl_launch_fftx_inv(h->map(M_FFTX), h->nblk[M_FFTX], h->tx, h->smem_x, mode == 0 ? 0 : 1, st));
-  if (mode == 0) KL("project", chl_launch_project(h->map(M_PT), h->nblk[M_PT], s, st));
+  KL("ifft_x", chl_launch_fftx_inv(h->map(M_FFTX), h->nblk[M_FFTX], h->tx, h->smem_x, mode == 0 ? 0 : 1, h->x_min_blocks, st));
+  if (correct) KL("project", chl_launch_project(h->map(M_PT), h->nblk[M_PT], s, st));
   LAUNCHED();
   return CHL_OK;
 }
@@ -906,6 +918,161 @@ int chl_rk3_step(chl_handle* h, int nsteps) {
     CK(cudaGraphInstantiate(&h->gexec, g, 0));
   }
   for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(h->gexec, h->st));
+  return CHL_OK;
+}
+
+// ------------------------------------------------------------ tile-shape tuner
+// Candidate tile shapes are timed one group at a time, keeping the fastest:
+//   the block size of the one-thread-per-point kernels, timed on the eddy
+//     viscosity (without the wall-model rows), the face fluxes and the RHS
+//     divergence in its actual-pressure mode;
+//   the x-transform and z-transform block targets and the tridiagonal form,
+//     timed on the projection's transforms and solve without the velocity
+//     correction;
+// all on velocity set 0.  Every candidate partitions the same independent
+// points, rows, columns and modes differently and leaves each one's
+// arithmetic unchanged, so tuning never changes a result.  The timed kernels
+// write only scratch that every step recomputes; the two arrays a caller can
+// read before stepping (nu + nu_t and the pseudo-pressure) are saved and
+// restored.  The step graph is rebuilt on the next step.
+static int enqueue_stencils(chl_handle* h) {
+  int rc = enqueue_sgs(h, 0, false);
+  if (rc) return rc;
+  chl_launch_flux(h->map(M_EDGE), h->nblk[M_EDGE], 0, h->st);
+  chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, 0, 0.0, 0.0, 2, h->st);
+  LAUNCHED();
+  return CHL_OK;
+}
+
+static int time_group(chl_handle* h, int group, int reps, double* ms) {
+  int rc = build_maps(h);
+  if (rc) return rc;
+  auto run = [&]() { return group == 0 ? enqueue_stencils(h) : enqueue_projection(h, 0, 2); };
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a)); CK(cudaEventCreate(&b));
+  double best = 1e30;
+  for (int trial = 0; trial < 3; ++trial) {           // best of three trials
+    if ((rc = run())) break;                          // warm (and first-touch) outside the timing
+    CK(cudaEventRecord(a, h->st));
+    for (int r = 0; r < reps && !rc; ++r) rc = run();
+    CK(cudaEventRecord(b, h->st));
+    CK(cudaEventSynchronize(b));
+    float f = 0.f;
+    CK(cudaEventElapsedTime(&f, a, b));
+    best = std::min(best, (double)f / reps);
+  }
+  cudaEventDestroy(a); cudaEventDestroy(b);
+  *ms = best;
+  return rc;
+}
+
+int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
+  int rc = check_ready(h); if (rc) return rc;
+  if (reps < 1) reps = 1;
+  // nu + nu_t and the pseudo-pressure of every instance, restored at the end
+  std::vector<double*> saved;
+  auto ncent = [](const Inst& I) { return (size_t)I.c.Nx * (I.c.Ny + 2) * I.c.Nz; };   // centre-field length
+  for (auto& I : h->in) {
+    const size_t n = ncent(I);
+    double* s = nullptr;
+    CK(cudaMalloc(&s, 16 * n));
+    saved.push_back(s);
+    CK(cudaMemcpyAsync(s, I.dev.nut, 8 * n, cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(s + n, I.dev.p, 8 * n, cudaMemcpyDeviceToDevice, h->st));
+  }
+  auto restore = [&]() {
+    for (size_t q = 0; q < h->in.size(); ++q) {
+      const size_t n = ncent(h->in[q]);
+      cudaMemcpyAsync(h->in[q].dev.nut, saved[q], 8 * n, cudaMemcpyDeviceToDevice, h->st);
+      cudaMemcpyAsync(h->in[q].dev.p, saved[q] + n, 8 * n, cudaMemcpyDeviceToDevice, h->st);
+    }
+    cudaStreamSynchronize(h->st);
+    for (double* s : saved) cudaFree(s);
+    saved.clear();
+  };
+  rc = [&]() -> int {
+  static const int targets[] = {1, CHL_SMS, 2 * CHL_SMS, 4 * CHL_SMS, 8 * CHL_SMS, 16 * CHL_SMS};
+  std::string rep;
+  char buf[160];
+  double t = 0.0, t0 = 0.0;
+  int rc2 = time_group(h, 0, reps, &t0);
+  if (!rc2) rc2 = time_group(h, 1, reps, &t);
+  if (rc2) return rc2;
+  std::snprintf(buf, sizeof buf, "defaults: stencils %.4f ms, projection %.4f ms;", t0, t);
+  rep += buf;
+  // point-kernel block size
+  {
+    int best_v = h->tb_pt;
+    double best_t = 1e30;
+    for (int v : {64, 128, 256}) {
+      h->tb_pt = v;
+      if ((rc2 = time_group(h, 0, reps, &t))) return rc2;
+      if (t < best_t) { best_t = t; best_v = v; }
+    }
+    h->tb_pt = best_v;
+    std::snprintf(buf, sizeof buf, " point_threads %d (%.4f ms);", best_v, best_t);
+    rep += buf;
+  }
+  // x transform, then z transform: block-count targets
+  for (int g = 0; g < 2; ++g) {
+    int& knob = g == 0 ? h->x_min_blocks : h->z_min_blocks;
+    int best_v = knob;
+    double best_t = 1e30;
+    for (int v : targets) {
+      knob = v;
+      if ((rc2 = time_group(h, 1, reps, &t))) return rc2;
+      if (t < best_t) { best_t = t; best_v = v; }
+    }
+    knob = best_v;
+    std::snprintf(buf, sizeof buf, " %s_min_blocks %d (%.4f ms);", g == 0 ? "x" : "z", best_v, best_t);
+    rep += buf;
+  }
+  // tridiagonal: row-batched, or staged in shared memory where it fits
+  {
+    int my = 0;
+    long modes = 0;
+    for (auto& I : h->in) { my = std::max(my, I.c.Ny); modes += (long)I.c.Nz * I.c.Nxh; }
+    const bool fits = chl_smem_tri(my, modes, 1) > 0;
+    int best_v = 0;
+    double best_t = 1e30;
+    for (int v = 0; v <= (fits ? 1 : 0); ++v) {
+      h->tri_mode = v;
+      if ((rc2 = time_group(h, 1, reps, &t))) return rc2;
+      if (t < best_t) { best_t = t; best_v = v; }
+    }
+    h->tri_mode = best_v;
+    std::snprintf(buf, sizeof buf, " tridiag %s (%.4f ms)", best_v == 1 ? "staged" : "row-batched", best_t);
+    rep += buf;
+  }
+  if ((rc2 = build_maps(h))) return rc2;
+  if (report && report_len > 0) {
+    std::strncpy(report, rep.c_str(), (size_t)report_len - 1);
+    report[report_len - 1] = 0;
+  }
+  return CHL_OK;
+  }();
+  restore();
+  if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
+  if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+  return rc ? rc : finish(h);
+}
+
+int chl_get_tile_shapes(chl_handle* h, int* out7) {
+  if (!h || !out7) return CHL_E_ARG;
+  out7[0] = h->x_min_blocks; out7[1] = h->z_min_blocks; out7[2] = h->tri_mode; out7[3] = h->tb_pt;
+  out7[4] = h->zcw; out7[5] = h->smem_t ? 1 : 0; out7[6] = h->tx;
+  return CHL_OK;
+}
+
+int chl_set_tile_shapes(chl_handle* h, int x_min_blocks, int z_min_blocks, int tri_mode, int point_threads) {
+  if (!h || x_min_blocks < 1 || z_min_blocks < 1 || tri_mode < 0 || tri_mode > 2) return CHL_E_ARG;
+  if (point_threads != 64 && point_threads != 128 && point_threads != 256) return CHL_E_ARG;
+  h->x_min_blocks = x_min_blocks; h->z_min_blocks = z_min_blocks; h->tri_mode = tri_mode;
+  h->tb_pt = point_threads;
+  int rc = build_maps(h);
+  if (rc) return rc;
+  if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
+  if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
   return CHL_OK;
 }
 

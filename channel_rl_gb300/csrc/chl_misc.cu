@@ -346,11 +346,11 @@ void chl_launch_minabs(const ChlMap& m, int nb, int s, cudaStream_t st) {
 }
 // nb: blocks of 256 centres (the point map)
 void chl_launch_nonfinite(const ChlMap& m, int nb, int s, cudaStream_t st) {
-  chl_launch_pdl(k_nonfinite, dim3(nb), dim3(256), 0, st, m, s);
+  chl_launch_pdl(k_nonfinite, dim3(nb), dim3(m.tb), 0, st, m, s);
 }
 void chl_launch_dt(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_dt, dim3(m.n), dim3(128), 0, st, m); }
 void chl_launch_massflow(const ChlMap& m, cudaStream_t st, int s, int force) { chl_launch_pdl(k_massflow, dim3(m.n), dim3(256), 0, st, m, s, force); }
-void chl_launch_shift(const ChlMap& m, int nb, int s, cudaStream_t st) { chl_launch_pdl(k_shift, dim3(nb), dim3(256), 0, st, m, s); }
+void chl_launch_shift(const ChlMap& m, int nb, int s, cudaStream_t st) { chl_launch_pdl(k_shift, dim3(nb), dim3(m.tb), 0, st, m, s); }
 void chl_launch_tadvance(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_tadvance, dim3(m.n), dim3(32), 0, st, m); }
 void chl_launch_divmax(const ChlMap& m, int s, double* out, cudaStream_t st) { k_divmax<<<m.n, 256, 0, st>>>(m, s, out); }
 void chl_launch_qflow(const ChlInst* inst, int Nz, int s, int slot, cudaStream_t st) {

@@ -177,11 +177,11 @@ k_rhs_update(ChlMap map, RhsArgs a) {
 
 extern "C" {
 void chl_launch_flux(const ChlMap& map, int nb_edge, int sin, cudaStream_t st) {
-  chl_launch_pdl(k_flux, dim3(nb_edge), dim3(256), 0, st, map, sin);
+  chl_launch_pdl(k_flux, dim3(nb_edge), dim3(map.tb), 0, st, map, sin);
 }
 void chl_launch_update(const ChlMap& map, int nb_pt, int sbase, int sout, double c1, double c2, int mode,
                        cudaStream_t st) {
   RhsArgs a{sbase, sout, 0.25 * c1, 0.25 * c2, mode};
-  chl_launch_pdl(k_rhs_update, dim3(nb_pt), dim3(256), 0, st, map, a);
+  chl_launch_pdl(k_rhs_update, dim3(nb_pt), dim3(map.tb), 0, st, map, a);
 }
 }

@@ -205,7 +205,6 @@ k_filter_xz(ChlMap map, int from_r) {
 // One block per (centre row jc, chunk of the x-z plane); each thread sums its
 // points in a fixed order, then a fixed-order block reduction writes
 // part[0|1][jc][chunk].  Filtered fields live in r after the three passes.
-#define DSM_PPT 4
 __global__ void __launch_bounds__(256)
 k_dsm_final(ChlMap map) {
   chl_pdl_wait();
@@ -217,8 +216,9 @@ k_dsm_final(ChlMap map) {
   const int plane = Nx * Nz;
   double lm = 0.0, mm = 0.0;
   const double* const* R = I.r;
-  for (int m = 0; m < DSM_PPT; ++m) {
-    const int pidx = chunk * (256 * DSM_PPT) + m * 256 + threadIdx.x;
+  const int ppt = I.dsm_ppt;
+  for (int m = 0; m < ppt; ++m) {
+    const int pidx = chunk * (256 * ppt) + m * 256 + threadIdx.x;
     if (pidx >= plane) break;
     const int i = pidx % Nx, k = pidx / Nx;
     const size_t c = cidx(I, i, jc, k);
@@ -410,13 +410,13 @@ k_nut(ChlMap map, int s_in, int use_wm) {
 
 // ------------------------------------------------------------ launchers
 extern "C" {
-void chl_launch_edges(const ChlMap& m, int nb, int src, cudaStream_t st) { chl_launch_pdl(k_edges, dim3(nb), dim3(256), 0, st, m, src); }
-void chl_launch_centre(const ChlMap& m, int nb, int s_in, int dsm, cudaStream_t st) { chl_launch_pdl(k_centre, dim3(nb), dim3(256), 0, st, m, s_in, dsm); }
-void chl_launch_filter_y(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_filter_y, dim3(nb), dim3(256), 0, st, m, s_in); }
-void chl_launch_filter_x(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<0>, dim3(nb), dim3(256), 0, st, m, 1); }
-void chl_launch_filter_z(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<1>, dim3(nb), dim3(256), 0, st, m, 0); }
+void chl_launch_edges(const ChlMap& m, int nb, int src, cudaStream_t st) { chl_launch_pdl(k_edges, dim3(nb), dim3(m.tb), 0, st, m, src); }
+void chl_launch_centre(const ChlMap& m, int nb, int s_in, int dsm, cudaStream_t st) { chl_launch_pdl(k_centre, dim3(nb), dim3(m.tb), 0, st, m, s_in, dsm); }
+void chl_launch_filter_y(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_filter_y, dim3(nb), dim3(m.tb), 0, st, m, s_in); }
+void chl_launch_filter_x(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<0>, dim3(nb), dim3(m.tb), 0, st, m, 1); }
+void chl_launch_filter_z(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<1>, dim3(nb), dim3(m.tb), 0, st, m, 0); }
 void chl_launch_dsm_final(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_dsm_final, dim3(nb), dim3(256), 0, st, m); }
 void chl_launch_coef(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_coef, dim3(m.n), dim3(128), 0, st, m); }
 void chl_launch_eqwm(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_eqwm, dim3(nb), dim3(CHL_WALL_THREADS), 0, st, m, s_in); }
-void chl_launch_nut(const ChlMap& m, int nb, int s_in, int use_wm, cudaStream_t st) { chl_launch_pdl(k_nut, dim3(nb), dim3(256), 0, st, m, s_in, use_wm); }
+void chl_launch_nut(const ChlMap& m, int nb, int s_in, int use_wm, cudaStream_t st) { chl_launch_pdl(k_nut, dim3(nb), dim3(m.tb), 0, st, m, s_in, use_wm); }
 }

@@ -157,6 +157,6 @@ k_vreman(ChlMap map, int s_in) {
 }
 
 extern "C" {
-void chl_launch_amd(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_amd, dim3(nb), dim3(256), 0, st, m, s_in); }
-void chl_launch_vreman(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_vreman, dim3(nb), dim3(256), 0, st, m, s_in); }
+void chl_launch_amd(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_amd, dim3(nb), dim3(m.tb), 0, st, m, s_in); }
+void chl_launch_vreman(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_vreman, dim3(nb), dim3(m.tb), 0, st, m, s_in); }
 }

@@ -65,6 +65,7 @@ EXPORTS = (
     "chl_stats", "chl_stats_profiles", "chl_synchronize", "chl_grid_constants_size",
     "chl_grid_constants", "chl_set_fields", "chl_download_async", "chl_time_steps",
     "chl_graph_kernel_count", "chl_profile_step",
+    "chl_autotune", "chl_get_tile_shapes", "chl_set_tile_shapes",
     "chl_check_divergence_noalloc", "chl_noalloc_last_error",
     "chl_mlp_set_params", "chl_mlp_get_params", "chl_mlp_configure", "chl_mlp_read_trace",
     "chl_mlp_eval", "chl_tc_selftest",
@@ -124,6 +125,9 @@ def load(build_if_missing=True):
     lib.chl_time_steps.argtypes = [H, C.c_int, _F64P]
     lib.chl_graph_kernel_count.argtypes = [H, C.POINTER(C.c_int)]
     lib.chl_profile_step.argtypes = [H, C.c_int, C.c_int, C.c_char_p, _F64P, C.POINTER(C.c_int)]
+    lib.chl_autotune.argtypes = [H, C.c_int, C.c_char_p, C.c_int]
+    lib.chl_get_tile_shapes.argtypes = [H, C.POINTER(C.c_int)]
+    lib.chl_set_tile_shapes.argtypes = [H, C.c_int, C.c_int, C.c_int, C.c_int]
     lib.chl_mlp_set_params.argtypes = [H, _F32P]
     lib.chl_mlp_get_params.argtypes = [H, _F32P]
     lib.chl_mlp_configure.argtypes = [H, C.c_float, C.c_ulonglong, C.c_int]
@@ -450,6 +454,26 @@ class Channel:
             nm = raw[32 * i:32 * i + 32].split(b"\0", 1)[0].decode()
             out[nm] = (float(ms[i]), int(cnt[i]))
         return out
+
+    # -- tile-shape tuner ------------------------------------------------------
+    def autotune(self, reps=10):
+        """Time the Poisson solve's tile-shape candidates on the uploaded fields
+        and keep the fastest (chl_autotune); returns the one-line report.
+        Results are bit-identical whatever is chosen."""
+        buf = C.create_string_buffer(512)
+        self._check(self.lib.chl_autotune(self.h, int(reps), buf, 512), "chl_autotune")
+        return buf.value.decode()
+
+    def tile_shapes(self):
+        """{x_min_blocks, z_min_blocks, tri_mode, point_threads, z_cols, tri_staged, x_threads}."""
+        v = (C.c_int * 7)()
+        self._check(self.lib.chl_get_tile_shapes(self.h, v), "chl_get_tile_shapes")
+        keys = ("x_min_blocks", "z_min_blocks", "tri_mode", "point_threads", "z_cols", "tri_staged", "x_threads")
+        return dict(zip(keys, (int(x) for x in v)))
+
+    def set_tile_shapes(self, x_min_blocks, z_min_blocks, tri_mode, point_threads=256):
+        self._check(self.lib.chl_set_tile_shapes(self.h, int(x_min_blocks), int(z_min_blocks), int(tri_mode),
+                                                 int(point_threads)), "chl_set_tile_shapes")
 
     # -- reference subroutines -------------------------------------------------
     def compute_dt(self):

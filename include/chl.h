@@ -153,6 +153,28 @@ int chl_graph_kernel_count(chl_handle* h, int* count);
  * returns the number of kernel kinds (<= maxk) or <0 on error. */
 int chl_profile_step(chl_handle* h, int reps, int maxk, char* names, double* ms_per_step, int* launches_per_step);
 
+/* Tile-shape tuner.  It stands where the reference plans its FFTW
+ * transforms (initialization.f90:287-290) for the Poisson solve of
+ * projection.f90:74-128, and extends to the stencil kernels.  On the
+ * uploaded fields it times, one group at a time, the block size of the
+ * one-thread-per-point kernels (eddy viscosity, fluxes, RHS divergence),
+ * the block-count targets of the x and z transforms and the tridiagonal
+ * form (reps runs per candidate, best of three), keeps the fastest and
+ * rebuilds the step graph.  Candidates only regroup independent points,
+ * rows, columns and modes, so results are bit-identical whatever is chosen,
+ * and the state a caller can read (fields, nu_t, pseudo-pressure, wall
+ * stress) is left as it was.  report (may be NULL) receives a one-line
+ * summary. */
+int chl_autotune(chl_handle* h, int reps, char* report, int report_len);
+/* The current tile shapes: out7 = {x_min_blocks, z_min_blocks, tri_mode,
+ * point_threads, z columns per block, staged tridiagonal in use (0/1),
+ * x-transform threads}. */
+int chl_get_tile_shapes(chl_handle* h, int* out7);
+/* Sets the tile shapes by hand: block-count targets >= 1; tri_mode 0
+ * row-batched, 1 staged where it fits, 2 the default rule; point_threads
+ * 64, 128 or 256. */
+int chl_set_tile_shapes(chl_handle* h, int x_min_blocks, int z_min_blocks, int tri_mode, int point_threads);
+
 /* Learned wall model (CHL_WM_MLP).  Counterpart of the smarties policy that
  * sets alpha_x from per-agent states (smarties_stat.f90:24-260): a
  * 4-64-64-1 tanh network per wall point, BF16 weights, FP32 accumulation,
