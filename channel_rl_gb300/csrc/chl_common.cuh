@@ -115,6 +115,16 @@ enum {
 };
 
 // block -> instance map shared by all multi-instance kernels
+// One field of a three-field layout conversion: the Fortran-layout array
+// (in the staging area) with its extents n1 x n2 x n3, the device field with
+// nrow stored y rows, and the unpack rule (0 U/W-like, 1 V-like).
+struct ChlField1 {
+  double* fort;
+  double* dev;
+  int n1, n2, n3, nrow, kind;
+};
+struct ChlFields3 { ChlField1 f[3]; };
+
 struct ChlMap {
   const ChlInst* inst;   // device array of instances
   const int* off;        // prefix sum of blocks per instance, off[n] = total
@@ -163,6 +173,26 @@ __device__ __forceinline__ size_t vidx(const ChlInst& I, int i, int jv, int k) {
 }
 
 #define LDG(p) __ldg(p)
+
+// wall-model eddy viscosity at the x face a of a wall: tau / (dU/dy) - nu
+// with dU/dy = (U(wall row) - U(ghost row)) / dyw (one division)
+// (compute_wall_model, wallmodel.f90:23-46)
+__device__ __forceinline__ double wm_face(const ChlInst& I, const double* U, int a, int k, int wall) {
+  const double al = I.alpha[(size_t)wall * I.Nx * I.Nz + (size_t)k * I.Nx + a];
+  const double du = wall == 0 ? U[cidx(I, a, 1, k)] - U[cidx(I, a, 0, k)]
+                              : U[cidx(I, a, I.Ny, k)] - U[cidx(I, a, I.Ny + 1, k)];
+  return al * I.dyw / du - I.nu;
+}
+
+// The ghost-row value of nu_t next to a wall from the clipped value v of the
+// first interior row: Neumann (copy), Dirichlet (mirror), or for AMD and
+// Vreman the mirror plus 2*0.38*dPdx^0.5*(y(2)-y(1))/2 (subgrid.f90:858-871,
+// 991-1002).
+__device__ __forceinline__ double nut_ghost(const ChlInst& I, double v) {
+  if (I.Dirichlet_nu_t == 1) return -v;
+  if (I.Dirichlet_nu_t == 2 && I.LES_model >= 3) return -v + 2.0 * 0.38 * sqrt(I.scal[CHL_S_DPDX]) * I.dy1 / 2.0;
+  return v;
+}
 
 // Programmatic dependent launch inside the step graph: each step kernel is
 // launched with programmatic stream serialisation, so its blocks may be

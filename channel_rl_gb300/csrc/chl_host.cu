@@ -26,8 +26,8 @@ void chl_launch_dsm_final(const ChlMap&, int, cudaStream_t);
 void chl_launch_coef(const ChlMap&, cudaStream_t);
 void chl_launch_eqwm(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_nut(const ChlMap&, int, int, int, cudaStream_t);
-void chl_launch_amd(const ChlMap&, int, int, cudaStream_t);
-void chl_launch_vreman(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_amd(const ChlMap&, int, int, int, cudaStream_t);
+void chl_launch_vreman(const ChlMap&, int, int, int, cudaStream_t);
 void chl_launch_agent_obs(const ChlInst*, int, int, double, const int*, const double*, double*, double*, cudaStream_t);
 size_t chl_smem_fftx(int, int, int);
 size_t chl_smem_fftz(int, int);
@@ -42,8 +42,9 @@ void chl_launch_fftx_inv(const ChlMap&, int, int, size_t, int, int, cudaStream_t
 void chl_launch_project(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_pbc(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_pghost(const ChlMap&, int, cudaStream_t);
-void chl_launch_unpack(double*, const double*, int, int, int, int, int, int, cudaStream_t);
 void chl_launch_pack(double*, const double*, int, int, int, int, int, int, double, cudaStream_t);
+void chl_launch_unpack3(const ChlFields3&, int, int, cudaStream_t);
+void chl_launch_pack3(const ChlFields3&, int, int, cudaStream_t);
 void chl_launch_pack_unique(double*, const double*, int, int, int, int, int, cudaStream_t);
 void chl_launch_minabs(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_nonfinite(const ChlMap&, int, int, cudaStream_t);
@@ -286,7 +287,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   size_t o_red = A.take(8 * 2 * (size_t)Nz);
   size_t o_trace = A.take(4 * (size_t)MLP_NPARAM);
   I.nstage = (size_t)c.nxg * c.nyg * c.nzg;
-  size_t o_stage = A.take(8 * I.nstage);
+  size_t o_stage = A.take(3 * 8 * I.nstage);   // three Fortran-layout fields (chl_set_fields)
   cudaError_t e = cudaMalloc(&I.arena, A.off);
   if (e != cudaSuccess) { h->err = "device allocation failed (" + std::to_string(A.off) + " bytes)"; return CHL_E_NOMEM; }
   CK(cudaMemsetAsync(I.arena, 0, A.off, h->st));
@@ -456,6 +457,16 @@ static int build_maps(chl_handle* h) {
 // ------------------------------------------------------------ schedules
 static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
   cudaStream_t st = h->st;
+  // AMD and Vreman write nu + nu_t in their own kernel, whose wall-model
+  // rows need the wall stress first; the other models leave it to k_nut
+  const bool fused = h->LES_model == CHL_LES_AMD || h->LES_model == CHL_LES_VREMAN;
+  auto wall_stress = [&]() {
+    if (with_wm && (h->wall_model == CHL_WM_EQLOG || h->wall_model == CHL_WM_MLP))
+      KL("eq_wallmodel", chl_launch_eqwm(h->map(M_WALLN), h->nblk[M_WALLN], s, st));
+    if (with_wm && h->wall_model == CHL_WM_MLP)
+      KL("mlp_wallmodel", chl_launch_mlp(h->map(M_MLP), h->nblk[M_MLP], s, stage, h->d_mlp_status, st));
+  };
+  if (fused) wall_stress();
   if (h->LES_model == CHL_LES_DYNAMIC) {
     KL("edges", chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st));
     KL("centre_strain", chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 1, st));
@@ -468,19 +479,17 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
     KL("edges", chl_launch_edges(h->map(M_EDGE), h->nblk[M_EDGE], s, st));
     KL("centre_strain", chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 0, st));
   } else if (h->LES_model == CHL_LES_AMD) {
-    KL("amd", chl_launch_amd(h->map(M_PT), h->nblk[M_PT], s, st));
+    KL("amd", chl_launch_amd(h->map(M_PT), h->nblk[M_PT], s, with_wm ? 1 : 0, st));
   } else if (h->LES_model == CHL_LES_VREMAN) {
-    KL("vreman", chl_launch_vreman(h->map(M_PT), h->nblk[M_PT], s, st));
+    KL("vreman", chl_launch_vreman(h->map(M_PT), h->nblk[M_PT], s, with_wm ? 1 : 0, st));
   }
-  // the row coefficient exists for the Smagorinsky models only (k_nut
-  // takes AMD's and Vreman's S as nu_t, and no model leaves nu_t = 0)
+  // the row coefficient exists for the Smagorinsky models only
   if (h->LES_model == CHL_LES_DYNAMIC || h->LES_model == CHL_LES_SMAGORINSKY)
     KL("nut_coef", chl_launch_coef(h->map(M_PT), st));
-  if (with_wm && (h->wall_model == CHL_WM_EQLOG || h->wall_model == CHL_WM_MLP))
-    KL("eq_wallmodel", chl_launch_eqwm(h->map(M_WALLN), h->nblk[M_WALLN], s, st));
-  if (with_wm && h->wall_model == CHL_WM_MLP)
-    KL("mlp_wallmodel", chl_launch_mlp(h->map(M_MLP), h->nblk[M_MLP], s, stage, h->d_mlp_status, st));
-  KL("nut", chl_launch_nut(h->map(M_FULL), h->nblk[M_FULL], s, with_wm ? 1 : 0, st));
+  if (!fused) {
+    wall_stress();
+    KL("nut", chl_launch_nut(h->map(M_FULL), h->nblk[M_FULL], s, with_wm ? 1 : 0, st));
+  }
   LAUNCHED();
   return CHL_OK;
 }
@@ -676,21 +685,31 @@ static Inst* get_inst(chl_handle* h, int inst) {
   return &h->in[inst];
 }
 
+// U, V, W of velocity set 0 and their Fortran-layout slots in the staging area
+static ChlFields3 fields3(Inst* I) {
+  const Consts& c = I->c;
+  double* s = I->staging;
+  const size_t n = I->nstage;
+  ChlFields3 f;
+  f.f[0] = ChlField1{s, I->dev.U[0], c.nx, c.nyg, c.nzg, c.Ny + 2, 0};
+  f.f[1] = ChlField1{s + n, I->dev.V[0], c.nxg, c.ny, c.nzg, c.Ny + 1, 1};
+  f.f[2] = ChlField1{s + 2 * n, I->dev.W[0], c.nxg, c.nyg, c.nz, c.Ny + 2, 0};
+  return f;
+}
+
 int chl_upload(chl_handle* h, int inst, const double* U, const double* V, const double* W) {
   Inst* I = get_inst(h, inst);
   if (!I) return CHL_E_ARG;
   if (!U || !V || !W) { h->err = "null field"; return CHL_E_ARG; }
-  const Consts& c = I->c;
-  const int Nx = c.Nx, Ny = c.Ny, Nz = c.Nz;
-  struct { const double* src; double* dst; int n1, n2, n3, nrow, kind; } f[3] = {
-      {U, I->dev.U[0], c.nx, c.nyg, c.nzg, Ny + 2, 0},
-      {V, I->dev.V[0], c.nxg, c.ny, c.nzg, Ny + 1, 1},
-      {W, I->dev.W[0], c.nxg, c.nyg, c.nz, Ny + 2, 0}};
-  for (auto& q : f) {
-    CK(cudaMemcpyAsync(I->staging, q.src, 8 * (size_t)q.n1 * q.n2 * q.n3, cudaMemcpyHostToDevice, h->st));
-    chl_launch_unpack(q.dst, I->staging, Nx, q.nrow, Nz, q.n1, q.n2, q.kind, h->st);
-    LAUNCHED();
+  const ChlFields3 f3 = fields3(I);
+  const double* src[3] = {U, V, W};
+  for (int q = 0; q < 3; ++q) {
+    const ChlField1& d = f3.f[q];
+    CK(cudaMemcpyAsync(d.fort, src[q], 8 * (size_t)d.n1 * d.n2 * d.n3, cudaMemcpyHostToDevice, h->st));
   }
+  chl_launch_unpack3(f3, I->c.Nx, I->c.Nz, h->st);
+  LAUNCHED();
+  const int Nz = I->c.Nz;
   // Qflow_x_0 of this instance (mass_flow.f90:271-309); the kernel runs per instance
   chl_launch_qflow(h->d_inst + inst, Nz, 0, CHL_S_Q0, h->st);
   LAUNCHED();
@@ -969,22 +988,30 @@ static int time_group(chl_handle* h, int group, int reps, double* ms) {
 int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
   int rc = check_ready(h); if (rc) return rc;
   if (reps < 1) reps = 1;
-  // nu + nu_t and the pseudo-pressure of every instance, restored at the end
+  // nu + nu_t, the pseudo-pressure, S (the strain or model nu_t that
+  // chl_compute_wall_model rebuilds nu_t from) and the row coefficients of
+  // every instance, restored at the end
   std::vector<double*> saved;
   auto ncent = [](const Inst& I) { return (size_t)I.c.Nx * (I.c.Ny + 2) * I.c.Nz; };   // centre-field length
+  auto ncoef = [](const Inst& I) { return (size_t)I.c.Ny + 2; };
   for (auto& I : h->in) {
     const size_t n = ncent(I);
     double* s = nullptr;
-    CK(cudaMalloc(&s, 16 * n));
+    CK(cudaMalloc(&s, 8 * (3 * n + ncoef(I))));
     saved.push_back(s);
     CK(cudaMemcpyAsync(s, I.dev.nut, 8 * n, cudaMemcpyDeviceToDevice, h->st));
     CK(cudaMemcpyAsync(s + n, I.dev.p, 8 * n, cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(s + 2 * n, I.dev.S, 8 * n, cudaMemcpyDeviceToDevice, h->st));
+    CK(cudaMemcpyAsync(s + 3 * n, I.dev.coef, 8 * ncoef(I), cudaMemcpyDeviceToDevice, h->st));
   }
   auto restore = [&]() {
     for (size_t q = 0; q < h->in.size(); ++q) {
-      const size_t n = ncent(h->in[q]);
-      cudaMemcpyAsync(h->in[q].dev.nut, saved[q], 8 * n, cudaMemcpyDeviceToDevice, h->st);
-      cudaMemcpyAsync(h->in[q].dev.p, saved[q] + n, 8 * n, cudaMemcpyDeviceToDevice, h->st);
+      const Inst& I = h->in[q];
+      const size_t n = ncent(I);
+      cudaMemcpyAsync(I.dev.nut, saved[q], 8 * n, cudaMemcpyDeviceToDevice, h->st);
+      cudaMemcpyAsync(I.dev.p, saved[q] + n, 8 * n, cudaMemcpyDeviceToDevice, h->st);
+      cudaMemcpyAsync(I.dev.S, saved[q] + 2 * n, 8 * n, cudaMemcpyDeviceToDevice, h->st);
+      cudaMemcpyAsync(I.dev.coef, saved[q] + 3 * n, 8 * ncoef(I), cudaMemcpyDeviceToDevice, h->st);
     }
     cudaStreamSynchronize(h->st);
     for (double* s : saved) cudaFree(s);
@@ -1171,16 +1198,15 @@ int chl_set_fields(chl_handle* h, int inst, const double* U, const double* V, co
   if (!I) return CHL_E_ARG;
   if (!I->uploaded) { h->err = "chl_set_fields before chl_upload"; return CHL_E_STATE; }
   if (!U || !V || !W) { h->err = "null field"; return CHL_E_ARG; }
-  const Consts& c = I->c;
-  struct { const double* src; double* dst; int n1, n2, n3, nrow, kind; } f[3] = {
-      {U, I->dev.U[0], c.nx, c.nyg, c.nzg, c.Ny + 2, 0},
-      {V, I->dev.V[0], c.nxg, c.ny, c.nzg, c.Ny + 1, 1},
-      {W, I->dev.W[0], c.nxg, c.nyg, c.nz, c.Ny + 2, 0}};
-  for (auto& q : f) {
-    CK(cudaMemcpyAsync(I->staging, q.src, 8 * (size_t)q.n1 * q.n2 * q.n3, cudaMemcpyHostToDevice, h->st));
-    chl_launch_unpack(q.dst, I->staging, c.Nx, q.nrow, c.Nz, q.n1, q.n2, q.kind, h->st);
-    LAUNCHED();
+  // the three copies back to back into the staging area, one conversion
+  const ChlFields3 f3 = fields3(I);
+  const double* src[3] = {U, V, W};
+  for (int q = 0; q < 3; ++q) {
+    const ChlField1& d = f3.f[q];
+    CK(cudaMemcpyAsync(d.fort, src[q], 8 * (size_t)d.n1 * d.n2 * d.n3, cudaMemcpyHostToDevice, h->st));
   }
+  chl_launch_unpack3(f3, I->c.Nx, I->c.Nz, h->st);
+  LAUNCHED();
   CK(cudaMemsetAsync(I->dev.status, 0, sizeof(int), h->st));
   return CHL_OK;   // stream-ordered; no synchronisation
 }
@@ -1188,16 +1214,15 @@ int chl_set_fields(chl_handle* h, int inst, const double* U, const double* V, co
 int chl_download_async(chl_handle* h, int inst, double* U, double* V, double* W) {
   Inst* I = get_inst(h, inst);
   if (!I) return CHL_E_ARG;
-  const Consts& c = I->c;
-  struct { double* dst; const double* src; int n1, n2, n3, nrow; } f[3] = {
-      {U, I->dev.U[0], c.nx, c.nyg, c.nzg, c.Ny + 2}, {V, I->dev.V[0], c.nxg, c.ny, c.nzg, c.Ny + 1},
-      {W, I->dev.W[0], c.nxg, c.nyg, c.nz, c.Ny + 2}};
-  for (auto& q : f) {
-    if (!q.dst) continue;
-    // one staging buffer: each copy must leave it before the next pack
-    chl_launch_pack(I->staging, q.src, c.Nx, q.nrow, c.Nz, q.n1, q.n2, q.n3, 0.0, h->st);
-    LAUNCHED();
-    CK(cudaMemcpyAsync(q.dst, I->staging, 8 * (size_t)q.n1 * q.n2 * q.n3, cudaMemcpyDeviceToHost, h->st));
+  // one conversion into the staging area, then the copies back to back
+  const ChlFields3 f3 = fields3(I);
+  double* dst[3] = {U, V, W};
+  chl_launch_pack3(f3, I->c.Nx, I->c.Nz, h->st);
+  LAUNCHED();
+  for (int q = 0; q < 3; ++q) {
+    if (!dst[q]) continue;
+    const ChlField1& d = f3.f[q];
+    CK(cudaMemcpyAsync(dst[q], d.fort, 8 * (size_t)d.n1 * d.n2 * d.n3, cudaMemcpyDeviceToHost, h->st));
   }
   return CHL_OK;
 }

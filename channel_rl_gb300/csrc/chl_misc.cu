@@ -3,23 +3,9 @@
 
 // ------------------------------------------------------------ Fortran <-> device layout
 // Fortran array F(n1,n2,n3) (column-major, full ghosted extents of the
-// reference) -> device field: x/z unique points, all y rows.
-// kind 0: U/W-like (ghost rows 0 and Ny+1 = minus the first interior row),
-// kind 1: V-like (wall rows 0 and Ny set to zero).
-__global__ void k_unpack(double* dst, const double* __restrict__ F, int Nx, int nrow, int Nz,
-                         int n1, int n2, int kind) {
-  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (long)Nx * nrow * Nz) return;
-  const int i = (int)(t % Nx), j = (int)((t / Nx) % nrow), k = (int)(t / ((long)Nx * nrow));
-  const size_t d = (size_t)i + (size_t)Nx * ((size_t)j + (size_t)nrow * k);
-  const int last = nrow - 1;
-  if (kind == 1 && (j == 0 || j == last)) { dst[d] = 0.0; return; }
-  int js = j; double sg = 1.0;
-  if (kind == 0 && j == 0) { js = 1; sg = -1.0; }
-  if (kind == 0 && j == last) { js = last - 1; sg = -1.0; }
-  const size_t f = (size_t)(i + 1) + (size_t)n1 * ((size_t)js + (size_t)n2 * (size_t)(k + 1));
-  dst[d] = sg * F[f];
-}
+// reference) <-> device field: x/z unique points, all y rows.  Unpacking
+// (k_unpack3): kind 0 U/W-like (ghost rows 0 and Ny+1 = minus the first
+// interior row), kind 1 V-like (wall rows 0 and Ny set to zero).
 
 // device field -> Fortran array with every ghost filled (periodic copies in
 // x and z, stored ghost/wall rows in y)
@@ -35,6 +21,38 @@ __global__ void k_pack(double* __restrict__ F, const double* __restrict__ src, i
   F[t] = sub == 0.0 ? v : v - sub;     // nu_t is stored as nu + nu_t
 }
 
+// The same two conversions for U, V and W in one launch (blockIdx.y picks
+// the field), between the device fields and the three Fortran-layout
+// arrays of the staging area, so that the three host copies of a transfer
+// run back to back and one kernel converts them.
+__global__ void k_unpack3(ChlFields3 f3, int Nx, int Nz) {
+  const ChlField1& q = f3.f[blockIdx.y];
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nrow = q.nrow;
+  if (t >= (long)Nx * nrow * Nz) return;
+  const int i = (int)(t % Nx), j = (int)((t / Nx) % nrow), k = (int)(t / ((long)Nx * nrow));
+  const size_t d = (size_t)i + (size_t)Nx * ((size_t)j + (size_t)nrow * k);
+  const int last = nrow - 1;
+  if (q.kind == 1 && (j == 0 || j == last)) { q.dev[d] = 0.0; return; }
+  int js = j; double sg = 1.0;
+  if (q.kind == 0 && j == 0) { js = 1; sg = -1.0; }
+  if (q.kind == 0 && j == last) { js = last - 1; sg = -1.0; }
+  const size_t fi = (size_t)(i + 1) + (size_t)q.n1 * ((size_t)js + (size_t)q.n2 * (size_t)(k + 1));
+  q.dev[d] = sg * q.fort[fi];
+}
+
+__global__ void k_pack3(ChlFields3 f3, int Nx, int Nz) {
+  const ChlField1& q = f3.f[blockIdx.y];
+  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int n1 = q.n1, n2 = q.n2, nrow = q.nrow;
+  if (t >= (long)n1 * n2 * q.n3) return;
+  const int i1 = (int)(t % n1), j1 = (int)((t / n1) % n2), k1 = (int)(t / ((long)n1 * n2));
+  int i = (i1 - 1) % Nx; if (i < 0) i += Nx;
+  int k = (k1 - 1) % Nz; if (k < 0) k += Nz;
+  const int j = j1 < nrow ? j1 : nrow - 1;
+  q.fort[t] = q.dev[(size_t)i + (size_t)Nx * ((size_t)j + (size_t)nrow * k)];
+}
+
 // device field (rows jlo..jhi) -> dense unique-point array (Nx, jhi-jlo+1, Nz)
 __global__ void k_pack_unique(double* __restrict__ F, const double* __restrict__ src, int Nx, int nrow,
                               int Nz, int jlo, int nj) {
@@ -45,14 +63,21 @@ __global__ void k_pack_unique(double* __restrict__ F, const double* __restrict__
 }
 
 extern "C" {
-void chl_launch_unpack(double* dst, const double* F, int Nx, int nrow, int Nz, int n1, int n2, int kind, cudaStream_t st) {
-  long n = (long)Nx * nrow * Nz;
-  k_unpack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(dst, F, Nx, nrow, Nz, n1, n2, kind);
-}
 void chl_launch_pack(double* F, const double* src, int Nx, int nrow, int Nz, int n1, int n2, int n3, double sub,
                      cudaStream_t st) {
   long n = (long)n1 * n2 * n3;
   k_pack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, src, Nx, nrow, Nz, n1, n2, n3, sub);
+}
+// one launch for the three fields; grid x covers the largest of them
+void chl_launch_unpack3(const ChlFields3& f3, int Nx, int Nz, cudaStream_t st) {
+  long n = 0;
+  for (auto& q : f3.f) n = n > (long)Nx * q.nrow * Nz ? n : (long)Nx * q.nrow * Nz;
+  k_unpack3<<<dim3((unsigned)((n + 255) / 256), 3), 256, 0, st>>>(f3, Nx, Nz);
+}
+void chl_launch_pack3(const ChlFields3& f3, int Nx, int Nz, cudaStream_t st) {
+  long n = 0;
+  for (auto& q : f3.f) n = n > (long)q.n1 * q.n2 * q.n3 ? n : (long)q.n1 * q.n2 * q.n3;
+  k_pack3<<<dim3((unsigned)((n + 255) / 256), 3), 256, 0, st>>>(f3, Nx, Nz);
 }
 void chl_launch_pack_unique(double* F, const double* src, int Nx, int nrow, int Nz, int jlo, int nj, cudaStream_t st) {
   long n = (long)Nx * nj * Nz;

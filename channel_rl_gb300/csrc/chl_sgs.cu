@@ -353,15 +353,6 @@ k_eqwm(ChlMap map, int s_in) {
 }
 
 // ------------------------------------------------------------ nu_t (+ wall model rows)
-// wall-model eddy viscosity at the x face a of a wall: tau / (dU/dy) - nu
-// with dU/dy = (U(wall row) - U(ghost row)) / dyw (one division)
-__device__ __forceinline__ double wm_face(const ChlInst& I, const double* U, int a, int k, int wall) {
-  const double al = I.alpha[(size_t)wall * I.Nx * I.Nz + (size_t)k * I.Nx + a];
-  const double du = wall == 0 ? U[cidx(I, a, 1, k)] - U[cidx(I, a, 0, k)]
-                              : U[cidx(I, a, I.Ny, k)] - U[cidx(I, a, I.Ny + 1, k)];
-  return al * I.dyw / du - I.nu;
-}
-
 // One thread per centre (i, jc, k), jc = 0..Ny+1.  On the wall-model rows
 // (jc = 0, 1 and Ny, Ny+1) nu_t is the mean of the face values at x faces
 // i-1 and i: each thread forms face i and takes face i-1 from the lane to
@@ -395,14 +386,7 @@ k_nut(ChlMap map, int s_in, int use_wm) {
     // AMD and Vreman store nu_t itself in S (row coefficient 1)
     const double sv = I.S[cidx(I, i, js, k)];
     v = fmax(I.LES_model >= 3 ? sv : I.coef[js] * sv, 0.0);
-    if (ghost) {
-      if (I.Dirichlet_nu_t == 1) {
-        v = -v;
-      } else if (I.Dirichlet_nu_t == 2 && I.LES_model >= 3) {
-        // -nu_t + 2*0.38*dPdx^0.5*(y(2)-y(1))/2 (subgrid.f90:868-871, 998-1001)
-        v = -v + 2.0 * 0.38 * sqrt(I.scal[CHL_S_DPDX]) * I.dy1 / 2.0;
-      }
-    }
+    if (ghost) v = nut_ghost(I, v);
   }
   // stored as nu + nu_t: every consumer adds nu (equations.f90:139-155)
   I.nut[cidx(I, i, jc, k)] = I.nu + v;

@@ -1,7 +1,9 @@
 // Anisotropic minimum-dissipation (AMD) and Vreman eddy viscosities, one
 // fused kernel each, one thread per interior centre (rows 1..Ny).  Both write
-// the unclipped nu_t into S; k_coef sets the row coefficient to 1 and k_nut
-// applies max(.,0), the ghost-row rule of Dirichlet_nu_t and the wall model.
+// the unclipped nu_t into S and, in the same pass, nu + nu_t with k_nut's
+// rules for these models (write_nut_rows): max(., 0), the ghost-row rule of
+// Dirichlet_nu_t and, when use_wm, the wall-model rows - so the step runs the
+// wall-stress kernels first and no separate nu_t pass.
 //
 // AMD (subgrid.f90:632-874):
 //   nu_t = max(0, -C N / D),  C = 0.3,
@@ -81,19 +83,49 @@ __device__ __forceinline__ Grad gradients(const ChlInst& I, const double* U, con
   return g;
 }
 
+// nu + nu_t for the interior centre (i, jc, k) from its unclipped value v,
+// plus the ghost row next to the first and last interior rows; with the
+// wall model on, rows 0, 1 and Ny, Ny+1 take the mean of the wall-model face
+// values at x faces i-1 and i (face i-1 from the lane to the left when that
+// lane is on the same row, i > 0).  Every lane of the warp reaches the
+// shuffle; lanes past the instance's last centre carry valid = false.
+__device__ __forceinline__ void write_nut_rows(const ChlInst& I, const double* U, int i, int jc, int k, double v,
+                                               int use_wm, bool valid) {
+  const int Ny = I.Ny;
+  const bool wmrow = valid && use_wm && I.wall_model != 0 && (jc == 1 || jc == Ny);
+  const int wall = jc == 1 ? 0 : 1;
+  const double f = wmrow ? wm_face(I, U, i, k, wall) : 0.0;
+  const double f_left = __shfl_up_sync(0xffffffffu, f, 1);
+  if (!valid) return;
+  const double nu = I.nu;
+  double* nt = I.nut;
+  if (wmrow) {
+    const double fl = ((threadIdx.x & 31) > 0 && i > 0) ? f_left : wm_face(I, U, wrap(i - 1, I.Nx), k, wall);
+    const double w = 0.5 * (fl + f);
+    nt[cidx(I, i, jc, k)] = nu + w;
+    nt[cidx(I, i, jc == 1 ? 0 : Ny + 1, k)] = nu + w;
+    return;
+  }
+  const double vc = fmax(v, 0.0);
+  nt[cidx(I, i, jc, k)] = nu + vc;
+  if (jc == 1) nt[cidx(I, i, 0, k)] = nu + nut_ghost(I, vc);
+  if (jc == Ny) nt[cidx(I, i, Ny + 1, k)] = nu + nut_ghost(I, vc);
+}
+
 }  // namespace
 
 __global__ void __launch_bounds__(256)
-k_amd(ChlMap map, int s_in) {
+k_amd(ChlMap map, int s_in, int use_wm) {
   chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
-  if (t >= (long)Nx * Ny * Nz) return;
-  const int i = (int)(t % Nx);
-  const int jc = 1 + (int)((t / Nx) % Ny);
-  const int k = (int)(t / ((long)Nx * Ny));
+  const long t = (long)lb * blockDim.x + threadIdx.x;
+  const bool valid = t < (long)Nx * Ny * Nz;
+  const long tv = valid ? t : 0;   // lanes past the end compute point 0 and write nothing
+  const int i = (int)(tv % Nx);
+  const int jc = 1 + (int)((tv / Nx) % Ny);
+  const int k = (int)(tv / ((long)Nx * Ny));
   const Grad g = gradients(I, I.U[s_in], I.V[s_in], I.W[s_in], i, jc, k);
   // centre strain: diagonal S_ii; 8 S_ij off the diagonal
   const double s11 = g.dux * g.rxc, s22 = g.dvy * g.ryc, s33 = g.dwz * g.rzc;
@@ -118,20 +150,23 @@ k_amd(ChlMap map, int s_in) {
   double N = a11 * s11;
   N = fma(a22, s22, N); N = fma(a33, s33, N);
   N = fma(a12, t12, N); N = fma(a13, t13, N); N = fma(a23, t23, N);
-  I.S[cidx(I, i, jc, k)] = (-0.3 * N) / D;
+  const double v = (-0.3 * N) / D;
+  if (valid) I.S[cidx(I, i, jc, k)] = v;
+  write_nut_rows(I, I.U[s_in], i, jc, k, v, use_wm, valid);
 }
 
 __global__ void __launch_bounds__(256)
-k_vreman(ChlMap map, int s_in) {
+k_vreman(ChlMap map, int s_in, int use_wm) {
   chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
-  if (t >= (long)Nx * Ny * Nz) return;
-  const int i = (int)(t % Nx);
-  const int jc = 1 + (int)((t / Nx) % Ny);
-  const int k = (int)(t / ((long)Nx * Ny));
+  const long t = (long)lb * blockDim.x + threadIdx.x;
+  const bool valid = t < (long)Nx * Ny * Nz;
+  const long tv = valid ? t : 0;
+  const int i = (int)(tv % Nx);
+  const int jc = 1 + (int)((tv / Nx) % Ny);
+  const int k = (int)(tv / ((long)Nx * Ny));
   const Grad g = gradients(I, I.U[s_in], I.V[s_in], I.W[s_in], i, jc, k);
   // a_ij = du_j/dx_i (reference layout 1 4 5 / 7 2 6 / 8 9 3); the
   // off-diagonal entries are kept 4 x (the 1/16 is folded below)
@@ -153,10 +188,12 @@ k_vreman(ChlMap map, int s_in) {
   double Ao = a4 * a4;
   Ao = fma(a5, a5, Ao); Ao = fma(a6, a6, Ao); Ao = fma(a7, a7, Ao); Ao = fma(a8, a8, Ao); Ao = fma(a9, a9, Ao);
   Ab = fma(0.0625, Ao, Ab);
-  I.S[cidx(I, i, jc, k)] = 2.5 * (0.1 * 0.1) * sqrt(Bb / Ab);
+  const double v = 2.5 * (0.1 * 0.1) * sqrt(Bb / Ab);
+  if (valid) I.S[cidx(I, i, jc, k)] = v;
+  write_nut_rows(I, I.U[s_in], i, jc, k, v, use_wm, valid);
 }
 
 extern "C" {
-void chl_launch_amd(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_amd, dim3(nb), dim3(m.tb), 0, st, m, s_in); }
-void chl_launch_vreman(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_vreman, dim3(nb), dim3(m.tb), 0, st, m, s_in); }
+void chl_launch_amd(const ChlMap& m, int nb, int s_in, int use_wm, cudaStream_t st) { chl_launch_pdl(k_amd, dim3(nb), dim3(m.tb), 0, st, m, s_in, use_wm); }
+void chl_launch_vreman(const ChlMap& m, int nb, int s_in, int use_wm, cudaStream_t st) { chl_launch_pdl(k_vreman, dim3(nb), dim3(m.tb), 0, st, m, s_in, use_wm); }
 }

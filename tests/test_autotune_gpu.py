@@ -13,6 +13,7 @@ pytestmark = pytest.mark.gpu
 
 WORKLOADS = {
     "rl_case_sized": lambda: [replace(C.smaller(C.rl_case(), 64, 40, 32), name="rl")],
+    "vreman_rule2": lambda: [replace(C.smaller(C.rl_case(), 48, 24, 36), name="vr", LES_model=C.LES_VREMAN)],
     "c2_64cubed": lambda: [C.c2_wm64()],
     "uneven_batch": lambda: [C.smaller(C.c2_wm64(), 32, 16, 16), C.smaller(C.c3_roofline(les=C.LES_DSM), 48, 24, 36),
                              replace(C.smaller(C.rl_case(), 24, 10, 12), name="b2", LES_model=C.LES_DSM)],
@@ -48,9 +49,15 @@ def _run(cases_, shapes=None, tune=False):
         for k in before[q]:
             assert np.array_equal(before[q][k], after[q][k]), ("tuning changed", q, k)
     info = ch.tile_shapes()
+    # rebuilds nu_t from the strain / model nu_t and row coefficients the
+    # last stage left, which the tuner's timing runs must not have replaced
+    ch.compute_wall_model()
+    wm_nut = [ch.download(inst=q, fields=("nu_t",))["nu_t"] for q in range(len(cases_))]
     ch.step(STEPS - 1)
     ch.compute_pressure()            # the same transforms in their pressure mode
     out = [ch.download(inst=q, fields=("U", "V", "W", "P", "nu_t")) for q in range(len(cases_))]
+    for q in range(len(cases_)):
+        out[q]["wm_nut"] = wm_nut[q]
     ch.close()
     return out, info, report
 
@@ -64,7 +71,7 @@ def test_tuned_and_forced_shapes_are_bit_identical(name):
         runs[shapes] = _run(cases_, shapes=shapes)
     for key, (out, info, report) in runs.items():
         for q in range(len(cases_)):
-            for f in ("U", "V", "W", "P", "nu_t"):
+            for f in ("U", "V", "W", "P", "nu_t", "wm_nut"):
                 assert np.array_equal(out[q][f], ref[q][f]), (key, info, q, f)
     # the forced shapes did change the partition
     assert runs[FORCED[0]][1]["tri_staged"] == 0 and runs[FORCED[0]][1]["point_threads"] == 64
