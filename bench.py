@@ -407,6 +407,24 @@ def timed_rate(cases_, args, steps, setup=None):
     return sum(c.points for c in cases_) * steps / (ms * 1e-3), ms / steps
 
 
+def utau_gate(theta, steps=120, spinup=200):
+    """The accuracy half of the batched line: u_tau error of each of the 16
+    channels against its target, from the wall stress averaged over `steps`
+    deterministic steps after a `spinup`, with the learned correction and
+    with the equilibrium model it corrects (channel_rl_gb300.rl.Trainer)."""
+    from channel_rl_gb300.rl import Trainer
+    tr = Trainer(C.c5_learned(), spinup=spinup)
+    try:
+        _, ut_l = tr.evaluate(theta, steps=steps)
+        _, ut_e = tr.evaluate(None, steps=steps)
+    finally:
+        tr.close()
+    return {"gate": 0.02, "steps": steps, "spinup": spinup,
+            "learned_max": float(max(ut_l)), "learned_mean": float(sum(ut_l) / len(ut_l)),
+            "equilibrium_max": float(max(ut_e)), "equilibrium_mean": float(sum(ut_e) / len(ut_e)),
+            "within_gate": bool(max(ut_l) <= 0.02)}
+
+
 def batched_mlp_rate(args):
     """16 uneven channels with the learned wall model in one launch per
     kernel, against the same 16 channels run one at a time, each as a plain
@@ -434,7 +452,8 @@ def batched_mlp_rate(args):
             "speedup_vs_plain_single": rate_b / rate_s,
             "plain_single_small_channel": {"grid": f"{small.Nx}x{small.Ny}x{small.Nz}", "value": rate_c1,
                                            "sgs": "dynamic-smagorinsky", "wall_model": "none"},
-            "speedup_vs_plain_single_small_channel": rate_b / rate_c1}
+            "speedup_vs_plain_single_small_channel": rate_b / rate_c1,
+            "u_tau_error": utau_gate(theta)}
 
 
 def e2e_rate(ch, case, args):

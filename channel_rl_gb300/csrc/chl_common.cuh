@@ -25,6 +25,20 @@
 #define CHL_SMS 152
 #define CHL_MIN_BLOCKS (4 * CHL_SMS)
 #define CHL_FFT_MIN_BLOCKS CHL_MIN_BLOCKS
+// Lanes sharing one mode's tridiagonal column (k_tri_scan).  The split
+// pays only where the whole solve is a few hundred serial chains; it costs
+// about twice the FP64 work, which a batch that fills the GPU would feel.
+// So: 1 for instances of CHL_TRI_SPLIT_MODES modes or more, else doubled
+// up to 8 while the instance has fewer than CHL_MIN_BLOCKS x 32 mode-lanes
+// and every lane keeps at least two rows.  A function of the instance's own
+// extents only, like chl_dsm_ppt.
+#define CHL_TRI_SPLIT_MODES 1024
+__host__ __device__ inline int chl_tri_lanes(long modes, int Ny) {
+  int P = 1;
+  if (modes >= CHL_TRI_SPLIT_MODES) return 1;
+  while (P < 8 && modes * P < (long)CHL_MIN_BLOCKS * 32 && Ny >= 4 * P) P *= 2;
+  return P;
+}
 // x-z points per thread of the DSM plane sums (k_dsm_final): 4, halved
 // while the instance's Ny x chunks grid would have fewer blocks than SMs.
 // (Each block ends in a shared-memory reduction tree, so cutting finer than

@@ -315,6 +315,124 @@ k_tri_staged(ChlMap map) {
   }
 }
 
+// Lane-split form, for instances with few modes: chl_tri_lanes(modes, Ny) =
+// P lanes per mode (P = 1 for the larger instances of the same launch).
+// Lane p owns rows [p L, (p+1) L), L = ceil(Ny / P).  Forward, the
+// elimination y_j = iv_j d_j - m_j y_{j-1} maps the value entering a lane's
+// rows affinely to the value leaving them: A y_in + B, A the product of the
+// -m_j.  Each lane forms (A, B) from y_in = 0, an inclusive scan of these
+// maps over the P lanes (warp shuffles within the lane group) gives every
+// lane its y_in, and the lane reruns its rows from it, storing them.  The
+// back substitution x_j = y_j - c_j x_{j+1} (c = 0 on the last row) is split
+// the same way from the top.  With P = 1 the arithmetic is k_tri's; with
+// P > 1 the scan rounds differently from the serial sweep (the multipliers
+// are below 1 in magnitude, so the maps are contractions).  Every lane of a
+// warp reaches the shuffles: a lane group belongs to one mode, and lanes
+// past the last mode carry no rows.
+// Rows of a lane are streamed TB at a time, their loads issued ahead of the
+// serial arithmetic as in k_tri.
+#define TSB 8
+__global__ void __launch_bounds__(128)
+k_tri_scan(ChlMap map) {
+  chl_pdl_wait();
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Ny = I.Ny;
+  const long modes = (long)I.Nz * I.Nxh;
+  const int P = chl_tri_lanes(modes, Ny);
+  const long g = (long)lb * blockDim.x + threadIdx.x;
+  const long mode = g / P;
+  const int p = (int)(g % P);
+  const bool valid = mode < modes;
+  const int L = (Ny + P - 1) / P;
+  const int lo = min(Ny, p * L);
+  const int hi = valid ? min(Ny, lo + L) : lo;      // rows [lo, hi) of this lane
+  const size_t ps = (size_t)modes;                  // row pitch of spec and factors
+  const long mm = valid ? mode : 0;
+  double2* __restrict__ s = I.spec + ps + mm;       // row jc = 1
+  const double* __restrict__ fi = I.tri_inv + mm;
+  const double* __restrict__ fm = I.tri_m + mm;
+  const double* __restrict__ fc = I.tri_c + mm;
+  const unsigned full = 0xffffffffu;
+  // forward sweep over [lo, hi) from `prev`; store = false only forms the
+  // lane's affine map (prev from 0, A the product of the -m_j)
+  auto forward = [&](double2 prev, bool store, double& A) {
+    for (int j0 = lo; j0 < hi; j0 += TSB) {
+      double2 d[TSB]; double iv[TSB], m[TSB];
+#pragma unroll
+      for (int q = 0; q < TSB; ++q) {
+        const int j = j0 + q;
+        if (j < hi) { d[q] = s[(size_t)j * ps]; iv[q] = LDG(fi + (size_t)j * ps); m[q] = LDG(fm + (size_t)j * ps); }
+      }
+#pragma unroll
+      for (int q = 0; q < TSB; ++q) {
+        const int j = j0 + q;
+        if (j < hi) {
+          d[q].x = fma(d[q].x, iv[q], -m[q] * prev.x);   // m = 0 on the first row
+          d[q].y = fma(d[q].y, iv[q], -m[q] * prev.y);
+          prev = d[q];
+          if (store) s[(size_t)j * ps] = d[q];
+          else A = -m[q] * A;
+        }
+      }
+    }
+    return prev;
+  };
+  auto backward = [&](double2 prev, bool store, double& A) {
+    for (int j1 = hi - 1; j1 >= lo; j1 -= TSB) {
+      double2 d[TSB]; double c[TSB];
+#pragma unroll
+      for (int q = 0; q < TSB; ++q) {
+        const int j = j1 - q;
+        if (j >= lo) { d[q] = s[(size_t)j * ps]; c[q] = LDG(fc + (size_t)j * ps); }
+      }
+#pragma unroll
+      for (int q = 0; q < TSB; ++q) {
+        const int j = j1 - q;
+        if (j >= lo) {
+          d[q].x = fma(-c[q], prev.x, d[q].x);        // c = 0 on the last row
+          d[q].y = fma(-c[q], prev.y, d[q].y);
+          prev = d[q];
+          if (store) s[(size_t)j * ps] = d[q];
+          else A = -c[q] * A;
+        }
+      }
+    }
+    return prev;
+  };
+  // ---- forward elimination
+  double2 yin = make_double2(0.0, 0.0);
+  if (P > 1) {
+    double A = 1.0;
+    double2 z = forward(make_double2(0.0, 0.0), false, A);
+    for (int off = 1; off < P; off <<= 1) {
+      const double Ao = __shfl_up_sync(full, A, off, P);
+      const double bx = __shfl_up_sync(full, z.x, off, P), by = __shfl_up_sync(full, z.y, off, P);
+      if (p >= off) { z.x = fma(A, bx, z.x); z.y = fma(A, by, z.y); A *= Ao; }
+    }
+    yin.x = __shfl_up_sync(full, z.x, 1, P);
+    yin.y = __shfl_up_sync(full, z.y, 1, P);
+    if (p == 0) yin = make_double2(0.0, 0.0);
+  }
+  double unused = 1.0;
+  forward(yin, true, unused);
+  // ---- back substitution from the top
+  double2 xin = make_double2(0.0, 0.0);   // x of the row above the lane's rows
+  if (P > 1) {
+    double A = 1.0;
+    double2 w = backward(make_double2(0.0, 0.0), false, A);
+    for (int off = 1; off < P; off <<= 1) {
+      const double Ao = __shfl_down_sync(full, A, off, P);
+      const double bx = __shfl_down_sync(full, w.x, off, P), by = __shfl_down_sync(full, w.y, off, P);
+      if (p + off < P) { w.x = fma(A, bx, w.x); w.y = fma(A, by, w.y); A *= Ao; }
+    }
+    xin.x = __shfl_down_sync(full, w.x, 1, P);
+    xin.y = __shfl_down_sync(full, w.y, 1, P);
+    if (p == P - 1) xin = make_double2(0.0, 0.0);
+  }
+  backward(xin, true, unused);
+}
+
 // ------------------------------------------------------------ inverse x -> pressure field
 __global__ void __launch_bounds__(256)
 k_fftx_inv(ChlMap map, int dst, int xmb) {
@@ -470,6 +588,7 @@ size_t chl_smem_tri(int maxNy, long modes, int mode) {
   return blocks <= per_sm * CHL_SMS ? b : 0;
 }
 int chl_tri_modes_per_block(size_t smem) { return smem ? TRI_W : 128; }
+void chl_launch_tri_scan(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_tri_scan, dim3(nb), dim3(128), 0, st, m); }
 void chl_launch_fftx_inv(const ChlMap& m, int nb, int nt, size_t smem, int dst, int xmb, cudaStream_t st) { chl_launch_pdl(k_fftx_inv, dim3(nb), dim3(nt), smem, st, m, dst, xmb); }
 void chl_launch_project(const ChlMap& m, int nb, int s, cudaStream_t st) { chl_launch_pdl(k_project, dim3(nb), dim3(m.tb), 0, st, m, s); }
 void chl_launch_pbc(const ChlMap& m, int nb, int s, cudaStream_t st) { k_pbc<<<nb, 256, 0, st>>>(m, s); }

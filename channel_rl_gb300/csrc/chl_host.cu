@@ -38,6 +38,7 @@ int chl_tri_modes_per_block(size_t);
 void chl_launch_div_fftx(const ChlMap&, int, int, size_t, int, int, int, cudaStream_t);
 void chl_launch_fftz(const ChlMap&, int, int, size_t, int, int, cudaStream_t);
 void chl_launch_tri(const ChlMap&, int, size_t, cudaStream_t);
+void chl_launch_tri_scan(const ChlMap&, int, cudaStream_t);
 void chl_launch_fftx_inv(const ChlMap&, int, int, size_t, int, int, cudaStream_t);
 void chl_launch_project(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_pbc(const ChlMap&, int, int, cudaStream_t);
@@ -221,6 +222,7 @@ struct chl_handle {
   // z transforms and the tridiagonal form (chl_smem_tri's mode)
   int x_min_blocks = CHL_FFT_MIN_BLOCKS, z_min_blocks = CHL_FFT_MIN_BLOCKS, tri_mode = 2;
   int tb_pt = 256;                    // threads per block of the point maps (stencils, updates)
+  bool tri_scan = false;              // some instance splits its tridiagonal columns (chl_tri_lanes)
   int LES_model = 0, wall_model = 0, any_mass = 0;
   float* d_mlp_theta = nullptr;       // learned wall model parameters (shared)
   unsigned int* d_mlp_cfg = nullptr;  // sigma, train, seed lo/hi, evaluation counter
@@ -413,7 +415,9 @@ static int build_maps(chl_handle* h) {
     const int nrow = I.c.Ny * (I.c.Nz / 2);
     h->tx = std::max(h->tx, chl_fft_threads(chl_fftx_rows(I.c.Nx, nrow, h->x_min_blocks), I.c.Nx));
   }
-  h->smem_t = chl_smem_tri(my, modes, h->tri_mode);
+  h->tri_scan = false;
+  for (auto& I : h->in) h->tri_scan = h->tri_scan || chl_tri_lanes((long)I.c.Nz * I.c.Nxh, I.c.Ny) > 1;
+  h->smem_t = h->tri_scan ? 0 : chl_smem_tri(my, modes, h->tri_mode);
   const int tri_w = chl_tri_modes_per_block(h->smem_t);
   for (int m = 0; m < NMAP; ++m) {
     std::vector<int> off(n + 1, 0);
@@ -430,7 +434,8 @@ static int build_maps(chl_handle* h) {
         case M_PLANE: b = cdiv((long)Nx * Nz, 256); break;
         case M_FFTX: b = cdiv((long)Ny * (Nz / 2), chl_fftx_rows(Nx, Ny * (Nz / 2), h->x_min_blocks)); break;
         case M_FFTZ: b = cdiv((long)Ny * Nxh, h->zcw); break;
-        case M_TRI: b = cdiv((long)Nz * Nxh, tri_w); break;
+        case M_TRI: b = h->tri_scan ? cdiv((long)Nz * Nxh * chl_tri_lanes((long)Nz * Nxh, Ny), 128)
+                                    : cdiv((long)Nz * Nxh, tri_w); break;
         case M_MINABS: b = Nz * ((Ny + 15) / 16); break;   // planes x 16-row chunks (chl_misc.cu)
         case M_ROWS: b = Ny + 1; break;
         case M_MLP: b = cdiv(2L * Nx * Nz, 128); break;
@@ -503,7 +508,8 @@ static int enqueue_projection(chl_handle* h, int s, int mode) {
   if (mode == 2) mode = 0;
   KL("div_fft_x", chl_launch_div_fftx(h->map(M_FFTX), h->nblk[M_FFTX], h->tx, h->smem_x, s, mode, h->x_min_blocks, st));
   KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->tz, h->smem_z, 0, h->zcw, st));
-  KL("tridiag", chl_launch_tri(h->map(M_TRI), h->nblk[M_TRI], h->smem_t, st));
+  if (h->tri_scan) KL("tridiag", chl_launch_tri_scan(h->map(M_TRI), h->nblk[M_TRI], st));
+  else KL("tridiag", chl_launch_tri(h->map(M_TRI), h->nblk[M_TRI], h->smem_t, st));
   KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->tz, h->smem_z, 1, h->zcw, st));
   KL("ifft_x", chl_launch_fftx_inv(h->map(M_FFTX), h->nblk[M_FFTX], h->tx, h->smem_x, mode == 0 ? 0 : 1, h->x_min_blocks, st));
   if (correct) KL("project", chl_launch_project(h->map(M_PT), h->nblk[M_PT], s, st));
@@ -1059,7 +1065,7 @@ int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
     int my = 0;
     long modes = 0;
     for (auto& I : h->in) { my = std::max(my, I.c.Ny); modes += (long)I.c.Nz * I.c.Nxh; }
-    const bool fits = chl_smem_tri(my, modes, 1) > 0;
+    const bool fits = !h->tri_scan && chl_smem_tri(my, modes, 1) > 0;
     int best_v = 0;
     double best_t = 1e30;
     for (int v = 0; v <= (fits ? 1 : 0); ++v) {
@@ -1068,7 +1074,8 @@ int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
       if (t < best_t) { best_t = t; best_v = v; }
     }
     h->tri_mode = best_v;
-    std::snprintf(buf, sizeof buf, " tridiag %s (%.4f ms)", best_v == 1 ? "staged" : "row-batched", best_t);
+    std::snprintf(buf, sizeof buf, " tridiag %s (%.4f ms)",
+                  h->tri_scan ? "lane-split" : (best_v == 1 ? "staged" : "row-batched"), best_t);
     rep += buf;
   }
   if ((rc2 = build_maps(h))) return rc2;
@@ -1087,7 +1094,7 @@ int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
 int chl_get_tile_shapes(chl_handle* h, int* out7) {
   if (!h || !out7) return CHL_E_ARG;
   out7[0] = h->x_min_blocks; out7[1] = h->z_min_blocks; out7[2] = h->tri_mode; out7[3] = h->tb_pt;
-  out7[4] = h->zcw; out7[5] = h->smem_t ? 1 : 0; out7[6] = h->tx;
+  out7[4] = h->zcw; out7[5] = h->tri_scan ? 2 : (h->smem_t ? 1 : 0); out7[6] = h->tx;
   return CHL_OK;
 }
 

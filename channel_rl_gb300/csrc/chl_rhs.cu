@@ -136,7 +136,7 @@ k_rhs_update(ChlMap map, RhsArgs a) {
   double Fu = (LDG(G[G_UX] + cidx(I, ip, jc, k)) - LDG(G[G_UX] + c)) * rxf;
   Fu = fma(LDG(G[G_UY] + e) - LDG(G[G_UY] + em), ryc, Fu);
   Fu = fma(LDG(G[G_UZ] + c) - LDG(G[G_UZ] + cidx(I, i, jc, km)), rzc, Fu);
-  Fu += 4.0 * I.scal[CHL_S_DPDX];   // the fluxes, so F, are 4 x
+  Fu = fma(4.0, I.scal[CHL_S_DPDX], Fu);   // the fluxes, so F, are 4 x (4 dPdx is exact)
   // w at (x-centre i, row jc, z-face k)
   double Fw = (LDG(G[G_WX] + c) - LDG(G[G_WX] + cidx(I, im, jc, k))) * rxc;
   Fw = fma(LDG(G[G_WY] + e) - LDG(G[G_WY] + em), ryc, Fw);
@@ -154,20 +154,23 @@ k_rhs_update(ChlMap map, RhsArgs a) {
     if (hasv) I.Fp[1][e] = 0.25 * Fv;
     return;
   }
+  // out = base + dt (c1 F1 + c2 F) as two FMAs per component, dt folded
+  // into the coefficients once per thread
   const double dt = I.scal[CHL_S_DT];
+  const double dc1 = dt * a.c1, dc2 = dt * a.c2;
   double* Uo = I.U[a.sout]; double* Vo = I.V[a.sout]; double* Wo = I.W[a.sout];
   const double* Ub = I.U[a.sbase]; const double* Vb = I.V[a.sbase]; const double* Wb = I.W[a.sbase];
   double un, vn = 0.0, wn;
   if (a.mode == 0) {
     I.F1[0][c] = Fu; I.F1[2][c] = Fw;
     if (hasv) I.F1[1][e] = Fv;
-    un = Ub[c] + dt * (a.c2 * Fu);
-    wn = Wb[c] + dt * (a.c2 * Fw);
-    if (hasv) vn = Vb[e] + dt * (a.c2 * Fv);
+    un = fma(dc2, Fu, Ub[c]);
+    wn = fma(dc2, Fw, Wb[c]);
+    if (hasv) vn = fma(dc2, Fv, Vb[e]);
   } else {
-    un = Ub[c] + dt * fma(a.c1, I.F1[0][c], a.c2 * Fu);
-    wn = Wb[c] + dt * fma(a.c1, I.F1[2][c], a.c2 * Fw);
-    if (hasv) vn = Vb[e] + dt * fma(a.c1, I.F1[1][e], a.c2 * Fv);
+    un = fma(dc1, I.F1[0][c], fma(dc2, Fu, Ub[c]));
+    wn = fma(dc1, I.F1[2][c], fma(dc2, Fw, Wb[c]));
+    if (hasv) vn = fma(dc1, I.F1[1][e], fma(dc2, Fv, Vb[e]));
   }
   Uo[c] = un; Wo[c] = wn;
   if (hasv) Vo[e] = vn;

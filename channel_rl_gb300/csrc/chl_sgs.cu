@@ -245,7 +245,7 @@ k_dsm_final(ChlMap map) {
     double mo = M4 * M4; mo = fma(M5, M5, mo); mo = fma(M6, M6, mo);
     double lmp = fma(0.25, lo, ld), mmp = fma(0.03125, mo, md);
     // duplicated periodic column i=2 and plane k=2 of the reference's sums
-    const double wgt = (i == 0 ? 2.0 : 1.0) * (k == 0 ? 2.0 : 1.0);
+    const double wgt = i == 0 ? (k == 0 ? 4.0 : 2.0) : (k == 0 ? 2.0 : 1.0);
     lm = fma(wgt, lmp, lm);
     mm = fma(wgt, mmp, mm);
   }

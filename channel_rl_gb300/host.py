@@ -465,10 +465,11 @@ class Channel:
         return buf.value.decode()
 
     def tile_shapes(self):
-        """{x_min_blocks, z_min_blocks, tri_mode, point_threads, z_cols, tri_staged, x_threads}."""
+        """{x_min_blocks, z_min_blocks, tri_mode, point_threads, z_cols, tri_form, x_threads};
+        tri_form 0 row-batched, 1 staged, 2 lane-split."""
         v = (C.c_int * 7)()
         self._check(self.lib.chl_get_tile_shapes(self.h, v), "chl_get_tile_shapes")
-        keys = ("x_min_blocks", "z_min_blocks", "tri_mode", "point_threads", "z_cols", "tri_staged", "x_threads")
+        keys = ("x_min_blocks", "z_min_blocks", "tri_mode", "point_threads", "z_cols", "tri_form", "x_threads")
         return dict(zip(keys, (int(x) for x in v)))
 
     def set_tile_shapes(self, x_min_blocks, z_min_blocks, tri_mode, point_threads=256):

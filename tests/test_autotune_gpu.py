@@ -74,7 +74,7 @@ def test_tuned_and_forced_shapes_are_bit_identical(name):
             for f in ("U", "V", "W", "P", "nu_t", "wm_nut"):
                 assert np.array_equal(out[q][f], ref[q][f]), (key, info, q, f)
     # the forced shapes did change the partition
-    assert runs[FORCED[0]][1]["tri_staged"] == 0 and runs[FORCED[0]][1]["point_threads"] == 64
+    assert runs[FORCED[0]][1]["tri_form"] != 1 and runs[FORCED[0]][1]["point_threads"] == 64
     assert runs[FORCED[0]][1]["z_cols"] >= runs[FORCED[2]][1]["z_cols"]
     out, info, report = runs["tuned"]
     assert "point_threads" in report and "x_min_blocks" in report and "tridiag" in report
