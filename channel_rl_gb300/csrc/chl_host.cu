@@ -969,26 +969,25 @@ static int enqueue_stencils(chl_handle* h) {
   return CHL_OK;
 }
 
-static int time_group(chl_handle* h, int group, int reps, double* ms) {
+// events a, b: created by the caller, which also destroys them
+static int time_group(chl_handle* h, int group, int reps, cudaEvent_t a, cudaEvent_t b, double* ms) {
   int rc = build_maps(h);
   if (rc) return rc;
   auto run = [&]() { return group == 0 ? enqueue_stencils(h) : enqueue_projection(h, 0, 2); };
-  cudaEvent_t a, b;
-  CK(cudaEventCreate(&a)); CK(cudaEventCreate(&b));
   double best = 1e30;
   for (int trial = 0; trial < 3; ++trial) {           // best of three trials
-    if ((rc = run())) break;                          // warm (and first-touch) outside the timing
+    if ((rc = run())) return rc;                      // warm (and first-touch) outside the timing
     CK(cudaEventRecord(a, h->st));
     for (int r = 0; r < reps && !rc; ++r) rc = run();
+    if (rc) return rc;
     CK(cudaEventRecord(b, h->st));
     CK(cudaEventSynchronize(b));
     float f = 0.f;
     CK(cudaEventElapsedTime(&f, a, b));
     best = std::min(best, (double)f / reps);
   }
-  cudaEventDestroy(a); cudaEventDestroy(b);
   *ms = best;
-  return rc;
+  return CHL_OK;
 }
 
 int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
@@ -998,20 +997,12 @@ int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
   // chl_compute_wall_model rebuilds nu_t from) and the row coefficients of
   // every instance, restored at the end
   std::vector<double*> saved;
+  cudaEvent_t ea = nullptr, eb = nullptr;
   auto ncent = [](const Inst& I) { return (size_t)I.c.Nx * (I.c.Ny + 2) * I.c.Nz; };   // centre-field length
   auto ncoef = [](const Inst& I) { return (size_t)I.c.Ny + 2; };
-  for (auto& I : h->in) {
-    const size_t n = ncent(I);
-    double* s = nullptr;
-    CK(cudaMalloc(&s, 8 * (3 * n + ncoef(I))));
-    saved.push_back(s);
-    CK(cudaMemcpyAsync(s, I.dev.nut, 8 * n, cudaMemcpyDeviceToDevice, h->st));
-    CK(cudaMemcpyAsync(s + n, I.dev.p, 8 * n, cudaMemcpyDeviceToDevice, h->st));
-    CK(cudaMemcpyAsync(s + 2 * n, I.dev.S, 8 * n, cudaMemcpyDeviceToDevice, h->st));
-    CK(cudaMemcpyAsync(s + 3 * n, I.dev.coef, 8 * ncoef(I), cudaMemcpyDeviceToDevice, h->st));
-  }
+  // puts back what was saved (every instance saved so far), frees the copies and events
   auto restore = [&]() {
-    for (size_t q = 0; q < h->in.size(); ++q) {
+    for (size_t q = 0; q < saved.size(); ++q) {
       const Inst& I = h->in[q];
       const size_t n = ncent(I);
       cudaMemcpyAsync(I.dev.nut, saved[q], 8 * n, cudaMemcpyDeviceToDevice, h->st);
@@ -1022,14 +1013,43 @@ int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
     cudaStreamSynchronize(h->st);
     for (double* s : saved) cudaFree(s);
     saved.clear();
+    if (ea) cudaEventDestroy(ea);
+    if (eb) cudaEventDestroy(eb);
   };
+  for (auto& I : h->in) {
+    const size_t n = ncent(I);
+    double* s = nullptr;
+    cudaError_t e = cudaMalloc(&s, 8 * (3 * n + ncoef(I)));
+    if (e == cudaSuccess) {
+      e = cudaMemcpyAsync(s, I.dev.nut, 8 * n, cudaMemcpyDeviceToDevice, h->st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(s + n, I.dev.p, 8 * n, cudaMemcpyDeviceToDevice, h->st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(s + 2 * n, I.dev.S, 8 * n, cudaMemcpyDeviceToDevice, h->st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(s + 3 * n, I.dev.coef, 8 * ncoef(I), cudaMemcpyDeviceToDevice, h->st);
+      if (e != cudaSuccess) cudaFree(s);
+      else saved.push_back(s);
+    }
+    if (e != cudaSuccess) {
+      restore();
+      h->err = std::string("CUDA: ") + cudaGetErrorString(e) + " saving state for the tuner";
+      return CHL_E_CUDA;
+    }
+  }
+  {
+    cudaError_t e = cudaEventCreate(&ea);
+    if (e == cudaSuccess) e = cudaEventCreate(&eb);
+    if (e != cudaSuccess) {
+      restore();
+      h->err = std::string("CUDA: ") + cudaGetErrorString(e);
+      return CHL_E_CUDA;
+    }
+  }
   rc = [&]() -> int {
   static const int targets[] = {1, CHL_SMS, 2 * CHL_SMS, 4 * CHL_SMS, 8 * CHL_SMS, 16 * CHL_SMS};
   std::string rep;
   char buf[160];
   double t = 0.0, t0 = 0.0;
-  int rc2 = time_group(h, 0, reps, &t0);
-  if (!rc2) rc2 = time_group(h, 1, reps, &t);
+  int rc2 = time_group(h, 0, reps, ea, eb, &t0);
+  if (!rc2) rc2 = time_group(h, 1, reps, ea, eb, &t);
   if (rc2) return rc2;
   std::snprintf(buf, sizeof buf, "defaults: stencils %.4f ms, projection %.4f ms;", t0, t);
   rep += buf;
@@ -1039,7 +1059,7 @@ int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
     double best_t = 1e30;
     for (int v : {64, 128, 256}) {
       h->tb_pt = v;
-      if ((rc2 = time_group(h, 0, reps, &t))) return rc2;
+      if ((rc2 = time_group(h, 0, reps, ea, eb, &t))) return rc2;
       if (t < best_t) { best_t = t; best_v = v; }
     }
     h->tb_pt = best_v;
@@ -1053,7 +1073,7 @@ int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
     double best_t = 1e30;
     for (int v : targets) {
       knob = v;
-      if ((rc2 = time_group(h, 1, reps, &t))) return rc2;
+      if ((rc2 = time_group(h, 1, reps, ea, eb, &t))) return rc2;
       if (t < best_t) { best_t = t; best_v = v; }
     }
     knob = best_v;
@@ -1070,7 +1090,7 @@ int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
     double best_t = 1e30;
     for (int v = 0; v <= (fits ? 1 : 0); ++v) {
       h->tri_mode = v;
-      if ((rc2 = time_group(h, 1, reps, &t))) return rc2;
+      if ((rc2 = time_group(h, 1, reps, ea, eb, &t))) return rc2;
       if (t < best_t) { best_t = t; best_v = v; }
     }
     h->tri_mode = best_v;
