@@ -167,8 +167,10 @@ int chl_profile_step(chl_handle* h, int reps, int maxk, char* names, double* ms_
  * summary. */
 int chl_autotune(chl_handle* h, int reps, char* report, int report_len);
 /* The current tile shapes: out7 = {x_min_blocks, z_min_blocks, tri_mode,
- * point_threads, z columns per block, staged tridiagonal in use (0/1),
- * x-transform threads}. */
+ * point_threads, z columns per block, tridiagonal form in use (0
+ * row-batched, 1 staged in shared memory, 2 lane-split for instances with
+ * few modes - chosen from the instances' extents, not tuned), x-transform
+ * threads}. */
 int chl_get_tile_shapes(chl_handle* h, int* out7);
 /* Sets the tile shapes by hand: block-count targets >= 1; tri_mode 0
  * row-batched, 1 staged where it fits, 2 the default rule; point_threads
