@@ -79,6 +79,9 @@ def workload(name):
         return [replace(C.c3_roofline(les=C.LES_DSM), LES_model=C.LES_VREMAN, name="c3_256x96x192_vreman_eqwm")]
     if name == "rl_case":
         return [C.rl_case()]
+    if name == "rl_batch16":
+        # 16 environments of the reference's RL size in one handle, one seed each
+        return [replace(C.rl_case(seed=2000 + q), name=f"rl_env{q}") for q in range(16)]
     if name == "c3_dsm_small":
         return [C.smaller(C.c3_roofline(les=C.LES_DSM), 128, 96, 96)]
     if name == "c1":
