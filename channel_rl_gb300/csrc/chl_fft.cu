@@ -53,13 +53,21 @@ __device__ __forceinline__ void dft_small(double2* v, bool inv) {
   }
 }
 
+// Work items (row, butterfly j) are numbered so that consecutive threads
+// touch neighbouring shared-memory words: j fastest when a row is contiguous
+// (es = 1, the x lines), the row fastest when rows are interleaved (rs = 1,
+// the z columns), which keeps the 16-byte accesses free of bank conflicts.
+// tw is the N-entry twiddle table, staged in shared memory by the caller.
 template <int R>
 __device__ void stockham_pass(const double2* __restrict__ x, double2* __restrict__ y, int nrows, int rs, int es,
                               int N, int Ns, const double2* __restrict__ tw, bool inv) {
   const int nb = N / R;
   const int tstep = N / (Ns * R);
+  const bool rowfast = rs < es;
   for (int w = threadIdx.x; w < nrows * nb; w += blockDim.x) {
-    const int row = w / nb, j = w - row * nb;
+    int row, j;
+    if (rowfast) { j = w / nrows; row = w - j * nrows; }
+    else { row = w / nb; j = w - row * nb; }
     const double2* xr = x + (size_t)row * rs;
     double2* yr = y + (size_t)row * rs;
     const int jm = j % Ns;
@@ -69,7 +77,7 @@ __device__ void stockham_pass(const double2* __restrict__ x, double2* __restrict
     if (Ns > 1) {
 #pragma unroll
       for (int r = 1; r < R; ++r) {
-        double2 t = LDG(tw + jm * r * tstep);
+        double2 t = tw[jm * r * tstep];
         if (inv) t.y = -t.y;
         v[r] = cmul(v[r], t);
       }
@@ -81,7 +89,14 @@ __device__ void stockham_pass(const double2* __restrict__ x, double2* __restrict
   }
 }
 
-// Full transform; returns the buffer holding the result (a or b).
+// Copies the N-entry twiddle table into shared memory; the first barrier of
+// fft_smem orders it before any use.
+__device__ __forceinline__ void stage_twiddles(double2* tws, const double2* __restrict__ tw, int N) {
+  for (int w = threadIdx.x; w < N; w += blockDim.x) tws[w] = LDG(tw + w);
+}
+
+// Full transform; returns the buffer holding the result (a or b).  tw: the
+// twiddle table in shared memory (stage_twiddles).
 __device__ double2* fft_smem(double2* a, double2* b, int nrows, int rs, int es, int N,
                              const double2* tw, bool inv) {
   int Ns = 1, rem = N;
@@ -115,6 +130,8 @@ k_div_fftx(ChlMap map, int s_in, int mode, int xmb) {
   const int cr_n = min(CR, nrow - g0);
   double2* A = sm;
   double2* B = sm + CR * Nx;
+  double2* T = sm + 2 * CR * Nx;        // twiddles
+  stage_twiddles(T, I.twx, Nx);
   const double *U, *V, *W;
   if (mode == 0) { U = I.U[s_in]; V = I.V[s_in]; W = I.W[s_in]; }
   else { U = I.Fp[0]; V = I.Fp[1]; W = I.Fp[2]; }
@@ -143,7 +160,7 @@ k_div_fftx(ChlMap map, int s_in, int mode, int xmb) {
     }
     A[cr * Nx + i] = make_double2(dv[0], dv[1]);
   }
-  double2* res = fft_smem(A, B, cr_n, Nx, 1, Nx, I.twx, false);
+  double2* res = fft_smem(A, B, cr_n, Nx, 1, Nx, T, false);
   // split the packed spectrum into the two half-spectra (each times 2)
   for (int w = threadIdx.x; w < cr_n * Nxh; w += blockDim.x) {
     const int cr = w / Nxh, kx = w - cr * Nxh;
@@ -180,12 +197,14 @@ k_fftz(ChlMap map, int inv, int zcw) {
   __syncthreads();
   double2* A = sm;
   double2* B = sm + Nz * zcw;
+  double2* T = sm + 2 * Nz * zcw;       // twiddles
+  stage_twiddles(T, I.twz, Nz);
   double2* spec = I.spec;
   for (int w = threadIdx.x; w < Nz * cw; w += blockDim.x) {
     const int k = w / cw, c = w - k * cw;
     A[k * zcw + c] = spec[coff[c] + (size_t)k * Nxh];
   }
-  double2* res = fft_smem(A, B, cw, 1, zcw, Nz, I.twz, inv != 0);
+  double2* res = fft_smem(A, B, cw, 1, zcw, Nz, T, inv != 0);
   for (int w = threadIdx.x; w < Nz * cw; w += blockDim.x) {
     const int k = w / cw, c = w - k * cw;
     spec[coff[c] + (size_t)k * Nxh] = res[k * zcw + c];
@@ -447,6 +466,8 @@ k_fftx_inv(ChlMap map, int dst, int xmb) {
   const int cr_n = min(CR, nrow - g0);
   double2* A = sm;
   double2* B = sm + CR * Nx;
+  double2* T = sm + 2 * CR * Nx;        // twiddles
+  stage_twiddles(T, I.twx, Nx);
   for (int w = threadIdx.x; w < cr_n * Nx; w += blockDim.x) {
     const int cr = w / Nx, kx = w - cr * Nx;
     const int g = g0 + cr;
@@ -458,7 +479,7 @@ k_fftx_inv(ChlMap map, int dst, int xmb) {
     A[cr * Nx + kx] = lo ? make_double2(pa.x - pb.y, pa.y + pb.x)
                          : make_double2(pa.x + pb.y, pb.x - pa.y);
   }
-  double2* res = fft_smem(A, B, cr_n, Nx, 1, Nx, I.twx, true);
+  double2* res = fft_smem(A, B, cr_n, Nx, 1, Nx, T, true);
   double* out = dst == 0 ? I.p : I.P;
   for (int w = threadIdx.x; w < cr_n * Nx; w += blockDim.x) {
     const int cr = w / Nx, i = w - cr * Nx;
@@ -546,8 +567,9 @@ __global__ void k_pghost(ChlMap map) {
 }
 
 extern "C" {
-size_t chl_smem_fftx(int Nx, int nrow, int xmb) { return (size_t)2 * chl_fftx_rows(Nx, nrow, xmb) * Nx * sizeof(double2); }
-size_t chl_smem_fftz(int maxNz, int zcw) { return (size_t)2 * maxNz * zcw * sizeof(double2); }
+// two ping-pong tiles plus the twiddle table
+size_t chl_smem_fftx(int Nx, int nrow, int xmb) { return ((size_t)2 * chl_fftx_rows(Nx, nrow, xmb) + 1) * Nx * sizeof(double2); }
+size_t chl_smem_fftz(int maxNz, int zcw) { return ((size_t)2 * zcw + 1) * maxNz * sizeof(double2); }
 // kx columns staged per z-transform block: 16, halved while two Nz x cols
 // complex tiles would exceed the 227 KB a block may use, and halved (down
 // to 2) while the grid over all `ncols` columns would have fewer than
