@@ -58,7 +58,11 @@ k_edges(ChlMap map, int src) {
   }
 }
 
-// Centre strain: diagonal D, 8*S_offdiag O (sum of four edges), |S|.
+// Centre strain: diagonal D, 8*S_offdiag O (sum of four edges), and
+// s = |S|/sqrt(2).  The sqrt(2) never needs forming: nu_t = c |S| where the
+// dynamic model's c comes from L:M / M:M with M linear in |S| and |S^| (so
+// keeping both /sqrt(2) scales c by sqrt(2) and c s = c_true |S|), and the
+// static model's row coefficient carries the sqrt(2) itself (k_coef).
 struct Strain { double d1, d2, d3, o12, o13, o23, s; };
 
 __device__ __forceinline__ Strain centre_strain(const ChlInst& I, const double* U, const double* V,
@@ -78,7 +82,7 @@ __device__ __forceinline__ Strain centre_strain(const ChlInst& I, const double* 
   // |S|^2 = 2 (d.d) + 4 (S12^2+S13^2+S23^2) = 2 (d.d + (o.o)/32)
   double dd = s.d1 * s.d1; dd = fma(s.d2, s.d2, dd); dd = fma(s.d3, s.d3, dd);
   double oo = s.o12 * s.o12; oo = fma(s.o13, s.o13, oo); oo = fma(s.o23, s.o23, oo);
-  s.s = sqrt(2.0 * fma(oo, 0.03125, dd));
+  s.s = sqrt(fma(oo, 0.03125, dd));   // |S| / sqrt(2)
   return s;
 }
 
@@ -224,7 +228,8 @@ k_dsm_final(ChlMap map) {
     const size_t c = cidx(I, i, jc, k);
     const Strain h = centre_strain(I, R[15], R[16], R[17], i, jc, k);  // 216 x filtered strain
     // M_ij / 216: the 216 of the filtered |S| S_ij terms moves into the
-    // strain factor (4/216), and k_coef takes the remaining 1/216
+    // strain factor (4/216); L_ij / 216: the filtered velocities are divided
+    // once, each product is then one FMA; k_coef's constant carries both
     const double s4 = h.s * (4.0 / 216.0);
     const double M1 = fma(s4, h.d1, -LDG(R[9] + c));
     const double M2 = fma(s4, h.d2, -LDG(R[10] + c));
@@ -233,12 +238,13 @@ k_dsm_final(ChlMap map) {
     const double M5 = fma(s4, h.o13, -LDG(R[13] + c));
     const double M6 = fma(s4, h.o23, -LDG(R[14] + c));
     const double fu = LDG(R[0] + c), fv = LDG(R[1] + c), fw = LDG(R[2] + c);
-    const double L1 = fma(216.0, LDG(R[3] + c), -fu * fu);
-    const double L2 = fma(216.0, LDG(R[4] + c), -fv * fv);
-    const double L3 = fma(216.0, LDG(R[5] + c), -fw * fw);
-    const double L4 = fma(216.0, LDG(R[6] + c), -fu * fv);
-    const double L5 = fma(216.0, LDG(R[7] + c), -fu * fw);
-    const double L6 = fma(216.0, LDG(R[8] + c), -fv * fw);
+    const double gu = fu * (1.0 / 216.0), gv = fv * (1.0 / 216.0);
+    const double L1 = fma(-gu, fu, LDG(R[3] + c));
+    const double L2 = fma(-gv, fv, LDG(R[4] + c));
+    const double L3 = fma(-fw * (1.0 / 216.0), fw, LDG(R[5] + c));
+    const double L4 = fma(-gu, fv, LDG(R[6] + c));
+    const double L5 = fma(-gu, fw, LDG(R[7] + c));
+    const double L6 = fma(-gv, fw, LDG(R[8] + c));
     double ld = L1 * M1; ld = fma(L2, M2, ld); ld = fma(L3, M3, ld);
     double lo = L4 * M4; lo = fma(L5, M5, lo); lo = fma(L6, M6, lo);
     double md = M1 * M1; md = fma(M2, M2, md); md = fma(M3, M3, md);
@@ -277,15 +283,16 @@ __global__ void k_coef(ChlMap map) {
           mm += I.part[(size_t)(Ny + 2) * np + (size_t)jc * np + q];
         }
         // -1/2 <LM>/<MM>: the filter and average scales give 1/8 (see the
-        // scaling note above), M is stored / 216, so <LM>/<MM> = 216 lm/mm
-        c = (-0.125 / 216.0) * (lm / mm);
+        // scaling note above); L and M are both stored / 216, so
+        // <LM>/<MM> = lm/mm (times the sqrt(2) that the strain leaves out)
+        c = -0.125 * (lm / mm);
       } else if (I.LES_model == 1) {
         // van Driest: f = 1 - exp(-d/25/(nu/utau)), utau = dPdx^0.5 (subgrid.f90:581-599)
         const double ut = sqrt(I.scal[CHL_S_DPDX]);
         double f = 1.0 - exp(-I.smag_dwall[jc] / 25.0 / (I.nu / ut));
         if (I.Dirichlet_nu_t == 0) f = 1.0;
         const double cd = I.smag_csdelta[jc] * f;   // Cs*Delta_j*f
-        c = cd * cd;
+        c = cd * cd * 1.41421356237309504880;      // (Cs Delta f)^2 |S| with S holding |S|/sqrt(2)
       } else if (I.LES_model >= 3) {
         c = 1.0;                           // AMD, Vreman: S holds nu_t itself (not launched for them)
       }
@@ -303,9 +310,11 @@ __global__ void k_coef(ChlMap map) {
 // left the first step lands right of it, then the iterates decrease).  The
 // start is `guess` (the previous stage's u_tau) when it lies above the
 // laminar estimate, which the root always does.  Convergence is quadratic
-// with relative constant 1/(2 kappa f') < 0.1, so once a correction is below
-// 1e-9 of ut the next one would be below 1e-19: the iteration stops there
-// and the root agrees with a fixed-count solve to rounding.  The log of the
+// with relative constant 1/(2 kappa f') < 0.1 (f' = u+ + 1/kappa > 11 where
+// the log law applies), so once a correction is below 3e-8 of ut the error
+// left after it is below 0.09 * (3e-8)^2 < 1e-16, under half an ulp: the
+// iteration stops there and the root agrees with a fixed-count solve to
+// rounding.  The log of the
 // branch test is reused as the first iterate's when the start is laminar.
 // FP64 is the scarce pipe here: h/nu is formed once, 1/kappa is a constant
 // multiplier, and each iteration holds one log and one division.
@@ -327,7 +336,7 @@ __device__ double eqlog_tau(double u, double h, double nu, double guess) {
       const double g = fma(lg, inv_k, EQWM_B);          // u+ at ut
       const double d = fma(ut, g, -au) / (g + inv_k);   // f / f'
       ut = ut - d;
-      if (fabs(d) <= 1e-9 * ut) break;
+      if (fabs(d) <= 3e-8 * ut) break;
     }
   }
   const double tau = ut * ut;
