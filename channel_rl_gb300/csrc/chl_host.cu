@@ -125,6 +125,15 @@ int make_consts(const chl_grid_desc& d, Consts& c, std::string& err) {
   for (int i = 2; i <= c.nx; ++i) if (!(c.xf[i] > c.xf[i - 1])) { err = "grid: x not increasing"; return CHL_E_ARG; }
   for (int i = 2; i <= c.ny; ++i) if (!(c.yf[i] > c.yf[i - 1])) { err = "grid: y not increasing"; return CHL_E_ARG; }
   for (int i = 2; i <= c.nz; ++i) if (!(c.zf[i] > c.zf[i - 1])) { err = "grid: z not increasing"; return CHL_E_ARG; }
+  // The Fourier solve's modified wavenumbers (initialization.f90:296-308)
+  // take one spacing per periodic direction, as the reference's do: x and z
+  // must be uniform (to rounding).
+  auto uniform = [](const std::vector<double>& f, int n) {
+    const double d0 = (f[n] - f[1]) / (n - 1);
+    for (int i = 2; i <= n; ++i) if (std::fabs((f[i] - f[i - 1]) - d0) > 1e-9 * d0) return false;
+    return true;
+  };
+  if (!uniform(c.xf, c.nx) || !uniform(c.zf, c.nz)) { err = "grid: x and z must be uniformly spaced"; return CHL_E_ARG; }
   centres(c.xf, c.nx, c.xg); centres(c.yf, c.ny, c.yg); centres(c.zf, c.nz, c.zg);
   auto dmin = [](const std::vector<double>& g, int n) {
     double m = INFINITY; for (int i = 2; i <= n; ++i) m = std::min(m, g[i] - g[i - 1]); return m; };

@@ -34,7 +34,8 @@ namespace {
 // two pairs: s?L/s?H are the two-point sums on the near/far edge in the
 // derivative direction (2 x the reference's first interpolation), s = sL+sH
 // (4 x the centre value) and d = rl sL + rr sH (4 x the centre derivative,
-// the edge differences divided by their centre-to-centre spacings first).
+// the edge differences divided by their centre-to-centre spacings first;
+// along the uniform x and z that is r (sL + sH)).
 // The centre strain of compute_Sij (subgrid.f90:1014-1072) is the same sums:
 // S12 = (dUy + dVx)/8 from the four edges, etc.
 struct Grad {
@@ -77,9 +78,12 @@ __device__ __forceinline__ Grad gradients(const ChlInst& I, const double* U, con
   g.wxR = (w(ip, jc, km) - wm) + (w(ip, jc, k) - w0);
   g.wyL = (wm - w(i, jc - 1, km)) + (w0 - w(i, jc - 1, k));
   g.wyH = (w(i, jc + 1, km) - wm) + (w(i, jc + 1, k) - w0);
-  g.dUy = fma(ryl, g.uyL, ryr * g.uyH); g.dUz = fma(rzl, g.uzL, rzr * g.uzH);
-  g.dVx = fma(rxl, g.vxL, rxr * g.vxR); g.dVz = fma(rzl, g.vzL, rzr * g.vzH);
-  g.dWx = fma(rxl, g.wxL, rxr * g.wxR); g.dWy = fma(ryl, g.wyL, ryr * g.wyH);
+  // y is stretched: each edge pair by its own spacing; x and z are uniform
+  // (checked at creation), so one spacing times the pair sum
+  (void)rxr; (void)rzr;
+  g.dUy = fma(ryl, g.uyL, ryr * g.uyH); g.dUz = rzl * (g.uzL + g.uzH);
+  g.dVx = rxl * (g.vxL + g.vxR); g.dVz = rzl * (g.vzL + g.vzH);
+  g.dWx = rxl * (g.wxL + g.wxR); g.dWy = fma(ryl, g.wyL, ryr * g.wyH);
   return g;
 }
 
@@ -133,20 +137,23 @@ k_amd(ChlMap map, int s_in, int use_wm) {
   // grid-scaled centre differences, 4 x: Yu, Zu, Xv, Zv, Xw, Yw
   const double Yu = g.uyL + g.uyH, Zu = g.uzL + g.uzH, Xv = g.vxL + g.vxR;
   const double Zv = g.vzL + g.vzH, Xw = g.wxL + g.wxR, Yw = g.wyL + g.wyH;
+  // Numerator and denominator are both formed 16 x (their ratio is what
+  // counts), which takes the 1/16 of the 4 x off-diagonal terms out.
   // denominator: sum of squared centre derivatives (the off-diagonal ones are 4 x)
   double q = g.dUy * g.dUy;
   q = fma(g.dUz, g.dUz, q); q = fma(g.dVx, g.dVx, q); q = fma(g.dVz, g.dVz, q);
   q = fma(g.dWx, g.dWx, q); q = fma(g.dWy, g.dWy, q);
   double D = s11 * s11; D = fma(s22, s22, D); D = fma(s33, s33, D);
-  D = fma(0.0625, q, D);
+  D = fma(16.0, D, q);                                   // 16 x
   // numerator: sum_k (d^_k u_i)(d^_k u_j) S_ij with the reference's product
   // forms; the third mixed term of each S_ij is the edge product averaged.
-  const double a11 = fma(0.0625, fma(Yu, Yu, Zu * Zu), g.dux * g.dux);
-  const double a22 = fma(0.0625, fma(Xv, Xv, Zv * Zv), g.dvy * g.dvy);
-  const double a33 = fma(0.0625, fma(Xw, Xw, Yw * Yw), g.dwz * g.dwz);
-  const double a12 = fma(0.0625, fma(Xv, g.dux, Yu * g.dvy), 0.03125 * fma(g.uzL, g.vzL, g.uzH * g.vzH));
-  const double a13 = fma(0.0625, fma(Xw, g.dux, Zu * g.dwz), 0.03125 * fma(g.uyL, g.wyL, g.uyH * g.wyH));
-  const double a23 = fma(0.0625, fma(Yw, g.dvy, Zv * g.dwz), 0.03125 * fma(g.vxL, g.wxL, g.vxR * g.wxR));
+  const double u4 = 4.0 * g.dux, v4 = 4.0 * g.dvy, w4 = 4.0 * g.dwz;
+  const double a11 = fma(u4, u4, fma(Yu, Yu, Zu * Zu));   // 16 x
+  const double a22 = fma(v4, v4, fma(Xv, Xv, Zv * Zv));
+  const double a33 = fma(w4, w4, fma(Xw, Xw, Yw * Yw));
+  const double a12 = fma(0.5, fma(g.uzL, g.vzL, g.uzH * g.vzH), fma(Xv, g.dux, Yu * g.dvy));
+  const double a13 = fma(0.5, fma(g.uyL, g.wyL, g.uyH * g.wyH), fma(Xw, g.dux, Zu * g.dwz));
+  const double a23 = fma(0.5, fma(g.vxL, g.wxL, g.vxR * g.wxR), fma(Yw, g.dvy, Zv * g.dwz));
   double N = a11 * s11;
   N = fma(a22, s22, N); N = fma(a33, s33, N);
   N = fma(a12, t12, N); N = fma(a13, t13, N); N = fma(a23, t23, N);

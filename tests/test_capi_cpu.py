@@ -76,6 +76,24 @@ def test_fft_length_rule(lib):
     assert rc == 1 and "2^a 3^b" in msg
 
 
+@pytest.mark.parametrize("axis", ["x", "z"])
+def test_nonuniform_periodic_spacing_rejected(lib, axis):
+    """The Fourier solve assumes uniform x and z (one spacing in the modified
+    wavenumbers, as the reference's initialisation); a stretched periodic
+    axis is refused at creation rather than solved wrongly."""
+    case = CS.c1_small()
+    keep = []
+    d = grid_desc(case, keep)
+    a = np.array(getattr(keep[0], axis), dtype=np.float64)
+    a[3] += 0.1 * (a[4] - a[3])          # one face moved off the uniform mesh
+    keep.append(a)
+    setattr(d, axis, a.ctypes.data_as(C.POINTER(C.c_double)))
+    h = C.c_void_p()
+    rc = lib.chl_create(C.byref(d), C.byref(h))
+    assert rc == 1 and "uniformly spaced" in lib.chl_last_error(h).decode()
+    lib.chl_destroy(h)
+
+
 def test_decreasing_coordinates_rejected(lib):
     case = CS.c1_small()
     keep = []
