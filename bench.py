@@ -47,10 +47,11 @@ UNIT = "grid-point-steps/s"
 KERNEL_BYTES = {
     "rhs_flux": 8 * 13.0,        # U, V, W, nu+nu_t in; 9 face fluxes out
     "rhs_update": 8 * 18.0,      # 9 fluxes + 3 base (+3 F1) in; 3 (+3 F1) out
-    "filter_y": 8 * 36.0, "filter_x": 8 * 36.0, "filter_z": 8 * 36.0,   # 18 components in + out
-    "centre_strain": 8 * 22.0,   # U,V,W + 3 edge fields in, |S| + 15 filter inputs out
+    # 15 components in + out (the 3 centre velocities on the wall rows only)
+    "filter_y": 8 * 30.0, "filter_x": 8 * 30.0, "filter_z": 8 * 30.0,
+    "centre_strain": 8 * 19.0,   # U,V,W + 3 edge fields in, |S| + 12 filter inputs out
     "edges": 8 * 6.0,
-    "dsm_LM_MM": 8 * 21.0,
+    "dsm_LM_MM": 8 * 18.0,       # 12 filtered centre fields, 3 filtered faces, 3 edge fields
     "nut": 8 * 2.0,
     "div_fft_x": 8 * 4.0,        # U,V,W in, half spectrum out
     "fft_z": 8 * 2.0,

@@ -65,13 +65,26 @@ k_edges(ChlMap map, int src) {
 // static model's row coefficient carries the sqrt(2) itself (k_coef).
 struct Strain { double d1, d2, d3, o12, o13, o23, s; };
 
-__device__ __forceinline__ Strain centre_strain(const ChlInst& I, const double* U, const double* V,
-                                                const double* W, int i, int jc, int k) {
+// The six face velocities around centre (i, jc, k): u0 = U(i-1), u1 = U(i),
+// v0 = V(jc-1), v1 = V(jc), w0 = W(k-1), w1 = W(k).
+struct Faces { double u0, u1, v0, v1, w0, w1; };
+
+__device__ __forceinline__ Faces centre_faces(const ChlInst& I, const double* U, const double* V,
+                                              const double* W, int i, int jc, int k) {
+  const int im = wrap(i - 1, I.Nx), km = wrap(k - 1, I.Nz);
+  Faces f;
+  f.u0 = LDG(U + cidx(I, im, jc, k)); f.u1 = LDG(U + cidx(I, i, jc, k));
+  f.v0 = LDG(V + vidx(I, i, jc - 1, k)); f.v1 = LDG(V + vidx(I, i, jc, k));
+  f.w0 = LDG(W + cidx(I, i, jc, km)); f.w1 = LDG(W + cidx(I, i, jc, k));
+  return f;
+}
+
+__device__ __forceinline__ Strain centre_strain(const ChlInst& I, const Faces& f, int i, int jc, int k) {
   const int im = wrap(i - 1, I.Nx), km = wrap(k - 1, I.Nz);
   Strain s;
-  s.d1 = (LDG(U + cidx(I, i, jc, k)) - LDG(U + cidx(I, im, jc, k))) * LDG(I.rdxc + i);
-  s.d2 = (LDG(V + vidx(I, i, jc, k)) - LDG(V + vidx(I, i, jc - 1, k))) * LDG(I.rdyc + jc);
-  s.d3 = (LDG(W + cidx(I, i, jc, k)) - LDG(W + cidx(I, i, jc, km))) * LDG(I.rdzc + k);
+  s.d1 = (f.u1 - f.u0) * LDG(I.rdxc + i);
+  s.d2 = (f.v1 - f.v0) * LDG(I.rdyc + jc);
+  s.d3 = (f.w1 - f.w0) * LDG(I.rdzc + k);
   const double* E12 = I.E[0]; const double* E13 = I.E[1]; const double* E23 = I.E[2];
   s.o12 = (LDG(E12 + vidx(I, im, jc - 1, k)) + LDG(E12 + vidx(I, i, jc - 1, k)))
         + (LDG(E12 + vidx(I, im, jc, k)) + LDG(E12 + vidx(I, i, jc, k)));
@@ -88,6 +101,12 @@ __device__ __forceinline__ Strain centre_strain(const ChlInst& I, const double* 
 
 // Raw strain and the DSM filter inputs at centres (rows 1..Ny):
 // q0..2 = 2*(centre velocities), q3..8 = their products, q9..14 = |S|*(d, o).
+// q0..2 are stored only in the two rows next to each wall: the filter is
+// linear and shift-invariant, so away from the walls the filtered centre
+// velocity is the centre average of the filtered face velocity (k_dsm_final
+// forms it there); only rows 1 and Ny, where the centre filter takes its
+// one-sided rule and the face filter does not, need the centre velocity
+// filtered in its own right.
 __global__ void __launch_bounds__(256)
 k_centre(ChlMap map, int s_in, int dsm) {
   chl_pdl_wait();
@@ -99,16 +118,13 @@ k_centre(ChlMap map, int s_in, int dsm) {
   const int i = (int)(t % Nx);
   const int jc = 1 + (int)((t / Nx) % Ny);
   const int k = (int)(t / ((long)Nx * Ny));
-  const double *U = I.U[s_in], *V = I.V[s_in], *W = I.W[s_in];
-  const Strain s = centre_strain(I, U, V, W, i, jc, k);
+  const Faces f = centre_faces(I, I.U[s_in], I.V[s_in], I.W[s_in], i, jc, k);
+  const Strain s = centre_strain(I, f, i, jc, k);
   const size_t c = cidx(I, i, jc, k);
   I.S[c] = s.s;
   if (!dsm) return;
-  const int im = wrap(i - 1, Nx), km = wrap(k - 1, Nz);
-  const double uc = LDG(U + cidx(I, im, jc, k)) + LDG(U + c);
-  const double vc = LDG(V + vidx(I, i, jc - 1, k)) + LDG(V + vidx(I, i, jc, k));
-  const double wc = LDG(W + cidx(I, i, jc, km)) + LDG(W + c);
-  I.q[0][c] = uc; I.q[1][c] = vc; I.q[2][c] = wc;
+  const double uc = f.u0 + f.u1, vc = f.v0 + f.v1, wc = f.w0 + f.w1;
+  if (jc <= 2 || jc >= Ny - 1) { I.q[0][c] = uc; I.q[1][c] = vc; I.q[2][c] = wc; }
   I.q[3][c] = uc * uc; I.q[4][c] = vc * vc; I.q[5][c] = wc * wc;
   I.q[6][c] = uc * vc; I.q[7][c] = uc * wc; I.q[8][c] = vc * wc;
   I.q[9][c] = s.s * s.d1; I.q[10][c] = s.s * s.d2; I.q[11][c] = s.s * s.d3;
@@ -128,6 +144,31 @@ __device__ __forceinline__ double fy(const double* f, size_t c, size_t pitch, in
   return fma(4.0, LDG(f + c), LDG(f + lo) + LDG(f + hi));
 }
 
+// N components from N0 on: out = in(lo) + 4 in(c) + in(hi).  All loads are
+// issued before the stores: the stores may alias the loads as far as the
+// compiler knows, so this is what keeps enough loads in flight.
+template <int N0, int N>
+__device__ __forceinline__ void filter_group(double* const* in, double* const* out, size_t c, size_t lo,
+                                             size_t hi) {
+  double a[N], b[N], d[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    const double* f = in[N0 + q];
+    a[q] = LDG(f + c); b[q] = LDG(f + lo); d[q] = LDG(f + hi);
+  }
+#pragma unroll
+  for (int q = 0; q < N; ++q) out[N0 + q][c] = fma(4.0, a[q], b[q] + d[q]);
+}
+
+// The centre components: products and |S| S (3..14) on every row, the centre
+// velocities (0..2) on the wall rows 1 and Ny only (see k_centre).
+__device__ __forceinline__ void filter_centre(double* const* in, double* const* out, size_t c, size_t lo,
+                                              size_t hi, bool wall_row) {
+  filter_group<3, 6>(in, out, c, lo, hi);
+  filter_group<9, 6>(in, out, c, lo, hi);
+  if (wall_row) filter_group<0, 3>(in, out, c, lo, hi);
+}
+
 __global__ void __launch_bounds__(256)
 k_filter_y(ChlMap map, int s_in) {
   chl_pdl_wait();
@@ -142,21 +183,8 @@ k_filter_y(ChlMap map, int s_in) {
   const size_t c = cidx(I, i, j, k);
   const size_t pc = (size_t)Nx;
   if (j >= 1 && j <= Ny) {
-    // loads of five components are issued before their stores: the stores
-    // may alias the loads as far as the compiler knows, so this is what keeps
-    // enough loads in flight
     const size_t lo = (j == 1) ? c + pc : c - pc, hi = (j == Ny) ? c - pc : c + pc;
-#pragma unroll
-    for (int m0 = 0; m0 < 15; m0 += 5) {
-      double a[5], b[5], d[5];
-#pragma unroll
-      for (int q = 0; q < 5; ++q) {
-        const double* f = I.q[m0 + q];
-        a[q] = LDG(f + c); b[q] = LDG(f + lo); d[q] = LDG(f + hi);
-      }
-#pragma unroll
-      for (int q = 0; q < 5; ++q) I.r[m0 + q][c] = fma(4.0, a[q], b[q] + d[q]);
-    }
+    filter_centre(I.q, I.r, c, lo, hi, j == 1 || j == Ny);
   }
   I.r[15][c] = fy(I.U[s_in], c, pc, j, 0, Ny + 1);
   I.r[17][c] = fy(I.W[s_in], c, pc, j, 0, Ny + 1);
@@ -184,19 +212,7 @@ k_filter_xz(ChlMap map, int from_r) {
   const int im = DIR == 0 ? wrap(i - 1, Nx) : i, ip = DIR == 0 ? wrap(i + 1, Nx) : i;
   const int km = DIR == 1 ? wrap(k - 1, Nz) : k, kp = DIR == 1 ? wrap(k + 1, Nz) : k;
   const size_t c = cidx(I, i, j, k), cm = cidx(I, im, j, km), cp = cidx(I, ip, j, kp);
-  if (j >= 1 && j <= Ny) {
-#pragma unroll
-    for (int m0 = 0; m0 < 15; m0 += 5) {       // five components' loads in flight (see k_filter_y)
-      double a[5], b[5], d[5];
-#pragma unroll
-      for (int q = 0; q < 5; ++q) {
-        const double* f = in[m0 + q];
-        a[q] = LDG(f + c); b[q] = LDG(f + cm); d[q] = LDG(f + cp);
-      }
-#pragma unroll
-      for (int q = 0; q < 5; ++q) out[m0 + q][c] = fma(4.0, a[q], b[q] + d[q]);
-    }
-  }
+  if (j >= 1 && j <= Ny) filter_centre(in, out, c, cm, cp, j == 1 || j == Ny);
   out[15][c] = fma(4.0, LDG(in[15] + c), LDG(in[15] + cm) + LDG(in[15] + cp));
   out[17][c] = fma(4.0, LDG(in[17] + c), LDG(in[17] + cm) + LDG(in[17] + cp));
   if (j <= Ny) {
@@ -226,7 +242,8 @@ k_dsm_final(ChlMap map) {
     if (pidx >= plane) break;
     const int i = pidx % Nx, k = pidx / Nx;
     const size_t c = cidx(I, i, jc, k);
-    const Strain h = centre_strain(I, R[15], R[16], R[17], i, jc, k);  // 216 x filtered strain
+    const Faces f = centre_faces(I, R[15], R[16], R[17], i, jc, k);    // 216 x filtered faces
+    const Strain h = centre_strain(I, f, i, jc, k);                     // 216 x filtered strain
     // M_ij / 216: the 216 of the filtered |S| S_ij terms moves into the
     // strain factor (4/216); L_ij / 216: the filtered velocities are divided
     // once, each product is then one FMA; k_coef's constant carries both
@@ -237,7 +254,12 @@ k_dsm_final(ChlMap map) {
     const double M4 = fma(s4, h.o12, -LDG(R[12] + c));
     const double M5 = fma(s4, h.o13, -LDG(R[13] + c));
     const double M6 = fma(s4, h.o23, -LDG(R[14] + c));
-    const double fu = LDG(R[0] + c), fv = LDG(R[1] + c), fw = LDG(R[2] + c);
+    // 2 x 216 x filtered centre velocities: filtered in their own right on
+    // the wall rows, the centre average of the filtered faces elsewhere
+    const bool wall_row = jc == 1 || jc == Ny;
+    const double fu = wall_row ? LDG(R[0] + c) : f.u0 + f.u1;
+    const double fv = wall_row ? LDG(R[1] + c) : f.v0 + f.v1;
+    const double fw = wall_row ? LDG(R[2] + c) : f.w0 + f.w1;
     const double gu = fu * (1.0 / 216.0), gv = fv * (1.0 / 216.0);
     const double L1 = fma(-gu, fu, LDG(R[3] + c));
     const double L2 = fma(-gv, fv, LDG(R[4] + c));
