@@ -87,8 +87,10 @@ struct ChlInst {
   const double *rdxc, *rdxf, *rdyc, *rdyf, *rdzc, *rdzf;
   const double *dxf, *dyf, *dzf;  // raw spacings (dt)
   const double *hx2, *hy2, *hz2;  // squared centre widths (x(i)-x(i-1))^2 etc. (Vreman)
-  const double *w0x2, *w1x2;      // 2 x weight_y_0/1 by face row jv (the flux kernel's scale)
-  const double *rdxc4, *rdyc4, *rdzc4;   // 4 x rdxc, rdyc, rdzc
+  const double *w0x2, *w1x2;      // 2 x weight_y_0/1 by face row jv
+  const double *w0, *w1;          // weight_y_0/1 by face row jv (w1 = 1 - w0)
+  const double *rdxc4, *rdyc4, *rdzc4;   // 4 x rdxc, rdyc, rdzc (centre fluxes, kept 4 x)
+  const double *rdxc2, *rdyc2, *rdzc2;   // 2 x rdxc, rdyc, rdzc (xy and yz edge fluxes, kept 2 x)
   const double *ygc;              // yg(1..nyg), centre y coordinates with the ghost rows
   const double *smag_csdelta;     // Cs*Delta_j by centre row (static Smagorinsky)
   const double *smag_dwall;       // distance of centre row to the nearer wall (van Driest)

@@ -275,6 +275,8 @@ static int upload_consts(chl_handle* h, Inst& I) {
   size_t o_hx2 = A.take(8 * (Nx + 3)), o_hz2 = A.take(8 * (Nz + 3)), o_hy2 = A.take(8 * (Ny + 2));
   size_t o_w0 = A.take(8 * (Ny + 2)), o_w1 = A.take(8 * (Ny + 2)), o_ygc = A.take(8 * (Ny + 2));
   size_t o_rdxc4 = A.take(8 * (Nx + 3)), o_rdyc4 = A.take(8 * (Ny + 2)), o_rdzc4 = A.take(8 * (Nz + 3));
+  size_t o_rdxc2 = A.take(8 * (Nx + 3)), o_rdyc2 = A.take(8 * (Ny + 2)), o_rdzc2 = A.take(8 * (Nz + 3));
+  size_t o_w0u = A.take(8 * (Ny + 2)), o_w1u = A.take(8 * (Ny + 2));
   size_t o_csd = A.take(8 * (Ny + 2)), o_dw = A.take(8 * (Ny + 2));
   size_t o_twx = A.take(16 * Nx), o_twz = A.take(16 * Nz);
   size_t o_ti = A.take(8 * ntri), o_tm = A.take(8 * ntri), o_tc = A.take(8 * ntri);
@@ -329,6 +331,8 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.hx2 = P(o_hx2) + 1; D.hz2 = P(o_hz2) + 1; D.hy2 = P(o_hy2);
   D.rdyc = P(o_rdyc); D.rdyf = P(o_rdyf); D.dyf = P(o_dyf); D.w0x2 = P(o_w0); D.w1x2 = P(o_w1); D.ygc = P(o_ygc);
   D.rdxc4 = P(o_rdxc4) + 1; D.rdyc4 = P(o_rdyc4); D.rdzc4 = P(o_rdzc4) + 1;
+  D.rdxc2 = P(o_rdxc2) + 1; D.rdyc2 = P(o_rdyc2); D.rdzc2 = P(o_rdzc2) + 1;
+  D.w0 = P(o_w0u); D.w1 = P(o_w1u);
   D.smag_csdelta = P(o_csd); D.smag_dwall = P(o_dw);
   D.twx = (const double2*)(base + o_twx); D.twz = (const double2*)(base + o_twz);
   D.tri_inv = P(o_ti); D.tri_m = P(o_tm); D.tri_c = P(o_tc);
@@ -354,18 +358,21 @@ static int upload_consts(chl_handle* h, Inst& I) {
   CK(put(o_hx2, c.hx2)); CK(put(o_hz2, c.hz2)); CK(put(o_hy2, c.hy2));
   const std::vector<double> ygc(c.yg.begin() + 1, c.yg.begin() + 1 + c.nyg);
   CK(put(o_ygc, ygc));
-  // the flux kernel keeps its face fluxes 4 x (chl_rhs.cu): doubled y
-  // weights and quadrupled centre reciprocals, exact power-of-two scalings
-  // (kept in `scaled` for the rest of this function)
+  // the flux kernel keeps its centre and xz-edge fluxes 4 x and its xy and
+  // yz edge fluxes 2 x (chl_rhs.cu): doubled y weights, quadrupled and
+  // doubled centre reciprocals, exact power-of-two scalings (kept in
+  // `scaled` for the rest of this function)
   std::vector<std::vector<double>> scaled;
   auto times = [&scaled](const std::vector<double>& v, double f) -> const std::vector<double>& {
     scaled.emplace_back(v);
     for (auto& x : scaled.back()) x *= f;
     return scaled.back();
   };
-  scaled.reserve(5);
+  scaled.reserve(8);
   CK(put(o_w0, times(c.w0, 2.0))); CK(put(o_w1, times(c.w1, 2.0)));
+  CK(put(o_w0u, c.w0)); CK(put(o_w1u, c.w1));
   CK(put(o_rdxc4, times(c.rdxc, 4.0))); CK(put(o_rdyc4, times(c.rdyc, 4.0))); CK(put(o_rdzc4, times(c.rdzc, 4.0)));
+  CK(put(o_rdxc2, times(c.rdxc, 2.0))); CK(put(o_rdyc2, times(c.rdyc, 2.0))); CK(put(o_rdzc2, times(c.rdzc, 2.0)));
   CK(put(o_csd, c.csdelta)); CK(put(o_dw, c.dwall));
   const double pi = 4.0 * std::atan(1.0);
   std::vector<double> tw(2 * (size_t)std::max(Nx, Nz));

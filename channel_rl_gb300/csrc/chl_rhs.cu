@@ -22,13 +22,16 @@
 // updates the stage: the FP64 pipe, not HBM, bounds this code, and each
 // flux is computed once instead of twice.
 //
-// The face fluxes are kept 4 x their value: the quarter of the x-z edge
-// averages and of the centre products -(u+u)^2/4 is then never formed, the
-// y weights come doubled (w0x2, w1x2) in place of halved per thread, and the
-// centre reciprocals quadrupled (rdxc4 ...).  The stage update takes the
-// quarter in its RK coefficients.  Scalings by powers of two are exact, so
-// the results are bit-for-bit those of the unscaled form, with 7 fewer FP64
-// instructions per face point.
+// The centre and xz-edge fluxes are kept 4 x their value, the xy and yz
+// edge fluxes 2 x: the quarter of the x-z edge averages and of the centre
+// products -(u+u)^2/4 is then never formed, nor the half of the y-face
+// averages, and the centre reciprocals come quadrupled (rdxc4 ...).  The
+// update takes the edge fluxes' differences with doubled reciprocals
+// (rdxc2 ...), so F is 4 x, and the quarter in its RK coefficients.
+// Scalings by powers of two are exact.  The y-face value of u (and w) is
+// u_a + w1 (u_b - u_a), the weighted average with w0 = 1 - w1, whose
+// difference u_b - u_a is also the face's y derivative: one FMA on top of a
+// difference the viscous flux needs anyway.
 #include "chl_common.cuh"
 
 // flux fields: centre-like (rows 1..Ny): 0 GUx, 1 GVy, 2 GWz, 3 GUz, 4 GWx;
@@ -58,29 +61,22 @@ k_flux(ChlMap map, int sin) {
 #define VV(ii, jj, kk) LDG(V + vidx(I, ii, jj, kk))
 #define NT(ii, jj, kk) LDG(nt + cidx(I, ii, jj, kk))
   const double rxf = LDG(I.rdxf + i), rzf = LDG(I.rdzf + k), ryf = LDG(I.rdyf + j);
-  const double qw0 = LDG(I.w0x2 + j), qw1 = LDG(I.w1x2 + j);   // 2 w0, 2 w1
+  const double w0 = LDG(I.w0 + j), w1 = LDG(I.w1 + j);
   // row j and j+1 values shared by the xy and yz edges (y-face jv = j)
   const double u_a = UC(i, j, k), u_b = UC(i, j + 1, k);
   const double w_a = WC(i, j, k), w_b = WC(i, j + 1, k);
   const double v_0 = VV(i, j, k);
   const double n_a = NT(i, j, k), n_b = NT(i, j + 1, k);
-  {  // xy edge (x-face i, y-face j, z-centre k): uv, nu -> GUy, GVx (all 4 x)
-    const double v_p = VV(ip, j, k);
-    const double uy = fma(qw0, u_a, qw1 * u_b);          // 2 u on the y-face
-    const double uv = uy * (v_0 + v_p);                  // 4 u v (v = 0.5 (v0+vp))
-    const double nxy = fma(qw0, n_a + NT(ip, j, k), qw1 * (n_b + NT(ip, j + 1, k)));
-    const size_t e = vidx(I, i, j, k);
-    G[G_UY][e] = fma(nxy, (u_b - u_a) * ryf, -uv);
-    G[G_VX][e] = fma(nxy, (v_p - v_0) * rxf, -uv);
-  }
-  {  // yz edge (x-centre i, y-face j, z-face k): vw, nu -> GVz, GWy
+  const double nx_a = n_a + NT(ip, j, k);   // x pair of row j: the xy and xz edges share it
+  {  // yz edge (x-centre i, y-face j, z-face k): vw, nu -> GVz, GWy (both 2 x)
     const double v_z = VV(i, j, kp);
-    const double wy = fma(qw0, w_a, qw1 * w_b);
+    const double dw = w_b - w_a;
+    const double wy = fma(w1, dw, w_a);
     const double vw = wy * (v_0 + v_z);
-    const double nyz = fma(qw0, n_a + NT(i, j, kp), qw1 * (n_b + NT(i, j + 1, kp)));
+    const double nyz = fma(w0, n_a + NT(i, j, kp), w1 * (n_b + NT(i, j + 1, kp)));
     const size_t e = vidx(I, i, j, k);
     G[G_VZ][e] = fma(nyz, (v_z - v_0) * rzf, -vw);
-    G[G_WY][e] = fma(nyz, (w_b - w_a) * ryf, -vw);
+    G[G_WY][e] = fma(nyz, dw * ryf, -vw);
   }
   if (j >= 1 && j <= Ny) {
     const int jc = j;
@@ -95,10 +91,20 @@ k_flux(ChlMap map, int sin) {
     {  // xz edge (x-face i, y-centre jc, z-face k): uw, nu -> GUz, GWx (all 4 x)
       const double u_z = UC(i, jc, kp), w_p = WC(ip, jc, k);
       const double uw = (u_a + u_z) * (w_a + w_p);
-      const double nxz = (n_a + NT(ip, jc, k)) + (NT(i, jc, kp) + NT(ip, jc, kp));
+      const double nxz = nx_a + (NT(i, jc, kp) + NT(ip, jc, kp));
       G[G_UZ][c] = fma(nxz, (u_z - u_a) * rzf, -uw);
       G[G_WX][c] = fma(nxz, (w_p - w_a) * rxf, -uw);
     }
+  }
+  {  // xy edge (x-face i, y-face j, z-centre k): uv, nu -> GUy, GVx (both 2 x)
+    const double v_p = VV(ip, j, k);
+    const double du = u_b - u_a;
+    const double uy = fma(w1, du, u_a);                  // u on the y-face
+    const double uv = uy * (v_0 + v_p);                  // 2 u v (v = 0.5 (v0+vp))
+    const double nxy = fma(w0, nx_a, w1 * (n_b + NT(ip, j + 1, k)));   // 2 nu
+    const size_t e = vidx(I, i, j, k);
+    G[G_UY][e] = fma(nxy, du * ryf, -uv);
+    G[G_VX][e] = fma(nxy, (v_p - v_0) * rxf, -uv);
   }
 #undef UC
 #undef WC
@@ -129,25 +135,25 @@ k_rhs_update(ChlMap map, RhsArgs a) {
   const double* const* G = I.G;
   const double rxc = LDG(I.rdxc + i), rxf = LDG(I.rdxf + i);
   const double rzc = LDG(I.rdzc + k), rzf = LDG(I.rdzf + k);
-  const double ryc = LDG(I.rdyc + jc);
+  const double ryc2 = LDG(I.rdyc2 + jc);   // the xy and yz edge fluxes are 2 x, the others 4 x
   const size_t c = cidx(I, i, jc, k);
   const size_t e = vidx(I, i, jc, k), em = vidx(I, i, jc - 1, k);
   // u at (x-face i, row jc, z-centre k)
   double Fu = (LDG(G[G_UX] + cidx(I, ip, jc, k)) - LDG(G[G_UX] + c)) * rxf;
-  Fu = fma(LDG(G[G_UY] + e) - LDG(G[G_UY] + em), ryc, Fu);
+  Fu = fma(LDG(G[G_UY] + e) - LDG(G[G_UY] + em), ryc2, Fu);
   Fu = fma(LDG(G[G_UZ] + c) - LDG(G[G_UZ] + cidx(I, i, jc, km)), rzc, Fu);
   Fu = fma(4.0, I.scal[CHL_S_DPDX], Fu);   // the fluxes, so F, are 4 x (4 dPdx is exact)
   // w at (x-centre i, row jc, z-face k)
   double Fw = (LDG(G[G_WX] + c) - LDG(G[G_WX] + cidx(I, im, jc, k))) * rxc;
-  Fw = fma(LDG(G[G_WY] + e) - LDG(G[G_WY] + em), ryc, Fw);
+  Fw = fma(LDG(G[G_WY] + e) - LDG(G[G_WY] + em), ryc2, Fw);
   Fw = fma(LDG(G[G_WZ] + cidx(I, i, jc, kp)) - LDG(G[G_WZ] + c), rzf, Fw);
   // v at (x-centre i, y-face jv = jc, z-centre k)
   const bool hasv = jc <= Ny - 1;
   double Fv = 0.0;
   if (hasv) {
-    Fv = (LDG(G[G_VX] + e) - LDG(G[G_VX] + vidx(I, im, jc, k))) * rxc;
+    Fv = (LDG(G[G_VX] + e) - LDG(G[G_VX] + vidx(I, im, jc, k))) * LDG(I.rdxc2 + i);
     Fv = fma(LDG(G[G_VY] + cidx(I, i, jc + 1, k)) - LDG(G[G_VY] + c), LDG(I.rdyf + jc), Fv);
-    Fv = fma(LDG(G[G_VZ] + e) - LDG(G[G_VZ] + vidx(I, i, jc, km)), rzc, Fv);
+    Fv = fma(LDG(G[G_VZ] + e) - LDG(G[G_VZ] + vidx(I, i, jc, km)), LDG(I.rdzc2 + k), Fv);
   }
   if (a.mode == 2) {           // actual-pressure RHS: keep F only, at its own scale
     I.Fp[0][c] = 0.25 * Fu; I.Fp[2][c] = 0.25 * Fw;
