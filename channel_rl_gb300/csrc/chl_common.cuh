@@ -127,8 +127,25 @@ struct ChlInst {
 // device scalar slots
 enum {
   CHL_S_DT = 0, CHL_S_T, CHL_S_DPDX, CHL_S_Q0, CHL_S_SHIFT, CHL_S_DIVMAX,
+  CHL_S_DC,            // 6 slots: dt c1 / 4, dt c2 / 4 of RK3 stages 0, 1, 2
   CHL_S_NSCAL = 16
 };
+
+// Stage coefficients of compute_time_step_RK3 (time_integration.f90:42-81):
+// stage s writes U^n + dt (c1 F(U^n) + c2 F(stage input)).
+__host__ __device__ inline double chl_rk_c1(int s) { return s == 0 ? 0.0 : 1.0 / 4.0; }
+__host__ __device__ inline double chl_rk_c2(int s) { return s == 0 ? 8.0 / 15.0 : (s == 1 ? 5.0 / 12.0 : 3.0 / 4.0); }
+
+// Writes dt and the stage products dt c / 4 that the stage update reads
+// (its fluxes are 4 x), so that no grid point forms them.  Every writer of
+// the step size goes through here.
+__host__ __device__ inline void chl_put_dt(double* scal, double dt) {
+  scal[CHL_S_DT] = dt;
+  for (int s = 0; s < 3; ++s) {
+    scal[CHL_S_DC + 2 * s] = dt * (0.25 * chl_rk_c1(s));
+    scal[CHL_S_DC + 2 * s + 1] = dt * (0.25 * chl_rk_c2(s));
+  }
+}
 
 // block -> instance map shared by all multi-instance kernels
 // One field of a three-field layout conversion: the Fortran-layout array

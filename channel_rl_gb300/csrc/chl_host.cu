@@ -16,7 +16,7 @@
 // ------------------------------------------------------------ launchers (other TUs)
 extern "C" {
 void chl_launch_flux(const ChlMap&, int, int, cudaStream_t);
-void chl_launch_update(const ChlMap&, int, int, int, double, double, int, cudaStream_t);
+void chl_launch_update(const ChlMap&, int, int, int, int, int, cudaStream_t);
 void chl_launch_edges(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_centre(const ChlMap&, int, int, int, cudaStream_t);
 void chl_launch_filter_y(const ChlMap&, int, int, cudaStream_t);
@@ -65,7 +65,6 @@ int chl_tc_selftest_launch(const void*, const void*, float*, int, int*, cudaStre
 namespace {
 
 constexpr double RK_T[3] = {8.0 / 15.0, 2.0 / 3.0, 1.0};
-constexpr double RK_C[3][3] = {{8.0 / 15.0, 0.0, 0.0}, {1.0 / 4.0, 5.0 / 12.0, 0.0}, {1.0 / 4.0, 0.0, 3.0 / 4.0}};
 
 enum { M_PT, M_EDGE, M_FULL, M_DSMF, M_WALL, M_PLANE, M_FFTX, M_FFTZ, M_TRI, M_MINABS, M_ROWS, M_MLP, M_WALLN, NMAP };
 constexpr int MLP_NPARAM = 4545;
@@ -549,10 +548,8 @@ static int enqueue_rk3(chl_handle* h) {
   for (int s = 0; s < 3; ++s) {
     int rc = enqueue_sgs(h, sin[s], h->wall_model != CHL_WM_NONE, s);
     if (rc) return rc;
-    const double c1 = s == 0 ? 0.0 : RK_C[s][0];
-    const double c2 = RK_C[s][s];
     KL("rhs_flux", chl_launch_flux(h->map(M_EDGE), h->nblk[M_EDGE], sin[s], h->st));
-    KL("rhs_update", chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, sout[s], c1, c2, s == 0 ? 0 : 1, h->st));
+    KL("rhs_update", chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, sout[s], s, s == 0 ? 0 : 1, h->st));
     LAUNCHED();
     rc = enqueue_projection(h, sout[s], 0);
     if (rc) return rc;
@@ -927,7 +924,7 @@ int chl_set_scalars(chl_handle* h, int inst, const double* in4) {
   CK(cudaMemcpyAsync(s, I->dev.scal, sizeof(s), cudaMemcpyDeviceToHost, h->st));
   int rc = finish(h);
   if (rc) return rc;
-  s[CHL_S_DT] = in4[0]; s[CHL_S_T] = in4[1]; s[CHL_S_DPDX] = in4[2]; s[CHL_S_Q0] = in4[3];
+  chl_put_dt(s, in4[0]); s[CHL_S_T] = in4[1]; s[CHL_S_DPDX] = in4[2]; s[CHL_S_Q0] = in4[3];
   CK(cudaMemcpyAsync(I->dev.scal, s, sizeof(s), cudaMemcpyHostToDevice, h->st));
   return finish(h);
 }
@@ -980,7 +977,7 @@ static int enqueue_stencils(chl_handle* h) {
   int rc = enqueue_sgs(h, 0, false);
   if (rc) return rc;
   chl_launch_flux(h->map(M_EDGE), h->nblk[M_EDGE], 0, h->st);
-  chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, 0, 0.0, 0.0, 2, h->st);
+  chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, 0, 0, 2, h->st);
   LAUNCHED();
   return CHL_OK;
 }
@@ -1172,7 +1169,7 @@ int chl_compute_rhs(chl_handle* h, int inst, double* Fu, double* Fv, double* Fw)
   Inst* I = get_inst(h, inst);
   if (!I) return CHL_E_ARG;
   chl_launch_flux(h->map(M_EDGE), h->nblk[M_EDGE], 0, h->st);
-  chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, 0, 0.0, 0.0, 2, h->st);
+  chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, 0, 0, 2, h->st);
   LAUNCHED();
   const Consts& c = I->c;
   const int Nx = c.Nx, Ny = c.Ny, Nz = c.Nz;
@@ -1215,7 +1212,7 @@ int chl_compute_pressure(chl_handle* h) {
   int rc = check_ready(h); if (rc) return rc;
   chl_launch_pbc(h->map(M_WALL), h->nblk[M_WALL], 0, h->st);
   chl_launch_flux(h->map(M_EDGE), h->nblk[M_EDGE], 0, h->st);
-  chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, 0, 0.0, 0.0, 2, h->st);
+  chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, 0, 0, 2, h->st);
   LAUNCHED();
   rc = enqueue_projection(h, 0, 1); if (rc) return rc;
   chl_launch_pghost(h->map(M_PLANE), h->nblk[M_PLANE], h->st);

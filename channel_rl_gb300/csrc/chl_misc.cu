@@ -205,7 +205,7 @@ k_dt(ChlMap map) {
   chl_pdl_wait();
   const ChlInst& I = map.inst[blockIdx.x];
   if (I.CFL < 0.0) {
-    if (threadIdx.x == 0) I.scal[CHL_S_DT] = -I.CFL;
+    if (threadIdx.x == 0) chl_put_dt(I.scal, -I.CFL);
     return;
   }
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
@@ -234,7 +234,7 @@ k_dt(ChlMap map) {
     const double dt_vis = fmin(fmin(C * I.dxmin * I.dxmin / nu, C * I.dymin * I.dymin / nu), C * I.dzmin * I.dzmin / nu);
     double dt = fmin(dt_conv, dt_vis);
     dt = fmin(dt, 1e-3);
-    I.scal[CHL_S_DT] = dt;
+    chl_put_dt(I.scal, dt);
   }
 }
 

@@ -115,7 +115,7 @@ k_flux(ChlMap map, int sin) {
 
 struct RhsArgs {
   int sbase, sout;        // velocity sets: stage base (U^n), output
-  double c1, c2;          // out = base + dt*(c1*F1 + c2*F), both passed / 4 (F1, F are 4 x)
+  int stage;              // RK3 stage 0..2: out = base + dt (c1 F1 + c2 F) (chl_put_dt's products)
   int mode;               // 0: stage 1 (store F1), 1: stages 2/3, 2: actual-pressure RHS only
 };
 
@@ -160,10 +160,9 @@ k_rhs_update(ChlMap map, RhsArgs a) {
     if (hasv) I.Fp[1][e] = 0.25 * Fv;
     return;
   }
-  // out = base + dt (c1 F1 + c2 F) as two FMAs per component, dt folded
-  // into the coefficients once per thread
-  const double dt = I.scal[CHL_S_DT];
-  const double dc1 = dt * a.c1, dc2 = dt * a.c2;
+  // out = base + dt (c1 F1 + c2 F) as two FMAs per component; the products
+  // dt c / 4 (F1, F are 4 x) are formed once per step where dt is set
+  const double dc1 = I.scal[CHL_S_DC + 2 * a.stage], dc2 = I.scal[CHL_S_DC + 2 * a.stage + 1];
   double* Uo = I.U[a.sout]; double* Vo = I.V[a.sout]; double* Wo = I.W[a.sout];
   const double* Ub = I.U[a.sbase]; const double* Vb = I.V[a.sbase]; const double* Wb = I.W[a.sbase];
   double un, vn = 0.0, wn;
@@ -188,9 +187,8 @@ extern "C" {
 void chl_launch_flux(const ChlMap& map, int nb_edge, int sin, cudaStream_t st) {
   chl_launch_pdl(k_flux, dim3(nb_edge), dim3(map.tb), 0, st, map, sin);
 }
-void chl_launch_update(const ChlMap& map, int nb_pt, int sbase, int sout, double c1, double c2, int mode,
-                       cudaStream_t st) {
-  RhsArgs a{sbase, sout, 0.25 * c1, 0.25 * c2, mode};
+void chl_launch_update(const ChlMap& map, int nb_pt, int sbase, int sout, int stage, int mode, cudaStream_t st) {
+  RhsArgs a{sbase, sout, stage, mode};
   chl_launch_pdl(k_rhs_update, dim3(nb_pt), dim3(map.tb), 0, st, map, a);
 }
 }
