@@ -347,7 +347,7 @@ def run_ours(args):
     roof["step_hbm_gbs_vs_fused_minimum"] = step_bytes / (tmax_ms / args.steps * 1e-3) / 1e9
     # FP64 issue roofline (the binding one on GB300): FP64-pipe instructions
     # per grid point of each kernel from the committed ncu capture, against
-    # the measured DFMA issue rate.
+    # the best measured FP64 issue rate (a DFMA loop on register operands).
     fl = (traffic or {}).get("fp64_instr_per_point", {}).get(args.workload, {})
     peak_gops = fp64.get("fp64_peak_gops") or fp64.get("dfma_gops")
     if peak_gops and dom in fl:
@@ -358,7 +358,8 @@ def run_ours(args):
                         "unit": "G FP64 instr/s", "frac": ach / peak_gops,
                         "step_achieved": step_ach, "step_frac": step_ach / peak_gops,
                         "step_fp64_instr_per_point": step_instr / points,
-                        "peak_source": "measured (profiles/fp64_peak.json, best FP64 issue rate of the probe)"}
+                        "peak_source": "measured (profiles/fp64_peak.json: best FP64 issue rate of the probe, "
+                                       "DFMA on register operands)"}
         roof["binding"] = "fp64"
     # e2e through the C ABI with pinned host buffers
     e2e = None

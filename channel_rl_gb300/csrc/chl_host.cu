@@ -309,6 +309,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.Nx = Nx; D.Ny = Ny; D.Nz = Nz; D.Nxh = Nxh;
   D.LES_model = I.d.LES_model; D.Dirichlet_nu_t = I.d.Dirichlet_nu_t;
   D.wall_model = I.d.wall_model; D.x_mass_cte = I.d.x_mass_cte;
+  D.fk[FK_ONE] = 1.0; D.fk[FK_MZERO] = -0.0; D.fk[FK_FOUR] = 4.0;
   D.nu = I.d.nu; D.CFL = I.d.CFL; D.Cs = I.d.Cs;
   D.dxmin = c.dxmin; D.dymin = c.dymin; D.dzmin = c.dzmin;
   D.dyw = c.yg[2] - c.yg[1];

@@ -138,22 +138,23 @@ k_rhs_update(ChlMap map, RhsArgs a) {
   const double ryc2 = LDG(I.rdyc2 + jc);   // the xy and yz edge fluxes are 2 x, the others 4 x
   const size_t c = cidx(I, i, jc, k);
   const size_t e = vidx(I, i, jc, k), em = vidx(I, i, jc - 1, k);
+  const F64 f = f64_of(I);   // sums, differences, products as register FMAs (bit-identical)
   // u at (x-face i, row jc, z-centre k)
-  double Fu = (LDG(G[G_UX] + cidx(I, ip, jc, k)) - LDG(G[G_UX] + c)) * rxf;
-  Fu = fma(LDG(G[G_UY] + e) - LDG(G[G_UY] + em), ryc2, Fu);
-  Fu = fma(LDG(G[G_UZ] + c) - LDG(G[G_UZ] + cidx(I, i, jc, km)), rzc, Fu);
-  Fu = fma(4.0, I.scal[CHL_S_DPDX], Fu);   // the fluxes, so F, are 4 x (4 dPdx is exact)
+  double Fu = f.mul(f.sub(LDG(G[G_UX] + cidx(I, ip, jc, k)), LDG(G[G_UX] + c)), rxf);
+  Fu = fma(f.sub(LDG(G[G_UY] + e), LDG(G[G_UY] + em)), ryc2, Fu);
+  Fu = fma(f.sub(LDG(G[G_UZ] + c), LDG(G[G_UZ] + cidx(I, i, jc, km))), rzc, Fu);
+  Fu = fma(I.fk[FK_FOUR], I.scal[CHL_S_DPDX], Fu);   // the fluxes, so F, are 4 x (4 dPdx is exact)
   // w at (x-centre i, row jc, z-face k)
-  double Fw = (LDG(G[G_WX] + c) - LDG(G[G_WX] + cidx(I, im, jc, k))) * rxc;
-  Fw = fma(LDG(G[G_WY] + e) - LDG(G[G_WY] + em), ryc2, Fw);
-  Fw = fma(LDG(G[G_WZ] + cidx(I, i, jc, kp)) - LDG(G[G_WZ] + c), rzf, Fw);
+  double Fw = f.mul(f.sub(LDG(G[G_WX] + c), LDG(G[G_WX] + cidx(I, im, jc, k))), rxc);
+  Fw = fma(f.sub(LDG(G[G_WY] + e), LDG(G[G_WY] + em)), ryc2, Fw);
+  Fw = fma(f.sub(LDG(G[G_WZ] + cidx(I, i, jc, kp)), LDG(G[G_WZ] + c)), rzf, Fw);
   // v at (x-centre i, y-face jv = jc, z-centre k)
   const bool hasv = jc <= Ny - 1;
   double Fv = 0.0;
   if (hasv) {
-    Fv = (LDG(G[G_VX] + e) - LDG(G[G_VX] + vidx(I, im, jc, k))) * LDG(I.rdxc2 + i);
-    Fv = fma(LDG(G[G_VY] + cidx(I, i, jc + 1, k)) - LDG(G[G_VY] + c), LDG(I.rdyf + jc), Fv);
-    Fv = fma(LDG(G[G_VZ] + e) - LDG(G[G_VZ] + vidx(I, i, jc, km)), LDG(I.rdzc2 + k), Fv);
+    Fv = f.mul(f.sub(LDG(G[G_VX] + e), LDG(G[G_VX] + vidx(I, im, jc, k))), LDG(I.rdxc2 + i));
+    Fv = fma(f.sub(LDG(G[G_VY] + cidx(I, i, jc + 1, k)), LDG(G[G_VY] + c)), LDG(I.rdyf + jc), Fv);
+    Fv = fma(f.sub(LDG(G[G_VZ] + e), LDG(G[G_VZ] + vidx(I, i, jc, km))), LDG(I.rdzc2 + k), Fv);
   }
   if (a.mode == 2) {           // actual-pressure RHS: keep F only, at its own scale
     I.Fp[0][c] = 0.25 * Fu; I.Fp[2][c] = 0.25 * Fw;

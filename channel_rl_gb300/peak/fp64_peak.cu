@@ -3,13 +3,19 @@
 // and 32 are swept, the loop body unrolled four times) so that the issue
 // rate, not the latency of one chain, is what is measured; the largest rate
 // of the sweep is the peak.  A mixed stream (DFMA, DADD, DMUL in the 2:1:1
-// ratio of the solver's kernels) is measured the same way.
+// ratio of the solver's kernels) is measured the same way.  The operands
+// other than the chain's own value are kernel parameters (constant bank) in
+// the first probes and registers loaded from memory in the "reg" probes,
+// which is how the solver's kernels hold theirs.
 #include <cstdio>
 #include <cuda_runtime.h>
 #define CK(x) do{cudaError_t e=(x); if(e!=cudaSuccess){printf("err %s line %d\n",cudaGetErrorString(e),__LINE__); return 1;}}while(0)
 
 template <int OP, int CH>
-__global__ void kd(double* out, double a, double b, int iters) {
+__global__ void kd(double* out, double a_, double b_, int iters, const double* ab) {
+  // OP >= 10: the same stream with a and b in registers (loaded, so not constants)
+  const double a = OP >= 10 ? ab[0] : a_, b = OP >= 10 ? ab[1] : b_;
+  const double one = ab[2], mzero = ab[3];   // 1.0 and -0.0, unknown to the compiler
   double r[CH];
 #pragma unroll
   for (int c = 0; c < CH; ++c) r[c] = threadIdx.x * 1e-9 + 1.0 + c * 1e-3;
@@ -18,11 +24,16 @@ __global__ void kd(double* out, double a, double b, int iters) {
     for (int u = 0; u < 4; ++u) {
 #pragma unroll
       for (int c = 0; c < CH; ++c) {
-        if (OP == 0) r[c] = fma(r[c], a, b);
-        if (OP == 1) r[c] = r[c] + a;
+        if (OP == 0 || OP == 10) r[c] = fma(r[c], a, b);
+        if (OP == 1 || OP == 11) r[c] = r[c] + a;
+        if (OP == 12) r[c] = r[c] * a;                 // DMUL, register operand
+        if (OP == 13) r[c] = fma(r[c], one, b);        // an addition issued as DFMA (exact: r*1 is r)
+        if (OP == 15) r[c] = fma(r[c], a, mzero);      // a product issued as DFMA (exact: adding -0)
+        if (OP == 16) r[c] = fma(r[c], 0.5, b);        // DFMA with a literal power of two
+        if (OP == 17) r[c] = fma(r[c], 0.999999, b);   // DFMA with a general literal
         if (OP == 2) r[c] = b / r[c];
         if (OP == 3) r[c] = sqrt(r[c] + a);
-        if (OP == 4) {   // mixed: per 4 ops, 2 DFMA, 1 DADD, 1 DMUL
+        if (OP == 4 || OP == 14) {   // mixed: per 4 ops, 2 DFMA, 1 DADD, 1 DMUL
           if ((c & 3) < 2) r[c] = fma(r[c], a, b);
           else if ((c & 3) == 2) r[c] = r[c] + b;
           else r[c] = r[c] * a;
@@ -49,12 +60,13 @@ __global__ void kf(float* out, float a, float b, int iters) {
 }
 
 template <int OP, int CH>
-int run(const char* name, double* d, int nb, int nt, int iters, int sms, int clk, double a, double b, double* best) {
+int run(const char* name, double* d, int nb, int nt, int iters, int sms, int clk, double a, double b, double* best,
+        const double* ab) {
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0); cudaEventCreate(&e1);
   for (int rep = 0; rep < 3; rep++) {
     cudaEventRecord(e0);
-    kd<OP, CH><<<nb, nt>>>(d, a, b, iters);
+    kd<OP, CH><<<nb, nt>>>(d, a, b, iters, ab);
     cudaEventRecord(e1);
     CK(cudaEventSynchronize(e1));
     float ms;
@@ -82,20 +94,36 @@ int main() {
   const int sms = p.multiProcessorCount, nb = sms * 8, nt = 256;
   double* d;
   float* f;
+  double* ab;
   CK(cudaMalloc(&d, nb * nt * 8));
   CK(cudaMalloc(&f, nb * nt * 4));
-  double dfma = 0, dadd = 0, ddiv = 0, dsqrt = 0, mixed = 0;
-  if (run<0, 8>("DFMA", d, nb, nt, 1024, sms, clk, 0.999999, 1e-7, &dfma)) return 1;
-  if (run<0, 16>("DFMA", d, nb, nt, 512, sms, clk, 0.999999, 1e-7, &dfma)) return 1;
-  if (run<0, 32>("DFMA", d, nb, nt, 256, sms, clk, 0.999999, 1e-7, &dfma)) return 1;
-  if (run<1, 8>("DADD", d, nb, nt, 1024, sms, clk, 1e-7, 1e-7, &dadd)) return 1;
-  if (run<1, 16>("DADD", d, nb, nt, 512, sms, clk, 1e-7, 1e-7, &dadd)) return 1;
-  if (run<1, 32>("DADD", d, nb, nt, 256, sms, clk, 1e-7, 1e-7, &dadd)) return 1;
-  if (run<4, 8>("MIXED", d, nb, nt, 1024, sms, clk, 0.999999, 1e-7, &mixed)) return 1;
-  if (run<4, 16>("MIXED", d, nb, nt, 512, sms, clk, 0.999999, 1e-7, &mixed)) return 1;
-  if (run<4, 32>("MIXED", d, nb, nt, 256, sms, clk, 0.999999, 1e-7, &mixed)) return 1;
-  if (run<2, 8>("DDIV", d, nb, nt, 64, sms, clk, 1e-7, 1.0000001, &ddiv)) return 1;
-  if (run<3, 8>("DSQRT", d, nb, nt, 64, sms, clk, 1e-7, 1e-7, &dsqrt)) return 1;
+  CK(cudaMalloc(&ab, 4 * 8));
+  const double hab[4] = {0.999999, 1e-7, 1.0, -0.0};
+  CK(cudaMemcpy(ab, hab, sizeof(hab), cudaMemcpyHostToDevice));
+  double dfma = 0, dadd = 0, ddiv = 0, dsqrt = 0, mixed = 0, regs = 0;
+  if (run<0, 8>("DFMA", d, nb, nt, 1024, sms, clk, 0.999999, 1e-7, &dfma, ab)) return 1;
+  if (run<0, 16>("DFMA", d, nb, nt, 512, sms, clk, 0.999999, 1e-7, &dfma, ab)) return 1;
+  if (run<0, 32>("DFMA", d, nb, nt, 256, sms, clk, 0.999999, 1e-7, &dfma, ab)) return 1;
+  if (run<1, 8>("DADD", d, nb, nt, 1024, sms, clk, 1e-7, 1e-7, &dadd, ab)) return 1;
+  if (run<1, 16>("DADD", d, nb, nt, 512, sms, clk, 1e-7, 1e-7, &dadd, ab)) return 1;
+  if (run<1, 32>("DADD", d, nb, nt, 256, sms, clk, 1e-7, 1e-7, &dadd, ab)) return 1;
+  if (run<4, 8>("MIXED", d, nb, nt, 1024, sms, clk, 0.999999, 1e-7, &mixed, ab)) return 1;
+  if (run<4, 16>("MIXED", d, nb, nt, 512, sms, clk, 0.999999, 1e-7, &mixed, ab)) return 1;
+  if (run<4, 32>("MIXED", d, nb, nt, 256, sms, clk, 0.999999, 1e-7, &mixed, ab)) return 1;
+  if (run<10, 8>("DFMA reg", d, nb, nt, 1024, sms, clk, 0.0, 0.0, &regs, ab)) return 1;
+  if (run<10, 16>("DFMA reg", d, nb, nt, 512, sms, clk, 0.0, 0.0, &regs, ab)) return 1;
+  if (run<10, 32>("DFMA reg", d, nb, nt, 256, sms, clk, 0.0, 0.0, &regs, ab)) return 1;
+  if (run<11, 8>("DADD reg", d, nb, nt, 1024, sms, clk, 0.0, 0.0, &regs, ab)) return 1;
+  if (run<11, 16>("DADD reg", d, nb, nt, 512, sms, clk, 0.0, 0.0, &regs, ab)) return 1;
+  if (run<14, 16>("MIXED reg", d, nb, nt, 512, sms, clk, 0.0, 0.0, &regs, ab)) return 1;
+  double dmulr = 0, addf = 0, mulf = 0, lit2 = 0, litg = 0;
+  if (run<12, 16>("DMUL reg", d, nb, nt, 512, sms, clk, 0.0, 0.0, &dmulr, ab)) return 1;
+  if (run<13, 16>("ADD as DFMA", d, nb, nt, 512, sms, clk, 0.0, 0.0, &addf, ab)) return 1;
+  if (run<15, 16>("MUL as DFMA", d, nb, nt, 512, sms, clk, 0.0, 0.0, &mulf, ab)) return 1;
+  if (run<16, 16>("DFMA literal 0.5", d, nb, nt, 512, sms, clk, 0.0, 0.0, &lit2, ab)) return 1;
+  if (run<17, 16>("DFMA literal 0.999999", d, nb, nt, 512, sms, clk, 0.0, 0.0, &litg, ab)) return 1;
+  if (run<2, 8>("DDIV", d, nb, nt, 64, sms, clk, 1e-7, 1.0000001, &ddiv, ab)) return 1;
+  if (run<3, 8>("DSQRT", d, nb, nt, 64, sms, clk, 1e-7, 1e-7, &dsqrt, ab)) return 1;
   double ffma = 0;
   for (int rep = 0; rep < 3; rep++) {
     cudaEvent_t e0, e1;
@@ -110,7 +138,8 @@ int main() {
     if (rep == 2) { ffma = nops / ms / 1e6; printf("FFMA: %.3f ms, %.1f Gop/s\n", ms, ffma); }
     cudaEventDestroy(e0); cudaEventDestroy(e1);
   }
-  printf("BEST dfma %.3f dadd %.3f mixed %.3f ddiv %.3f dsqrt %.3f ffma %.1f\n", dfma, dadd, mixed, ddiv, dsqrt, ffma);
+  printf("BEST dfma %.3f dadd %.3f mixed %.3f ddiv %.3f dsqrt %.3f ffma %.1f reg %.3f\n", dfma, dadd, mixed, ddiv, dsqrt,
+         ffma, regs);
   CK(cudaGetLastError());
   return 0;
 }
