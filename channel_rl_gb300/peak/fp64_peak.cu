@@ -16,6 +16,11 @@ __global__ void kd(double* out, double a_, double b_, int iters, const double* a
   // OP >= 10: the same stream with a and b in registers (loaded, so not constants)
   const double a = OP >= 10 ? ab[0] : a_, b = OP >= 10 ? ab[1] : b_;
   const double one = ab[2], mzero = ab[3];   // 1.0 and -0.0, unknown to the compiler
+  // OP 18: every DFMA reads three different registers (no operand reuse
+  // between consecutive instructions), as the stencil kernels' FMAs do
+  double x[8], y[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) { x[q] = OP == 18 ? ab[0] + q * 1e-9 : 0.0; y[q] = OP == 18 ? ab[1] * (q + 1) : 0.0; }
   double r[CH];
 #pragma unroll
   for (int c = 0; c < CH; ++c) r[c] = threadIdx.x * 1e-9 + 1.0 + c * 1e-3;
@@ -31,6 +36,7 @@ __global__ void kd(double* out, double a_, double b_, int iters, const double* a
         if (OP == 15) r[c] = fma(r[c], a, mzero);      // a product issued as DFMA (exact: adding -0)
         if (OP == 16) r[c] = fma(r[c], 0.5, b);        // DFMA with a literal power of two
         if (OP == 17) r[c] = fma(r[c], 0.999999, b);   // DFMA with a general literal
+        if (OP == 18) r[c] = fma(x[c & 7], r[c], y[(c + 3) & 7]);   // three distinct registers
         if (OP == 2) r[c] = b / r[c];
         if (OP == 3) r[c] = sqrt(r[c] + a);
         if (OP == 4 || OP == 14) {   // mixed: per 4 ops, 2 DFMA, 1 DADD, 1 DMUL
@@ -122,6 +128,9 @@ int main() {
   if (run<15, 16>("MUL as DFMA", d, nb, nt, 512, sms, clk, 0.0, 0.0, &mulf, ab)) return 1;
   if (run<16, 16>("DFMA literal 0.5", d, nb, nt, 512, sms, clk, 0.0, 0.0, &lit2, ab)) return 1;
   if (run<17, 16>("DFMA literal 0.999999", d, nb, nt, 512, sms, clk, 0.0, 0.0, &litg, ab)) return 1;
+  double distinct = 0;
+  if (run<18, 16>("DFMA 3 distinct regs", d, nb, nt, 512, sms, clk, 0.0, 0.0, &distinct, ab)) return 1;
+  if (run<18, 32>("DFMA 3 distinct regs", d, nb, nt, 256, sms, clk, 0.0, 0.0, &distinct, ab)) return 1;
   if (run<2, 8>("DDIV", d, nb, nt, 64, sms, clk, 1e-7, 1.0000001, &ddiv, ab)) return 1;
   if (run<3, 8>("DSQRT", d, nb, nt, 64, sms, clk, 1e-7, 1e-7, &dsqrt, ab)) return 1;
   double ffma = 0;
