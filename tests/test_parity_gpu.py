@@ -122,6 +122,30 @@ def test_ten_steps_c1_every_field_every_step():
     ch.close()
 
 
+def test_rk3_takes_the_dt_set_from_the_host():
+    """compute_time_step_RK3 without compute_dt uses the step size set through
+    chl_set_scalars (which also forms the stage products dt c / 4 that the
+    update kernel reads): a dt that compute_dt would not produce, two steps,
+    every velocity field within FIELD_RTOL of the oracle's RK3 with that dt."""
+    case = C.c1_small()
+    U, V, W = C.initial_fields(case)
+    o = oracle_for(case)
+    o.set_fields(U, V, W)
+    ch = _channel(case)
+    ch.upload(U, V, W)
+    dt = 0.37 * o.compute_dt()
+    for s in range(2):
+        o.dt = dt
+        ch.set_scalars(dt=dt)
+        o.compute_time_step_RK3()
+        ch.compute_time_step_RK3()
+        d = ch.download(fields=("U", "V", "W"))
+        for f, e in _cmp_fields(d, o).items():
+            assert e < FIELD_RTOL, (s + 1, f, e)
+        assert ch.scalars()["dt"] == dt
+    ch.close()
+
+
 def test_golden_fixtures_on_gpu():
     from tests.golden.make_golden import NSTEP, golden_cases, summarise
     gold = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "golden.npz"))
