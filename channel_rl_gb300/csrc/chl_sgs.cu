@@ -201,8 +201,10 @@ k_filter_y(ChlMap map, int s_in) {
 }
 
 // x or z pass (periodic, weights 1-4-1) over all stored rows of each component.
+// The x pass fits 40 registers without spilling (6 blocks of 256 per SM);
+// the z pass, with its two plane offsets, keeps 48.
 template <int DIR>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(256, DIR == 0 ? 6 : 5)
 k_filter_xz(ChlMap map, int from_r) {
   chl_pdl_wait();
   int lb;
@@ -215,16 +217,29 @@ k_filter_xz(ChlMap map, int from_r) {
   const int k = (int)(t / ((long)Nx * (Ny + 2)));
   double* const* in = from_r ? I.r : I.q;
   double* const* out = from_r ? I.q : I.r;
-  const int im = DIR == 0 ? wrap(i - 1, Nx) : i, ip = DIR == 0 ? wrap(i + 1, Nx) : i;
-  const int km = DIR == 1 ? wrap(k - 1, Nz) : k, kp = DIR == 1 ? wrap(k + 1, Nz) : k;
-  const size_t c = cidx(I, i, j, k), cm = cidx(I, im, j, km), cp = cidx(I, ip, j, kp);
+  // periodic neighbours as offsets from the point (the wrap folded in), the
+  // same along x for the centre-like and V-like layouts; along z their
+  // plane sizes differ
+  long dm, dp, dmv, dpv;
+  if (DIR == 0) {
+    dm = i == 0 ? Nx - 1 : -1;
+    dp = i == Nx - 1 ? 1 - Nx : 1;
+    dmv = dm; dpv = dp;
+  } else {
+    const long pc = (long)Nx * (Ny + 2), pv = (long)Nx * (Ny + 1);
+    dm = k == 0 ? (Nz - 1) * pc : -pc;
+    dp = k == Nz - 1 ? -(Nz - 1) * pc : pc;
+    dmv = k == 0 ? (Nz - 1) * pv : -pv;
+    dpv = k == Nz - 1 ? -(Nz - 1) * pv : pv;
+  }
+  const size_t c = cidx(I, i, j, k), cm = c + dm, cp = c + dp;
   const F64 f = f64_of(I);
   const double four = I.fk[FK_FOUR];
   if (j >= 1 && j <= Ny) filter_centre(in, out, c, cm, cp, j == 1 || j == Ny, f, four);
   out[15][c] = fma(four, LDG(in[15] + c), f.add(LDG(in[15] + cm), LDG(in[15] + cp)));
   out[17][c] = fma(four, LDG(in[17] + c), f.add(LDG(in[17] + cm), LDG(in[17] + cp)));
   if (j <= Ny) {
-    const size_t v = vidx(I, i, j, k), vm = vidx(I, im, j, km), vp = vidx(I, ip, j, kp);
+    const size_t v = vidx(I, i, j, k), vm = v + dmv, vp = v + dpv;
     out[16][v] = fma(four, LDG(in[16] + v), f.add(LDG(in[16] + vm), LDG(in[16] + vp)));
   }
 }
