@@ -107,6 +107,9 @@ int chl_get_scalars(chl_handle* h, int inst, double* out4);
  * CFL pass, bit 2 (4) an out-of-range field index (only the bounds-checked
  * build checks; it clamps the index and records it here).  Cleared by upload. */
 int chl_status_flags(chl_handle* h, int inst, int* flags);
+/* Sets the four scalars of chl_get_scalars.  The dt given here is the one
+ * chl_compute_time_step_RK3 uses until the next chl_compute_dt (the stage
+ * coefficients times dt are formed here too). */
 int chl_set_scalars(chl_handle* h, int inst, const double* in4);
 
 /* compute_dt (time_integration.f90:102-150), all instances. */
