@@ -80,7 +80,7 @@ struct ChlInst {
   int LES_model, Dirichlet_nu_t, wall_model, x_mass_cte;
   double nu, CFL, Cs;
   double dxmin, dymin, dzmin;   // initialization.f90:233-235
-  double dyw;                   // yg(2)-yg(1), used for both walls (wallmodel.f90:448-450)
+  double dyw;                   // yg(2)-yg(1), used for both walls (wallmodel.f90:32-35)
   double hb, ht;                // matching heights of the log-law wall model
   double cbc1, cbc2;            // coef_bc_1*(yg(2)-yg(1)), coef_bc_2*(yg(nyg)-yg(nyg-1))
   double ybot, ytop;            // y(1), y(ny)

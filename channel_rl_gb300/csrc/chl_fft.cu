@@ -1,8 +1,9 @@
 // Fractional-step projection: divergence, 2-D Fourier transform in x and z,
 // one tridiagonal solve in y per wavenumber pair, inverse transform and the
 // velocity correction.  Restates compute_projection_step
-// (projection.f90:20-214) and, for the actual pressure, the solver of
-// compute_pressure (pressure.f90:42-172).
+// (projection.f90:20-214) and, for the actual pressure, the right-hand side
+// and solver that compute_pressure (pressure.f90:21-29) calls
+// (pressure.f90:42-172).
 //
 // The reference transforms each y-plane with FFTW-MPI and calls LAPACK
 // zgtsv per mode.  Here:

@@ -730,7 +730,7 @@ int chl_upload(chl_handle* h, int inst, const double* U, const double* V, const 
   chl_launch_unpack3(f3, I->c.Nx, I->c.Nz, h->st);
   LAUNCHED();
   const int Nz = I->c.Nz;
-  // Qflow_x_0 of this instance (mass_flow.f90:271-309); the kernel runs per instance
+  // Qflow_x_0 of this instance (mass_flow.f90:24-61); the kernel runs per instance
   chl_launch_qflow(h->d_inst + inst, Nz, 0, CHL_S_Q0, h->st);
   LAUNCHED();
   CK(cudaMemsetAsync(I->dev.status, 0, sizeof(int), h->st));

@@ -239,7 +239,7 @@ k_dt(ChlMap map) {
 }
 
 // ------------------------------------------------------------ constant mass flow
-// compute_dPx_for_constant_mass_flow (mass_flow.f90:360-413) over the unique
+// compute_dPx_for_constant_mass_flow (mass_flow.f90:113-166) over the unique
 // x-z points of rows j_f = 3 and nyg-2, then U += dPdx on the interior
 // (time_integration.f90:89-94); one block per instance for the sum.
 __global__ void k_massflow(ChlMap map, int s, int force) {
@@ -323,7 +323,7 @@ __global__ void k_divmax(ChlMap map, int s, double* out) {
 }
 
 // ------------------------------------------------------------ initial bulk flow Qflow_x_0
-// compute_mean_mass_flow_U (mass_flow.f90:271-309), trapezoid over rows
+// compute_mean_mass_flow_U (mass_flow.f90:24-61), trapezoid over rows
 // j_f = 3..nyg-1 of the unique x-z points; one block per instance.
 // one block per z plane: compensated (Kahan) partial sums of the plane
 // into red[2k], red[2k+1]; k_qflow_final adds them in plane order

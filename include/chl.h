@@ -61,7 +61,7 @@ typedef struct {
   double nu;                   /* kinematic viscosity */
   double CFL;                  /* CFL number, or -dt for a fixed step */
   double dPdx;                 /* imposed pressure gradient (x_mass_cte = 0) */
-  int x_mass_cte;              /* 1: constant mass flow (mass_flow.f90:360-413) */
+  int x_mass_cte;              /* 1: constant mass flow (mass_flow.f90:113-166) */
   int LES_model;               /* CHL_LES_* */
   int Dirichlet_nu_t;          /* 1: nu_t ghost = -nu_t (Dirichlet), 0: Neumann; 2 (AMD, Vreman):
                                   -nu_t + 0.38 sqrt(dPdx) (y(2)-y(1)) (subgrid.f90:868-871); DSM and
@@ -127,7 +127,7 @@ int chl_compute_wall_model(chl_handle* h);           /* wallmodel.f90:23-46 (eq.
  * outputs on the unique points: Fu(Nx,Ny,Nz), Fv(Nx,Ny-1,Nz), Fw(Nx,Ny,Nz). */
 int chl_compute_rhs(chl_handle* h, int inst, double* Fu, double* Fv, double* Fw);
 int chl_compute_projection_step(chl_handle* h);      /* projection.f90:20-28 */
-int chl_compute_dPx_for_constant_mass_flow(chl_handle* h, int inst, double* dPdx); /* mass_flow.f90:360-413 */
+int chl_compute_dPx_for_constant_mass_flow(chl_handle* h, int inst, double* dPdx); /* mass_flow.f90:113-166 */
 int chl_compute_pressure(chl_handle* h);             /* pressure.f90:21-29 */
 int chl_check_divergence(chl_handle* h, int inst, double* max_div, double* max_abs_div); /* projection.f90:223-245 */
 int chl_stats(chl_handle* h, int inst, chl_stats_out* out);  /* statistics.f90:22-145 */

@@ -24,10 +24,10 @@ Known reference quirks reproduced on purpose (each is a switchable oracle
 mode where the reference itself cannot run it):
 * compute_dt takes max(dx/|u|) (time_integration.f90:117-119);
 * the constant-mass-flow control averages planes j=3 and nyg-2 only and
-  shifts U by the difference (mass_flow.f90:382-411, time_integration.f90:89-94);
+  shifts U by the difference (mass_flow.f90:135-155, time_integration.f90:89-94);
 * the wall model overwrites nu_t in rows 1,2,nyg-1,nyg and uses yg(2)-yg(1)
-  for both walls (wallmodel.f90:447-457); its x interpolation writes centres
-  2..nx (one past the section, wallmodel.f90:452);
+  for both walls (wallmodel.f90:32-42); its x interpolation writes centres
+  2..nx (one past the section, wallmodel.f90:37);
 * x/z interpolation ignores ``di`` (interpolation.f90:24-40, 88-105); the
   viscous y flux of u and w uses the un-interpolated dU/dy (equations.f90:115,417);
 * the 00 Fourier mode is pinned by D(2)*=3/2 (projection.f90:107);
