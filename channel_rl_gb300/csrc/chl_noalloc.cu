@@ -22,25 +22,29 @@
 // the GPU (different streams, or different host threads on one device)
 // race on it and must be serialised by the caller.
 //
-// Set-up: host code cannot use the array's name as a device address (it is
-// a host-side stand-in), so the first call on each device looks the address
-// up with cudaGetSymbolAddress with that device current and keeps it.  That
-// first call on a device should come before any stream capture.
+// Address lookup: host code cannot use the array's name as a device
+// address (it is a host-side stand-in), so every call asks the CUDA runtime
+// for the array's address with cudaGetSymbolAddress in the context current
+// on the calling thread.  The array sits at a different address in each
+// context the library's kernels are loaded into (a context the caller made
+// with the driver API, or the primary context after a device reset), so an
+// address kept from an earlier call could point outside the current one.
+// The call is a host-side table lookup once the module is loaded.
+//
+// Stream capture: a call copies its two results to pageable host memory and
+// synchronises `stream`, so it cannot be made while any stream is being
+// captured.
 #include "../../include/chl.h"
 
 #include <cuda_runtime.h>
-#include <mutex>
 #include <cstring>
 
 #define CHL_NOALLOC_MAX_PLANES 4096
-#define CHL_NOALLOC_MAX_DEVICES 64
 
 static __device__ __align__(256) double chl_noalloc_scratch[2 * CHL_NOALLOC_MAX_PLANES + 2];
 
 namespace {
 
-std::mutex g_mu;
-double* g_scratch[CHL_NOALLOC_MAX_DEVICES] = {};
 thread_local char g_err[256] = "";
 
 void set_err(const char* m) { std::strncpy(g_err, m, sizeof(g_err) - 1); g_err[sizeof(g_err) - 1] = 0; }
@@ -126,32 +130,33 @@ int chl_check_divergence_noalloc(const double* U, const double* V, const double*
     set_err("chl_check_divergence_noalloc: nz - 1 exceeds the 4096 z planes its fixed scratch holds");
     return CHL_E_ARG;
   }
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= CHL_NOALLOC_MAX_DEVICES) {
-    set_err("chl_check_divergence_noalloc: no usable current CUDA device");
+  void* sym = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&sym, chl_noalloc_scratch);
+  if (e != cudaSuccess || !sym) {
+    set_err("chl_check_divergence_noalloc: cudaGetSymbolAddress of the scratch array failed (no usable CUDA context?)");
     return CHL_E_CUDA;
   }
-  double* scratch = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch[dev]) {
-      void* p = nullptr;
-      cudaError_t e = cudaGetSymbolAddress(&p, chl_noalloc_scratch);
-      if (e != cudaSuccess || !p) {
-        set_err("chl_check_divergence_noalloc: cudaGetSymbolAddress of the scratch array failed");
-        return CHL_E_CUDA;
-      }
-      g_scratch[dev] = (double*)p;
-    }
-    scratch = g_scratch[dev];
-  }
+  double* scratch = static_cast<double*>(sym);
   cudaStream_t st = (cudaStream_t)stream;
-  k_div_planes<<<nplanes, 256, 0, st>>>(U, V, W, x, y, z, nx, ny, nz, scratch);
-  k_div_final<<<1, 256, 0, st>>>(scratch, nplanes);
+  // cudaLaunchKernel returns this launch's own status, so an error that an
+  // unrelated earlier call left pending is neither reported here nor cleared
+  {
+    void* a[] = {(void*)&U, (void*)&V, (void*)&W, (void*)&x, (void*)&y, (void*)&z,
+                 (void*)&nx, (void*)&ny, (void*)&nz, (void*)&scratch};
+    e = cudaLaunchKernel((const void*)k_div_planes, dim3(nplanes), dim3(256), a, 0, st);
+  }
+  if (e == cudaSuccess) {
+    int np = nplanes;
+    void* a[] = {(void*)&scratch, (void*)&np};
+    e = cudaLaunchKernel((const void*)k_div_final, dim3(1), dim3(256), a, 0, st);
+  }
+  if (e != cudaSuccess) {
+    set_err(cudaGetErrorString(e));
+    return CHL_E_CUDA;
+  }
   double r[2];
-  cudaError_t e = cudaMemcpyAsync(r, scratch + 2 * CHL_NOALLOC_MAX_PLANES, sizeof(r), cudaMemcpyDeviceToHost, st);
+  e = cudaMemcpyAsync(r, scratch + 2 * CHL_NOALLOC_MAX_PLANES, sizeof(r), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_err(cudaGetErrorString(e));
     return CHL_E_CUDA;

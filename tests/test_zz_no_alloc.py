@@ -8,6 +8,9 @@ partials in a fixed 64 KiB device array shared by every call.  This file is
 collected last so that a failure here comes after every other test has run.
 """
 import ctypes as C
+import os
+import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -72,3 +75,87 @@ def test_noalloc_divergence_matches_handle_version_twice(lib):
         else:
             assert ref[1] < 1e-12          # after a projected step
     ch.close()
+
+
+# Run in a child process: it drives contexts through the driver API, which
+# must not disturb the test process's own CUDA context.
+_CONTEXTS = r"""
+import ctypes as C, sys
+from dataclasses import replace
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from channel_rl_gb300 import cases as CS
+from channel_rl_gb300.host import load
+
+lib = load(build_if_missing=False)
+f = lib.chl_check_divergence_noalloc
+F64P = C.POINTER(C.c_double)
+f.argtypes = [C.c_void_p] * 6 + [C.c_int, C.c_int, C.c_int, C.c_void_p, F64P, F64P]
+f.restype = C.c_int
+lib.chl_noalloc_last_error.restype = C.c_char_p
+cu = C.CDLL("libcuda.so.1")
+
+def ck(r, what):
+    if r != 0:
+        raise SystemExit(f"{what}: CUresult {r}")
+
+def expected(U, V, W, x, y, z):
+    # centres i = 2..nxg-1, j = 2..nyg-1, k = 2..nzg-1 (Fortran), 0-based here
+    d = ((U[1:, 1:-1, 1:-1] - U[:-1, 1:-1, 1:-1]) / np.diff(x)[:, None, None]
+         + (V[1:-1, 1:, 1:-1] - V[1:-1, :-1, 1:-1]) / np.diff(y)[None, :, None]
+         + (W[1:-1, 1:-1, 1:] - W[1:-1, 1:-1, :-1]) / np.diff(z)[None, None, :])
+    return max(0.0, float(d.max())), float(np.abs(d).max())
+
+def call(case, seed):
+    U, V, W = CS.initial_fields(case if seed is None else replace(case, seed=seed))
+    x, y, z = CS.faces(case)
+    ptrs = []
+    for a in (U, V, W, x, y, z):
+        a = np.asfortranarray(a, dtype=np.float64)
+        d = C.c_uint64()
+        ck(cu.cuMemAlloc_v2(C.byref(d), C.c_size_t(a.nbytes)), "cuMemAlloc")
+        ck(cu.cuMemcpyHtoD_v2(d, a.ctypes.data_as(C.c_void_p), C.c_size_t(a.nbytes)), "cuMemcpyHtoD")
+        ptrs.append(d)
+    a, b = C.c_double(), C.c_double()
+    rc = f(*(C.c_void_p(p.value) for p in ptrs), case.nx, case.ny, case.nz, None, C.byref(a), C.byref(b))
+    for p in ptrs:
+        ck(cu.cuMemFree_v2(p), "cuMemFree")
+    if rc != 0:
+        raise SystemExit(f"noalloc rc {rc}: {lib.chl_noalloc_last_error()}")
+    ref = expected(U, V, W, x, y, z)
+    h = min(np.diff(q).min() for q in (x, y, z))
+    scale = sum(np.abs(q).max() for q in (U, V, W)) * 2.0 / h
+    if abs(a.value - ref[0]) > 1e-12 * scale or abs(b.value - ref[1]) > 1e-12 * scale:
+        raise SystemExit(f"mismatch: {(a.value, b.value)} vs {ref}")
+    return b.value
+
+case = CS.smaller(CS.c2_wm64(), 48, 32, 64)
+ck(cu.cuInit(0), "cuInit")
+dev = C.c_int()
+ck(cu.cuDeviceGet(C.byref(dev), 0), "cuDeviceGet")
+prim = C.c_void_p()
+ck(cu.cuDevicePrimaryCtxRetain(C.byref(prim), dev), "cuDevicePrimaryCtxRetain")
+ck(cu.cuCtxSetCurrent(prim), "cuCtxSetCurrent")
+r1 = call(case, None)                       # primary context
+other = C.c_void_p()
+ck(cu.cuCtxCreate_v2(C.byref(other), 0, dev), "cuCtxCreate")     # now current
+r2 = call(case, 99)                         # a second context: the array has another address there
+ck(cu.cuCtxDestroy_v2(other), "cuCtxDestroy")
+ck(cu.cuCtxSetCurrent(prim), "cuCtxSetCurrent")
+r3 = call(case, 7)                          # back in the primary context, fresh buffers
+ck(cu.cuDevicePrimaryCtxRelease_v2(dev), "cuDevicePrimaryCtxRelease")
+print("ok", r1, r2, r3)
+"""
+
+
+@pytest.mark.gpu
+def test_noalloc_in_a_second_context():
+    """A caller may run the library in a context it created with the driver
+    API.  The scratch array then sits at another address than in the primary
+    context, and each call must find it there: the primary context, a
+    second context with fresh buffers, then the primary context again, each
+    checked against the divergence computed on the host."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", _CONTEXTS, root], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.startswith("ok"), r.stdout
