@@ -120,13 +120,15 @@ struct ChlInst {
   double *coef;                   // nu_t coefficient per centre row [Ny+2]
   double *scal;                   // device scalars (CHL_S_*)
   unsigned long long *minabs;     // [Nx+1 | Nz] min |u| bit patterns (dt)
-  double *red;                    // bulk-flow plane partials [2][Nz] (upload)
+  double *red;                    // plane partials [2][Nz]: bulk flow (upload), divergence check
   int *status;                    // device status word (0 ok)
   // learned wall model (chl_mlp.cu)
   double retau;                   // nominal Re_tau of the instance (feature ln(h Re_tau))
   float *mlp_trace;               // policy-gradient trace of this instance (4545)
   const float *mlp_theta;         // network parameters, shared by the batch (4545)
-  unsigned int *mlp_cfg;          // shared: sigma bits, train, seed lo/hi, evaluation counter
+  unsigned int *mlp_cfg;          // shared: sigma bits, train, seed lo/hi, evaluation counter,
+                                  //   record flag, withheld-commit poll limit (chl_mlp_debug)
+  float *mlp_rec;                 // [3 stages][2 Nx Nz][8] per-point record (chl_mlp_debug), or null
 };
 
 // FP64 issue forms.  In a throughput loop on GB300 an FP64 FMA whose

@@ -53,7 +53,7 @@ void chl_launch_dt(const ChlMap&, cudaStream_t);
 void chl_launch_massflow(const ChlMap&, cudaStream_t, int, int);
 void chl_launch_shift(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_tadvance(const ChlMap&, cudaStream_t);
-void chl_launch_divmax(const ChlMap&, int, double*, cudaStream_t);
+void chl_launch_divmax(const ChlMap&, int, int, double*, cudaStream_t);
 void chl_launch_qflow(const ChlInst*, int, int, int, cudaStream_t);
 void chl_launch_stats(const ChlMap&, int, double*, int, int, cudaStream_t);
 int chl_mlp_setup();
@@ -66,7 +66,8 @@ namespace {
 
 constexpr double RK_T[3] = {8.0 / 15.0, 2.0 / 3.0, 1.0};
 
-enum { M_PT, M_EDGE, M_FULL, M_DSMF, M_WALL, M_PLANE, M_FFTX, M_FFTZ, M_TRI, M_MINABS, M_ROWS, M_MLP, M_WALLN, NMAP };
+enum { M_PT, M_EDGE, M_FULL, M_DSMF, M_WALL, M_PLANE, M_FFTX, M_FFTZ, M_TRI, M_MINABS, M_ROWS, M_MLP, M_WALLN,
+       M_ZPLANE, NMAP };
 constexpr int MLP_NPARAM = 4545;
 
 // Grid constants of one instance (host, FP64), in the device index
@@ -298,6 +299,8 @@ static int upload_consts(chl_handle* h, Inst& I) {
   size_t o_min = A.take(8 * (size_t)(Nx + Ny + 1 + Nz)), o_status = A.take(64);
   size_t o_red = A.take(8 * 2 * (size_t)Nz);
   size_t o_trace = A.take(4 * (size_t)MLP_NPARAM);
+  const bool mlp = I.d.wall_model == CHL_WM_MLP;
+  size_t o_rec = mlp ? A.take(4 * (size_t)CHL_MLP_REC * 3 * 2 * Nx * Nz) : 0;
   I.nstage = (size_t)c.nxg * c.nyg * c.nzg;
   size_t o_stage = A.take(3 * 8 * I.nstage);   // three Fortran-layout fields (chl_set_fields)
   cudaError_t e = cudaMalloc(&I.arena, A.off);
@@ -349,6 +352,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.mlp_trace = (float*)(base + o_trace);
   D.mlp_theta = h->d_mlp_theta;
   D.mlp_cfg = h->d_mlp_cfg;
+  D.mlp_rec = mlp ? (float*)(base + o_rec) : nullptr;
   I.staging = P(o_stage);
   // host constant arrays -> device
   auto put = [&](size_t o, const std::vector<double>& v) { return cudaMemcpyAsync(base + o, v.data(), 8 * v.size(), cudaMemcpyHostToDevice, h->st); };
@@ -456,6 +460,7 @@ static int build_maps(chl_handle* h) {
         case M_ROWS: b = Ny + 1; break;
         case M_MLP: b = cdiv(2L * Nx * Nz, 128); break;
         case M_WALLN: b = cdiv(2L * Nx * Nz, CHL_WALL_THREADS); break;
+        case M_ZPLANE: b = Nz; break;
       }
       off[q + 1] = off[q] + b;
     }
@@ -592,6 +597,23 @@ static int check_finite(chl_handle* h, int inst = -1) {
       h->err = "non-finite velocity in instance " + std::to_string(q) + " (found by compute_dt); re-upload the fields";
       return CHL_E_NAN;
     }
+  }
+  return CHL_OK;
+}
+
+// The learned wall model's bounded tensor-core waits (chl_mlp.cu) set the
+// handle's status word when they run out; the CTA then keeps the
+// equilibrium stress for its points.  Checked at the calls that
+// synchronise, reported once and cleared.
+static int check_mlp(chl_handle* h) {
+  if (h->wall_model != CHL_WM_MLP || !h->d_mlp_status) return CHL_OK;
+  int st = 0;
+  cudaError_t e = cudaMemcpy(&st, h->d_mlp_status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && st) e = cudaMemset(h->d_mlp_status, 0, sizeof(int));
+  if (e != cudaSuccess) { h->err = std::string("CUDA: ") + cudaGetErrorString(e); return CHL_E_CUDA; }
+  if (st) {
+    h->err = "learned wall model: a tensor-core completion wait ran out; those points kept the equilibrium stress";
+    return CHL_E_TIMEOUT;
   }
   return CHL_OK;
 }
@@ -750,7 +772,7 @@ int chl_download(chl_handle* h, int inst, double* U, double* V, double* W, doubl
   Inst* I = get_inst(h, inst);
   if (!I) return CHL_E_ARG;
   int rc0 = finish(h);
-  if (rc0 || (rc0 = check_finite(h, inst))) return rc0;
+  if (rc0 || (rc0 = check_finite(h, inst)) || (rc0 = check_mlp(h))) return rc0;
   const Consts& c = I->c;
   const int Ny = c.Ny;
   int rc = 0;
@@ -1147,7 +1169,8 @@ int chl_set_tile_shapes(chl_handle* h, int x_min_blocks, int z_min_blocks, int t
 int chl_synchronize(chl_handle* h) {
   if (!h) return CHL_E_ARG;
   int rc = finish(h);
-  return rc ? rc : check_finite(h);
+  if (!rc) rc = check_finite(h);
+  return rc ? rc : check_mlp(h);
 }
 
 int chl_compute_eddy_viscosity(chl_handle* h) {
@@ -1224,7 +1247,7 @@ int chl_compute_pressure(chl_handle* h) {
 int chl_check_divergence(chl_handle* h, int inst, double* max_div, double* max_abs_div) {
   int rc = check_ready(h); if (rc) return rc;
   if (!get_inst(h, inst)) return CHL_E_ARG;
-  chl_launch_divmax(h->map(M_PT), 0, h->d_divout, h->st);
+  chl_launch_divmax(h->map(M_ZPLANE), h->nblk[M_ZPLANE], 0, h->d_divout, h->st);
   LAUNCHED();
   double r[2];
   CK(cudaMemcpyAsync(r, h->d_divout + 2 * inst, sizeof(r), cudaMemcpyDeviceToHost, h->st));
@@ -1363,12 +1386,27 @@ int chl_mlp_read_trace(chl_handle* h, int inst, float* trace, int zero_after) {
   if (!I || !trace) return CHL_E_ARG;
   CK(cudaMemcpyAsync(trace, I->dev.mlp_trace, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost, h->st));
   if (zero_after) CK(cudaMemsetAsync(I->dev.mlp_trace, 0, sizeof(float) * MLP_NPARAM, h->st));
-  int st = 0;
-  CK(cudaMemcpyAsync(&st, h->d_mlp_status, sizeof(int), cudaMemcpyDeviceToHost, h->st));
   int rc = finish(h);
   if (rc) return rc;
-  if (st) { h->err = "wall-model network: tensor-core wait timed out"; return CHL_E_CUDA; }
-  return CHL_OK;
+  return check_mlp(h);
+}
+
+int chl_mlp_debug(chl_handle* h, int record, int withhold_polls) {
+  if (!h) return CHL_E_ARG;
+  if (withhold_polls < 0 || withhold_polls > 64) { h->err = "withhold_polls must be in [0, 64]"; return CHL_E_ARG; }
+  if (record && h->wall_model != CHL_WM_MLP) { h->err = "record: the instances have no learned wall model"; return CHL_E_ARG; }
+  const unsigned int c[2] = {record ? 1u : 0u, (unsigned int)withhold_polls};
+  CK(cudaMemcpyAsync(h->d_mlp_cfg + 5, c, sizeof(c), cudaMemcpyHostToDevice, h->st));
+  return finish(h);
+}
+
+int chl_mlp_read_record(chl_handle* h, int inst, float* rec) {
+  Inst* I = get_inst(h, inst);
+  if (!I || !rec) return CHL_E_ARG;
+  if (!I->dev.mlp_rec) { h->err = "no learned wall model in this instance"; return CHL_E_ARG; }
+  const size_t n = (size_t)CHL_MLP_REC * 3 * 2 * I->c.Nx * I->c.Nz;
+  CK(cudaMemcpyAsync(rec, I->dev.mlp_rec, sizeof(float) * n, cudaMemcpyDeviceToHost, h->st));
+  return finish(h);
 }
 
 int chl_mlp_eval(chl_handle* h, const float* x, const float* g, int P, float* mu, float* trace) {
@@ -1392,14 +1430,18 @@ int chl_mlp_eval(chl_handle* h, const float* x, const float* g, int P, float* mu
     if (e == cudaSuccess) e = cudaMemcpyAsync(&st, h->d_mlp_status, sizeof(int), cudaMemcpyDeviceToHost, h->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
     if (e != cudaSuccess) { h->err = std::string("CUDA: ") + cudaGetErrorString(e); rc = CHL_E_CUDA; }
-    else if (st) { h->err = "wall-model network: tensor-core wait timed out"; rc = CHL_E_CUDA; }
+    else if (st) {
+      h->err = "wall-model network: tensor-core wait timed out";
+      rc = CHL_E_TIMEOUT;
+      cudaMemset(h->d_mlp_status, 0, sizeof(int));   // reported here, not again by a later call
+    }
   }
   cudaFree(dx); cudaFree(dg); cudaFree(dmu); cudaFree(dtr);
   return rc;
 }
 
 int chl_tc_selftest(const unsigned short* A, const unsigned short* B, float* D, int variant) {
-  if (!A || !B || !D || variant < 0 || variant > 1) return CHL_E_ARG;
+  if (!A || !B || !D || variant < 0 || variant > 2) return CHL_E_ARG;
   void *dA = nullptr, *dB = nullptr; float* dD = nullptr; int* ds = nullptr;
   int rc = CHL_OK;
   if (cudaMalloc(&dA, 2 * 128 * 64) != cudaSuccess || cudaMalloc(&dB, 2 * 64 * 64) != cudaSuccess ||
@@ -1414,7 +1456,8 @@ int chl_tc_selftest(const unsigned short* A, const unsigned short* B, float* D, 
     int st = 0;
     if (e == cudaSuccess) e = cudaMemcpy(D, dD, 4 * 128 * 64, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(&st, ds, sizeof(int), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess || st) rc = CHL_E_CUDA;
+    if (e != cudaSuccess) rc = CHL_E_CUDA;
+    else if (st) rc = CHL_E_TIMEOUT;
   }
   cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(ds);
   return rc;
@@ -1434,7 +1477,7 @@ static int run_stats(chl_handle* h, int inst, std::vector<double>& buf) {
 int chl_stats(chl_handle* h, int inst, chl_stats_out* out) {
   if (!out || !h) return CHL_E_ARG;
   int rc0 = finish(h);
-  if (rc0 || (rc0 = check_finite(h, inst))) return rc0;
+  if (rc0 || (rc0 = check_finite(h, inst)) || (rc0 = check_mlp(h))) return rc0;
   std::vector<double> buf;
   int rc = run_stats(h, inst, buf); if (rc) return rc;
   const Inst& I = h->in[inst];

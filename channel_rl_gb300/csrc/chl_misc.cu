@@ -299,19 +299,10 @@ __global__ void k_tadvance(ChlMap map) {
 
 // ------------------------------------------------------------ divergence check
 // check_divergence (projection.f90:223-245): signed max and max |div| over
-// the unique centres; one block per instance, results in scal.
-__global__ void k_divmax(ChlMap map, int s, double* out) {
-  const ChlInst& I = map.inst[blockIdx.x];
-  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  const double *U = I.U[s], *V = I.V[s], *W = I.W[s];
-  double mx = 0.0, ma = 0.0;
-  for (long w = threadIdx.x; w < (long)Nx * Ny * Nz; w += blockDim.x) {
-    const int i = (int)(w % Nx), jc = 1 + (int)((w / Nx) % Ny), k = (int)(w / ((long)Nx * Ny));
-    const double d = (U[cidx(I, i, jc, k)] - U[cidx(I, wrap(i - 1, Nx), jc, k)]) * I.rdxc[i]
-                   + (V[vidx(I, i, jc, k)] - V[vidx(I, i, jc - 1, k)]) * I.rdyc[jc]
-                   + (W[cidx(I, i, jc, k)] - W[cidx(I, i, jc, wrap(k - 1, Nz))]) * I.rdzc[k];
-    mx = fmax(mx, d); ma = fmax(ma, fabs(d));
-  }
+// the unique centres.  One block per z plane of every instance writes the
+// plane's pair into red[2k], red[2k+1] (the upload's bulk-flow partials,
+// free outside chl_upload); k_divmax_final reduces an instance's planes.
+__device__ __forceinline__ void block_max2(double& mx, double& ma) {
   __shared__ double r0[256], r1[256];
   r0[threadIdx.x] = mx; r1[threadIdx.x] = ma;
   __syncthreads();
@@ -319,7 +310,34 @@ __global__ void k_divmax(ChlMap map, int s, double* out) {
     if (threadIdx.x < h) { r0[threadIdx.x] = fmax(r0[threadIdx.x], r0[threadIdx.x + h]); r1[threadIdx.x] = fmax(r1[threadIdx.x], r1[threadIdx.x + h]); }
     __syncthreads();
   }
-  if (threadIdx.x == 0) { out[2 * blockIdx.x] = r0[0]; out[2 * blockIdx.x + 1] = r1[0]; }
+  mx = r0[0]; ma = r1[0];
+}
+
+__global__ void __launch_bounds__(256) k_divmax_plane(ChlMap map, int s) {
+  int k;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, k)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const double *U = I.U[s], *V = I.V[s], *W = I.W[s];
+  const double rz = I.rdzc[k];
+  const int km = wrap(k - 1, Nz);
+  double mx = 0.0, ma = 0.0;
+  for (int w = threadIdx.x; w < Nx * Ny; w += blockDim.x) {
+    const int i = w % Nx, jc = 1 + w / Nx;
+    const double d = (U[cidx(I, i, jc, k)] - U[cidx(I, wrap(i - 1, Nx), jc, k)]) * I.rdxc[i]
+                   + (V[vidx(I, i, jc, k)] - V[vidx(I, i, jc - 1, k)]) * I.rdyc[jc]
+                   + (W[cidx(I, i, jc, k)] - W[cidx(I, i, jc, km)]) * rz;
+    mx = fmax(mx, d); ma = fmax(ma, fabs(d));
+  }
+  block_max2(mx, ma);
+  if (threadIdx.x == 0) { I.red[2 * k] = mx; I.red[2 * k + 1] = ma; }
+}
+
+__global__ void __launch_bounds__(256) k_divmax_final(ChlMap map, double* out) {
+  const ChlInst& I = map.inst[blockIdx.x];
+  double mx = 0.0, ma = 0.0;
+  for (int k = threadIdx.x; k < I.Nz; k += blockDim.x) { mx = fmax(mx, I.red[2 * k]); ma = fmax(ma, I.red[2 * k + 1]); }
+  block_max2(mx, ma);
+  if (threadIdx.x == 0) { out[2 * blockIdx.x] = mx; out[2 * blockIdx.x + 1] = ma; }
 }
 
 // ------------------------------------------------------------ initial bulk flow Qflow_x_0
@@ -377,7 +395,10 @@ void chl_launch_dt(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_dt, dim3
 void chl_launch_massflow(const ChlMap& m, cudaStream_t st, int s, int force) { chl_launch_pdl(k_massflow, dim3(m.n), dim3(256), 0, st, m, s, force); }
 void chl_launch_shift(const ChlMap& m, int nb, int s, cudaStream_t st) { chl_launch_pdl(k_shift, dim3(nb), dim3(m.tb), 0, st, m, s); }
 void chl_launch_tadvance(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_tadvance, dim3(m.n), dim3(32), 0, st, m); }
-void chl_launch_divmax(const ChlMap& m, int s, double* out, cudaStream_t st) { k_divmax<<<m.n, 256, 0, st>>>(m, s, out); }
+void chl_launch_divmax(const ChlMap& planes, int nplanes, int s, double* out, cudaStream_t st) {
+  k_divmax_plane<<<nplanes, 256, 0, st>>>(planes, s);
+  k_divmax_final<<<planes.n, 256, 0, st>>>(planes, out);
+}
 void chl_launch_qflow(const ChlInst* inst, int Nz, int s, int slot, cudaStream_t st) {
   k_qflow_part<<<Nz, 256, 0, st>>>(inst, s);
   k_qflow_final<<<1, 1, 0, st>>>(inst, slot);

@@ -106,6 +106,11 @@ k_mlp(ChlMap map, MlpArgs A) {
   const unsigned int* cfg = chan ? I->mlp_cfg : nullptr;
   const bool train = chan ? (cfg[1] != 0) : true;
   float* trace = chan ? I->mlp_trace : A.trace_out;
+  // checking hooks (chl_mlp_debug): the per-point record, and a withheld
+  // MMA whose completion wait gives up after cfg[6] polls
+  float* rec = (chan && cfg[5] != 0u && I->mlp_rec) ? I->mlp_rec + (size_t)A.stage * P * 8 : nullptr;
+  const unsigned int withhold = chan ? cfg[6] : 0u;
+  const long wait_iters = withhold ? (long)withhold : MLP_WAIT_ITERS;
 
   if (tid == 0) tc::mbar_init(mbar, 1);
   if (warp == 0) tc::tmem_alloc(tslot, 256);
@@ -164,6 +169,12 @@ k_mlp(ChlMap map, MlpArgs A) {
     x[0] = A.x[4 * gp]; x[1] = A.x[4 * gp + 1]; x[2] = A.x[4 * gp + 2]; x[3] = A.x[4 * gp + 3];
     g = A.g[gp];
   }
+  if (rec && valid) {
+    float* r = rec + (size_t)gp * 8;
+    r[0] = x[0]; r[1] = x[1]; r[2] = x[2]; r[3] = x[3];
+    r[4] = __int_as_float(0x7fc00000); r[5] = 0.f;     // mu, a: set below unless the wait runs out
+    r[6] = trusted ? 1.f : 0.f; r[7] = 0.f;
+  }
   // ---------------------------------------------------------------- layer 1 (FP32) -> H1 tiles
   float h1[MLP_H];
 #pragma unroll
@@ -180,14 +191,14 @@ k_mlp(ChlMap map, MlpArgs A) {
   __syncthreads();
   tc::fence_after_sync();
   // ---------------------------------------------------------------- layer 2 on the tensor cores
-  if (tid == 0) {
+  if (tid == 0 && !withhold) {
 #pragma unroll
     for (int s = 0; s < 4; ++s)
       tc::mma_bf16(taddr, tc::make_desc(tc::smem_u32(sm + S_A1 + 256 * s), 128, 1024),
                    tc::make_desc(tc::smem_u32(sm + S_BW2 + 256 * s), 128, 1024), IDESC_128x64, s);
     tc::mma_commit(mbar);
   }
-  bool ok = tc::mbar_wait(mbar, 0, MLP_WAIT_ITERS);
+  bool ok = tc::mbar_wait(mbar, 0, wait_iters);
   ok = __syncthreads_and(ok);
   float mu = 0.f;
   if (ok) {
@@ -219,6 +230,7 @@ k_mlp(ChlMap map, MlpArgs A) {
         g = (train && sigma > 0.f) ? eps / sigma : 0.f;
         I->alpha[gp] = taueq * exp((double)a);
       }
+      if (rec && valid) { rec[(size_t)gp * 8 + 4] = mu; rec[(size_t)gp * 8 + 5] = a; }
     } else if (valid) {
       A.mu_out[gp] = mu;
     }
@@ -319,7 +331,9 @@ k_mlp(ChlMap map, MlpArgs A) {
 // ---------------------------------------------------------------- tcgen05 self-test
 // D[128x64] = A[128x64] . B[64x64]^T for BF16 A, B (row-major, K contiguous),
 // one CTA.  `variant` selects which descriptor field carries the K-direction
-// core-matrix stride (0: LBO, 1: SBO); both stay inside the tiles.
+// core-matrix stride (0: LBO, 1: SBO); both stay inside the tiles.  Variant
+// 2 issues no MMA and waits at most 64 polls on the completion barrier,
+// which nothing arrives at: the bounded-wait path (status set, TMEM freed).
 __global__ void __launch_bounds__(128)
 k_tc_selftest(const __nv_bfloat16* Ag, const __nv_bfloat16* Bg, float* D, int variant, int* status) {
   extern __shared__ __align__(1024) unsigned char sm[];
@@ -344,14 +358,15 @@ k_tc_selftest(const __nv_bfloat16* Ag, const __nv_bfloat16* Bg, float* D, int va
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = *tslot;
-  const uint32_t lbo = variant == 0 ? 128u : 1024u, sbo = variant == 0 ? 1024u : 128u;
-  if (tid == 0) {
+  const uint32_t lbo = variant == 1 ? 1024u : 128u, sbo = variant == 1 ? 128u : 1024u;
+  const bool withhold = variant == 2;
+  if (tid == 0 && !withhold) {
     for (int s = 0; s < 4; ++s)
       tc::mma_bf16(taddr, tc::make_desc(tc::smem_u32(As + 256 * s), lbo, sbo),
                    tc::make_desc(tc::smem_u32(Bs + 256 * s), lbo, sbo), IDESC_128x64, s);
     tc::mma_commit(mbar);
   }
-  bool ok = tc::mbar_wait(mbar, 0, MLP_WAIT_ITERS);
+  bool ok = tc::mbar_wait(mbar, 0, withhold ? 64L : MLP_WAIT_ITERS);
   ok = __syncthreads_and(ok);
   if (ok) {
     tc::fence_after_sync();

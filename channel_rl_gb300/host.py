@@ -27,7 +27,15 @@ _F64P = C.POINTER(C.c_double)
 
 
 class ChlError(RuntimeError):
-    pass
+    """A C-ABI call returned an error; ``rc`` is its CHL_E_* code."""
+
+    def __init__(self, msg, rc=None):
+        super().__init__(msg)
+        self.rc = rc
+
+
+# CHL_E_* (include/chl.h)
+E_ARG, E_CUDA, E_NOMEM, E_STATE, E_NAN, E_IO, E_TIMEOUT = 1, 2, 3, 4, 5, 6, 7
 
 
 class GridDesc(C.Structure):
@@ -68,7 +76,7 @@ EXPORTS = (
     "chl_autotune", "chl_get_tile_shapes", "chl_set_tile_shapes",
     "chl_check_divergence_noalloc", "chl_noalloc_last_error",
     "chl_mlp_set_params", "chl_mlp_get_params", "chl_mlp_configure", "chl_mlp_read_trace",
-    "chl_mlp_eval", "chl_tc_selftest",
+    "chl_mlp_eval", "chl_mlp_debug", "chl_mlp_read_record", "chl_tc_selftest",
     "chl_snapshot_dims", "chl_snapshot_read", "chl_snapshot_write", "chl_io_last_error",
     "chl_read_parameters", "chl_save_snapshot", "chl_load_snapshot",
     "chl_agent_observe", "chl_agent_act", "chl_status_flags",
@@ -133,6 +141,8 @@ def load(build_if_missing=True):
     lib.chl_mlp_configure.argtypes = [H, C.c_float, C.c_ulonglong, C.c_int]
     lib.chl_mlp_read_trace.argtypes = [H, C.c_int, _F32P, C.c_int]
     lib.chl_mlp_eval.argtypes = [H, _F32P, _F32P, C.c_int, _F32P, _F32P]
+    lib.chl_mlp_debug.argtypes = [H, C.c_int, C.c_int]
+    lib.chl_mlp_read_record.argtypes = [H, C.c_int, _F32P]
     lib.chl_tc_selftest.argtypes = [C.POINTER(C.c_ushort), C.POINTER(C.c_ushort), _F32P, C.c_int]
     I = C.POINTER(C.c_int)
     lib.chl_snapshot_dims.argtypes = [C.c_char_p, I, I, I]
@@ -242,7 +252,7 @@ def tc_selftest(A_bf16_bits, B_bf16_bits, variant=0):
     rc = lib.chl_tc_selftest(A.ctypes.data_as(C.POINTER(C.c_ushort)), B.ctypes.data_as(C.POINTER(C.c_ushort)),
                              D.ctypes.data_as(_F32P), variant)
     if rc:
-        raise ChlError(f"chl_tc_selftest failed ({rc})")
+        raise ChlError(f"chl_tc_selftest failed ({rc})", rc)
     return D
 
 
@@ -284,7 +294,7 @@ class Channel:
     def _check(self, rc, what):
         if rc:
             msg = self.lib.chl_last_error(self.h).decode() if self.h else ""
-            raise ChlError(f"{what} failed ({rc}): {msg}")
+            raise ChlError(f"{what} failed ({rc}): {msg}", rc)
 
     def close(self):
         if getattr(self, "h", None):
@@ -416,6 +426,19 @@ class Channel:
         t = np.zeros(MLP_NPARAM, np.float32)
         self._check(self.lib.chl_mlp_read_trace(self.h, inst, t.ctypes.data_as(_F32P), int(zero)), "chl_mlp_read_trace")
         return t
+
+    def mlp_debug(self, record=False, withhold_polls=0):
+        """Checking hooks: per-point record of every evaluation, or MMAs
+        withheld so that the completion wait runs out (chl_mlp_debug)."""
+        self._check(self.lib.chl_mlp_debug(self.h, int(bool(record)), int(withhold_polls)), "chl_mlp_debug")
+
+    def mlp_record(self, inst=0):
+        """(3, 2, Nz, Nx, 8) float32: per RK stage, wall, z, x point the
+        normalised features x0..x3, mu, the action a and the trust flag."""
+        c = self.cases[inst]
+        r = np.zeros((3, 2, c.Nz, c.Nx, 8), np.float32)
+        self._check(self.lib.chl_mlp_read_record(self.h, inst, r.ctypes.data_as(_F32P)), "chl_mlp_read_record")
+        return r
 
     def mlp_eval(self, x, g):
         """mu and sum_p g_p dmu_p/dtheta of the network on given features (tensor-core kernel)."""

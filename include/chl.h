@@ -35,6 +35,10 @@ extern "C" {
 #define CHL_E_NAN 5      /* non-finite velocity found by the step's CFL pass; reported by
                             chl_synchronize, chl_download and chl_stats until the next upload */
 #define CHL_E_IO 6       /* file could not be opened, read or written */
+#define CHL_E_TIMEOUT 7  /* a bounded device wait ran out: the learned wall model's tensor-core
+                            completion barrier.  Points of the CTAs that gave up kept the
+                            equilibrium stress for that stage.  Reported once (then cleared) by
+                            chl_synchronize, chl_download, chl_stats and chl_mlp_read_trace. */
 
 /* LES_model (subgrid.f90:30-45) */
 #define CHL_LES_NONE 0
@@ -196,8 +200,26 @@ int chl_mlp_read_trace(chl_handle* h, int inst, float* trace, int zero_after);
 /* Network on given points (no channel): x[P][4] normalised features,
  * g[P] upstream weights -> mu[P] and trace = sum_p g_p dmu_p/dtheta. */
 int chl_mlp_eval(chl_handle* h, const float* x, const float* g, int P, float* mu, float* trace);
+/* Checking hooks of the learned wall model.
+ * record != 0: every evaluation in the channel writes, per wall point, the
+ *   CHL_MLP_REC floats [x0, x1, x2, x3 (normalised features), mu, action a,
+ *   trusted (1 or 0), 0] into its instance's record, one slot per RK3 stage
+ *   (the record holds the last evaluation of each stage).
+ * withhold_polls > 0: the tensor-core MMAs are not issued and the completion
+ *   wait gives up after withhold_polls polls (at most 64): every evaluation
+ *   times out, keeps the equilibrium stress and reports CHL_E_TIMEOUT.  0
+ *   restores normal operation. */
+#define CHL_MLP_REC 8
+int chl_mlp_debug(chl_handle* h, int record, int withhold_polls);
+/* Record of one instance: 3 x 2*Nx*Nz x CHL_MLP_REC floats, stage-major,
+ * then wall point p = (wall*Nz + k)*Nx + i (i, k unique cells, wall 0 bottom). */
+int chl_mlp_read_record(chl_handle* h, int inst, float* rec);
 /* Standalone tensor-core check: D[128x64] = A[128x64] B[64x64]^T, BF16
- * inputs (raw 16-bit patterns, row major), FP32 output. */
+ * inputs (raw 16-bit patterns, row major), FP32 output.  variant 0 and 1
+ * place the K-direction core-matrix stride in the descriptor's LBO or SBO
+ * field; variant 2 issues no MMA and waits with a limit of 64 polls on the
+ * completion barrier that nothing arrives at: it frees its TMEM and returns
+ * CHL_E_TIMEOUT (the bounded-wait path of the wall-model kernel). */
 int chl_tc_selftest(const unsigned short* A, const unsigned short* B, float* D, int variant);
 
 /* Allocation-free divergence check, for callers that must not let a
@@ -212,9 +234,11 @@ int chl_tc_selftest(const unsigned short* A, const unsigned short* B, float* D, 
  * NULL for the default stream); it synchronises that stream.
  * Limit: nz - 1 <= 4096 (its scratch is a fixed 64 KiB device array held by
  * every GPU that loads the library); larger grids return CHL_E_ARG.
- * The first call on each device looks up the scratch address and should
- * come before any stream capture.  Calls that overlap on the GPU race on
- * the shared scratch and must be serialised by the caller.
+ * It cannot be called while any stream is being captured (it copies its
+ * results to pageable host memory and synchronises `stream`).  Each call
+ * looks up the scratch address in the calling thread's current context.
+ * Calls that overlap on the GPU race on the shared scratch and must be
+ * serialised by the caller.
  * Errors: chl_noalloc_last_error() (per host thread). */
 int chl_check_divergence_noalloc(const double* U, const double* V, const double* W,
                                  const double* x, const double* y, const double* z,

@@ -64,7 +64,7 @@ B_LOG = 5.2
 EQWM_NEWTON_ITERS = 12
 
 LES_NONE, LES_SMAG, LES_DSM, LES_AMD, LES_VREMAN = 0, 1, 2, 3, 4
-WM_NONE, WM_STRESS, WM_EQLOG = 0, 1, 2
+WM_NONE, WM_STRESS, WM_EQLOG, WM_MLP = 0, 1, 2, 3
 
 
 def pad1(a):
@@ -90,6 +90,7 @@ class Params:
     Dirichlet_nu_t: int = 1
     wall_model: int = WM_NONE      # oracle switch (see module doc)
     Cs: float = 0.1                # static Smagorinsky constant
+    Re_tau: float = 0.0            # nominal Re_tau (learned wall model feature ln(h Re_tau))
 
 
 class Grid:
@@ -271,6 +272,16 @@ class ChannelOracle:
         self.t = 0.0
         self.dt = 0.0
         self.Qflow_x_0 = 0.0
+        # learned wall model (WM_MLP, oracle/mlp_wm_ref.py): network
+        # parameters (None: zero network), optional per-stage actions
+        # callable(stage) -> (Nx, 2, Nz) float32 in place of the network's,
+        # the nu + nu_t field of the previous stage's wall-model pass (zero
+        # before the first, as a new GPU handle holds it), and the last
+        # evaluation's features and actions per stage
+        self.mlp_theta = None
+        self.mlp_actions = None
+        self.mlp_nutot = alloc(g.nxg, g.nyg, g.nzg)
+        self.mlp_info = [None, None, None]
 
     # -- state I/O ---------------------------------------------------------
     def set_fields(self, U, V, W):
@@ -995,12 +1006,20 @@ class ChannelOracle:
         return self.Qflow_x_0 - float(Ui.sum()) / float(Ui.size)
 
     # -- RK3 step (time_integration.f90:24-96) -------------------------------
-    def _stage_sgs_wm(self):
+    def _stage_sgs_wm(self, stage=0):
         self.compute_eddy_viscosity()
-        if self.p.wall_model == WM_EQLOG:
-            self.set_wall_stress(self.compute_wall_stress_eqlog())
+        if self.p.wall_model in (WM_EQLOG, WM_MLP):
+            alpha = self.compute_wall_stress_eqlog()
+            if self.p.wall_model == WM_MLP:
+                from . import mlp_wm_ref
+                act = self.mlp_actions(stage) if self.mlp_actions else None
+                alpha, self.mlp_info[stage] = mlp_wm_ref.wall_stress(self, alpha, self.mlp_nutot,
+                                                                     self.mlp_theta, act)
+            self.set_wall_stress(alpha)
         if self.p.wall_model != WM_NONE:
             self.compute_wall_model()
+        if self.p.wall_model == WM_MLP:
+            self.mlp_nutot = self.p.nu + self.nu_t
 
     def compute_time_step_RK3(self):
         g, dt = self.g, self.dt
@@ -1009,7 +1028,7 @@ class ChannelOracle:
         Uo, Vo, Wo = self.U.copy(), self.V.copy(), self.W.copy()
         Fu, Fv, Fw = [None] * 3, [None] * 3, [None] * 3
         for s in range(3):
-            self._stage_sgs_wm()
+            self._stage_sgs_wm(s)
             Fu[s] = self.compute_rhs_u(self.U, self.V, self.W, self.nu_t, self.dPdx)
             Fv[s] = self.compute_rhs_v(self.U, self.V, self.W, self.nu_t)
             Fw[s] = self.compute_rhs_w(self.U, self.V, self.W, self.nu_t)

@@ -16,7 +16,7 @@ def oracle_for(case):
     g = Grid(*C.faces(case))
     p = Params(nu=case.nu, CFL=case.CFL, dPdx=case.dPdx, x_mass_cte=case.x_mass_cte,
                LES_model=case.LES_model, Dirichlet_nu_t=case.Dirichlet_nu_t,
-               wall_model=min(case.wall_model, 2), Cs=case.Cs)
+               wall_model=case.wall_model, Cs=case.Cs, Re_tau=case.Retau)
     return ChannelOracle(g, p)
 
 
