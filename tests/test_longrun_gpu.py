@@ -78,14 +78,14 @@ def test_small_channel_1000_steps_statistics():
 
 def test_wallmodelled_channel_long_run_against_host():
     """The wall-modelled 64^3 channel (Re_tau 2000, equilibrium wall model,
-    dynamic Smagorinsky, constant mass flow): GPU and the host restatement
-    from the same start, compared every 500 steps.  Default 1000 steps;
-    CHL_LONGRUN_STEPS=5000 runs the configuration's full 5000."""
+    dynamic Smagorinsky, constant mass flow) over the configuration's full
+    5000 steps: GPU and the host restatement from the same start, compared
+    every 500 steps (CHL_LONGRUN_STEPS sets another horizon)."""
     import os
     from channel_rl_gb300.host import Channel
     from oracle.refcpu import RefCPU
     case = C.c2_wm64()
-    nsteps = int(os.environ.get("CHL_LONGRUN_STEPS", "1000"))
+    nsteps = int(os.environ.get("CHL_LONGRUN_STEPS", "5000"))
     U, V, W = C.initial_fields(case)
     ch = Channel(case)
     ch.upload(U, V, W)
