@@ -598,6 +598,20 @@ def _c2c_record(out):
     return res
 
 
+def _barrier_record(out):
+    """bench_peaks barrier output: microseconds per phase of each ordering."""
+    import re
+    res = {"raw": out.strip().splitlines()}
+    per = [float(x) for x in re.findall(r"^persistent .*: ([0-9.]+) us per phase", out, re.M)]
+    pdl = [float(x) for x in re.findall(r"^graph pdl .*: ([0-9.]+) us per phase", out, re.M)]
+    if per and pdl:
+        res["persistent_barrier_us_best"] = min(per)
+        res["graph_pdl_boundary_us_best"] = min(pdl)
+    res["how"] = ("bench_peaks.cu barrier: 49152-double update per phase; 2000 phases in one cooperative kernel "
+                  "(grid barrier: arrival counter and generation word) vs 200 kernels in one CUDA graph, CUDA events")
+    return res
+
+
 def measure_peaks():
     """Compile bench_peaks.cu, run both probes, write their records."""
     import tempfile
@@ -605,12 +619,14 @@ def measure_peaks():
         exe = os.path.join(d, "bench_peaks")
         subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-o", exe,
                         os.path.join(HERE, "bench_peaks.cu")], check=True)
-        outs = {m: subprocess.run([exe, m], check=True, capture_output=True, text=True).stdout for m in ("fp64", "c2c")}
+        outs = {m: subprocess.run([exe, m], check=True, capture_output=True, text=True).stdout
+                for m in ("fp64", "c2c", "barrier")}
     os.makedirs(os.path.join(HERE, "profiles"), exist_ok=True)
-    for name, rec in (("fp64_peak.json", _fp64_record(outs["fp64"])), ("c2c_bandwidth.json", _c2c_record(outs["c2c"]))):
+    for name, rec in (("fp64_peak.json", _fp64_record(outs["fp64"])), ("c2c_bandwidth.json", _c2c_record(outs["c2c"])),
+                      ("phase_ordering.json", _barrier_record(outs["barrier"]))):
         with open(os.path.join(HERE, "profiles", name), "w") as f:
             json.dump(rec, f, indent=1)
-    print(outs["fp64"] + outs["c2c"])
+    print(outs["fp64"] + outs["c2c"] + outs["barrier"])
 
 
 def main():

@@ -2,8 +2,12 @@
 // compiles and runs this file and writes profiles/fp64_peak.json and
 // profiles/c2c_bandwidth.json).
 //
-//   bench_peaks fp64   FP64 / FP32 issue rates (the FP64 roofline's denominator)
-//   bench_peaks c2c    host<->device bandwidth (the end-to-end line's transfer floor)
+//   bench_peaks fp64     FP64 / FP32 issue rates (the FP64 roofline's denominator)
+//   bench_peaks c2c      host<->device bandwidth (the end-to-end line's transfer floor)
+//   bench_peaks barrier  a grid-wide barrier inside one cooperative persistent
+//                        kernel against a kernel boundary inside a CUDA graph
+//                        (with and without programmatic dependent launch): the
+//                        cost per phase of the two ways to order a step's phases
 //
 #include <cstdio>
 #include <cstring>
@@ -200,9 +204,113 @@ static int c2c_main() {
   return 0;
 }
 
+// ---------------------------------------------------------------- barrier
+// Phase ordering cost.  Each phase updates 49152 doubles (the points of a
+// 32x48x32 channel) once.  Persistent: all phases in one cooperative kernel,
+// separated by a grid barrier (arrival counter plus generation word, every
+// wait bounded: a block that gives up sets the error word and returns).
+// Graph: one kernel per phase captured into a CUDA graph.
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned* gen, unsigned nb, long max_iter) {
+  __syncthreads();
+  int ok = 1;
+  if (threadIdx.x == 0) {
+    const unsigned g = ld_acquire_gpu(gen);
+    __threadfence();
+    if (atomicAdd(count, 1u) + 1u == nb) {
+      atomicExch(count, 0u);
+      __threadfence();
+      atomicAdd(gen, 1u);
+    } else {
+      long it = 0;
+      while (ld_acquire_gpu(gen) == g) if (++it > max_iter) { ok = 0; break; }
+    }
+    __threadfence();
+  }
+  return __syncthreads_and(ok);
+}
+__global__ void k_persist(unsigned* count, unsigned* gen, int nphase, double* buf, int n, int* err) {
+  for (int ph = 0; ph < nphase; ++ph) {
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) buf[t] = fma(buf[t], 0.999, 1e-3);
+    if (!grid_barrier(count, gen, gridDim.x, 2000000L)) { if (threadIdx.x == 0) atomicExch(err, 1); return; }
+  }
+}
+__global__ void k_phase(double* buf, int n) {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) buf[t] = fma(buf[t], 0.999, 1e-3);
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+static int barrier_main() {
+  int sms;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
+  const int n = 49152, nphase = 2000, ngraph = 200;
+  double* buf; unsigned* cnt; int* err;
+  CK(cudaMalloc(&buf, n * 8)); CK(cudaMemset(buf, 0, n * 8));
+  CK(cudaMalloc(&cnt, 64)); CK(cudaMemset(cnt, 0, 64));
+  CK(cudaMalloc(&err, 4)); CK(cudaMemset(err, 0, 4));
+  cudaStream_t st;
+  CK(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  cudaEvent_t a, b;
+  cudaEventCreate(&a); cudaEventCreate(&b);
+  for (int tpb : {256, 512}) {
+    int per = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_persist, tpb, 0));
+    for (int mult = 1; mult <= 2 && mult <= per; ++mult) {   // co-resident grids only
+      int nb = sms * mult, np = nphase, nn = n;
+      unsigned* gen = cnt + 1;
+      void* args[] = {&cnt, &gen, &np, &buf, &nn, &err};
+      for (int rep = 0; rep < 3; ++rep) {
+        CK(cudaEventRecord(a, st));
+        CK(cudaLaunchCooperativeKernel((void*)k_persist, nb, tpb, args, 0, st));
+        CK(cudaEventRecord(b, st));
+        CK(cudaEventSynchronize(b));
+        float ms;
+        cudaEventElapsedTime(&ms, a, b);
+        if (rep == 2) printf("persistent %d blocks x %d: %.3f us per phase\n", nb, tpb, ms * 1e3 / nphase);
+      }
+    }
+  }
+  int herr = 0;
+  CK(cudaMemcpy(&herr, err, 4, cudaMemcpyDeviceToHost));
+  printf("barrier timeouts %d\n", herr);
+  for (int nb : {192, 768}) {
+    for (int pdl = 1; pdl >= 0; --pdl) {
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      at[0].val.programmaticStreamSerializationAllowed = 1;
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = nb; cfg.blockDim = 64; cfg.stream = st; cfg.attrs = at; cfg.numAttrs = pdl;
+      cudaGraph_t g;
+      cudaGraphExec_t ge;
+      CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+      for (int i = 0; i < ngraph; ++i) CK(cudaLaunchKernelEx(&cfg, k_phase, buf, n));
+      CK(cudaStreamEndCapture(st, &g));
+      CK(cudaGraphInstantiate(&ge, g, 0));
+      for (int rep = 0; rep < 4; ++rep) {
+        CK(cudaEventRecord(a, st));
+        CK(cudaGraphLaunch(ge, st));
+        CK(cudaEventRecord(b, st));
+        CK(cudaEventSynchronize(b));
+        float ms;
+        cudaEventElapsedTime(&ms, a, b);
+        if (rep == 3) printf("graph %s %d blocks x 64: %.3f us per phase\n", pdl ? "pdl" : "plain", nb, ms * 1e3 / ngraph);
+      }
+      cudaGraphExecDestroy(ge);
+      cudaGraphDestroy(g);
+    }
+  }
+  CK(cudaGetLastError());
+  return 0;
+}
+
 int main(int argc, char** argv) {
   if (argc > 1 && !std::strcmp(argv[1], "fp64")) return fp64_main();
   if (argc > 1 && !std::strcmp(argv[1], "c2c")) return c2c_main();
-  std::printf("usage: bench_peaks fp64|c2c\n");
+  if (argc > 1 && !std::strcmp(argv[1], "barrier")) return barrier_main();
+  std::printf("usage: bench_peaks fp64|c2c|barrier\n");
   return 2;
 }

@@ -54,3 +54,40 @@ def test_shipped_checkpoint_beats_equilibrium_model():
     assert ml_err.mean() <= 1.001 * eq_err.mean()
     assert ml_ut.mean() <= 0.9 * eq_ut.mean()
     assert ml_ut.max() <= 0.02                   # the 2% u_tau gate at every Re_tau
+
+
+def test_shipped_checkpoint_held_out():
+    """The shipped network on channels it never saw: Re_tau 3000 and 7000
+    (training used 2000, 5200, 10000), other grids and seeds.  Spin-up of
+    1000 steps with the equilibrium model (the reference's agents first act
+    at step 1000), then the deterministic policy with statistics every 200
+    steps (its decision interval), over 1200 steps and over 7600 steps (3-4
+    near-wall response times h/u_tau).
+
+    Measured: the profile error (the reward) is lower on every held-out
+    channel; the u_tau error is not lower (0.44 % -> 0.51 % mean at 1200
+    steps).  Asserted: profile error lower on every channel at both
+    horizons, u_tau within the 2 % gate at 1200 steps for both models, and
+    the learned u_tau error at most 0.2 points above the equilibrium
+    model's."""
+    from channel_rl_gb300.rl import Trainer
+    path = os.path.join(os.path.dirname(__file__), "..", "channel_rl_gb300", "data", "mlp_wm.npy")
+    theta = np.load(path).astype(np.float32)
+    spec = [(64, 48, 64, 3000.0), (96, 64, 96, 3000.0), (64, 48, 64, 7000.0), (96, 64, 96, 7000.0)]
+    held_out = [C.wallmodelled(f"held_out_{m}", Nx, Ny, Nz, rt, seed=9000 + 37 * m, wall_model=C.WM_MLP)
+                for m, (Nx, Ny, Nz, rt) in enumerate(spec)]
+    tr = Trainer(held_out, seed=11, spinup=1000)
+    res = {}
+    for steps in (1200, 7600):
+        eq_err, eq_ut = tr.evaluate(None, steps=steps, chunks=steps // 200)
+        ml_err, ml_ut = tr.evaluate(theta, steps=steps, chunks=steps // 200)
+        res[steps] = (eq_err, eq_ut, ml_err, ml_ut)
+        print(json.dumps({"steps": steps, "equilibrium_profile_err": eq_err.tolist(),
+                          "learned_profile_err": ml_err.tolist(), "equilibrium_utau_err": eq_ut.tolist(),
+                          "learned_utau_err": ml_ut.tolist()}))
+    tr.close()
+    for steps, (eq_err, eq_ut, ml_err, ml_ut) in res.items():
+        assert np.all(ml_err < eq_err), steps
+        assert ml_ut.mean() <= eq_ut.mean() + 0.002, steps
+    eq_err, eq_ut, ml_err, ml_ut = res[1200]
+    assert eq_ut.max() <= 0.02 and ml_ut.max() <= 0.02
