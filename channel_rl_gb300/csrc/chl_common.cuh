@@ -39,16 +39,18 @@ __host__ __device__ inline int chl_tri_lanes(long modes, int Ny) {
   while (P < 8 && modes * P < (long)CHL_MIN_BLOCKS * 32 && Ny >= 4 * P) P *= 2;
   return P;
 }
-// x-z points per thread of the DSM plane sums (k_dsm_final): 4, halved
-// while the instance's Ny x chunks grid would have fewer blocks than SMs.
-// (Each block ends in a shared-memory reduction tree, so cutting finer than
-// one block per SM costs more than it spreads; in a batch the other
-// instances fill the GPU anyway.)  A function of the instance's own extents
-// only, so an instance sums its planes in the same order alone and in a
-// batch.
+// x-z points per thread of the DSM plane sums (k_dsm_final, blocks of
+// CHL_DSMF_THREADS): 4, halved while the instance's Ny x chunks grid would
+// have fewer than CHL_MIN_BLOCKS blocks.  A large instance has chunks of 256
+// points (192 per plane at 256x192); a 32x48x32 channel gets 768 blocks of
+// one point per thread, 5 per SM, where 256-thread blocks left 2 blocks on
+// some SMs and 1 on most.  A function of the instance's own extents only,
+// so an instance sums its planes in the same order alone and in a batch.
+#define CHL_DSMF_THREADS 64
 __host__ __device__ inline int chl_dsm_ppt(int Nx, int Ny, int Nz) {
   int ppt = 4;
-  while (ppt > 1 && (long)Ny * ((Nx * Nz + 256 * ppt - 1) / (256 * ppt)) < CHL_SMS) ppt >>= 1;
+  while (ppt > 1 && (long)Ny * ((Nx * Nz + CHL_DSMF_THREADS * ppt - 1) / (CHL_DSMF_THREADS * ppt)) < CHL_MIN_BLOCKS)
+    ppt >>= 1;
   return ppt;
 }
 // complex rows (pairs of real x lines) per x-transform block: up to
@@ -80,6 +82,7 @@ struct ChlInst {
   int LES_model, Dirichlet_nu_t, wall_model, x_mass_cte;
   double nu, CFL, Cs;
   double dxmin, dymin, dzmin;   // initialization.f90:233-235
+  double dt_vis;                // viscous limit of compute_dt, min(CFL d^2/nu) over x, y, z (host-formed)
   double dyw;                   // yg(2)-yg(1), used for both walls (wallmodel.f90:32-35)
   double hb, ht;                // matching heights of the log-law wall model
   double cbc1, cbc2;            // coef_bc_1*(yg(2)-yg(1)), coef_bc_2*(yg(nyg)-yg(nyg-1))
@@ -121,7 +124,8 @@ struct ChlInst {
   double *scal;                   // device scalars (CHL_S_*)
   unsigned long long *minabs;     // [Nx+1 | Nz] min |u| bit patterns (dt)
   double *red;                    // plane partials [2][Nz]: bulk flow (upload), divergence check
-  int *status;                    // device status word (0 ok)
+  int *status;                    // device status word (0 ok); [CHL_CNT_DT] block counter of k_minabs
+  int *dsm_cnt;                   // [Ny+2] block counters of the DSM plane sums per centre row
   // learned wall model (chl_mlp.cu)
   double retau;                   // nominal Re_tau of the instance (feature ln(h Re_tau))
   float *mlp_trace;               // policy-gradient trace of this instance (4545)
@@ -207,6 +211,9 @@ __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >=
 // 4 an index outside the field (bounds-checked build only).
 #define CHL_STATUS_NONFINITE 1
 #define CHL_STATUS_BOUNDS 4
+// slot of the status area that counts k_minabs's finished blocks (the last
+// one forms dt); the counters return to 0 after each use
+#define CHL_CNT_DT 4
 
 // The bounds-checked build (-DCHL_BOUNDS_CHECK, build.build(variant="bounds"))
 // records an out-of-range index in the status word and clamps it, so the

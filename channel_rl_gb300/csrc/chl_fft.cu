@@ -21,6 +21,8 @@
 //  * the inverse runs the same way back and the x pass writes the pressure.
 #include "chl_common.cuh"
 
+#include <cooperative_groups.h>
+
 // ------------------------------------------------------------ Stockham passes
 // Data of `nrows` transforms of length N; element e of row r is at
 // r*rs + e*es.  One pass of radix R with sub-transform size Ns.
@@ -453,6 +455,173 @@ k_tri_scan(ChlMap map) {
   backward(xin, true, unused);
 }
 
+// ------------------------------------------------------------ fused z transform + tridiagonal + inverse z
+// For instances whose wavenumber column block fits in shared memory: one
+// thread-block cluster of P CTAs per (instance, kx), P = chl_tri_lanes of
+// the instance (the lane count of k_tri_scan).  CTA r holds the rows that
+// lane r of k_tri_scan owns, [r L, min(Ny, (r+1) L)) with L = ceil(Ny/P),
+// for all Nz wavenumbers kz, and runs on them
+//   the forward z transform (the Stockham passes of k_fftz),
+//   the Thomas sweeps of k_tri_scan, whose lane maps (A, z) it exchanges
+//     with the other CTAs of its cluster through distributed shared memory
+//     and scans with the same warp shuffles (one thread per (kz, lane)),
+//   the inverse z transform,
+// so the result is bit-identical to k_fftz, the tridiagonal kernel and
+// k_fftz again, in one launch and without the two round trips of the
+// spectrum.  The cluster barriers are hardware barriers that every thread
+// of the cluster reaches (no early exit).
+namespace cg = cooperative_groups;
+
+__global__ void __launch_bounds__(256)
+k_zsolve(ChlMap map) {
+  chl_pdl_wait();
+  extern __shared__ double2 sm[];
+  cg::cluster_group cl = cg::this_cluster();
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Ny = I.Ny, Nz = I.Nz, Nxh = I.Nxh;
+  const long modes = (long)Nz * Nxh;
+  const int P = chl_tri_lanes(modes, Ny);       // the cluster size (host-checked)
+  const int r = lb % P, kx = lb / P;
+  const int L = (Ny + P - 1) / P;
+  const int lo = min(Ny, r * L), hi = min(Ny, lo + L), nr = hi - lo;
+  const size_t ps = (size_t)modes;              // row pitch of spec and factors
+  double2* A = sm;
+  double2* B = sm + (size_t)L * Nz;
+  double2* T = sm + (size_t)2 * L * Nz;
+  double2* fz = T + Nz;                         // forward lane values
+  double2* bw = fz + Nz;                        // backward lane values
+  double2* yin = bw + Nz;
+  double2* xin = yin + Nz;
+  double* fA = reinterpret_cast<double*>(xin + Nz);
+  double* bA = fA + Nz;
+  const int t = threadIdx.x, bd = blockDim.x;
+  stage_twiddles(T, I.twz, Nz);
+  // rows [lo, hi) of column kx: element (row l, kz) at l + kz*nr
+  double2* spec = I.spec + ps + kx;             // row jc = 1
+  for (int w = t; w < nr * Nz; w += bd) {
+    const int l = w % nr, kz = w / nr;
+    A[l + (size_t)kz * nr] = spec[(size_t)(lo + l) * ps + (size_t)kz * Nxh];
+  }
+  double2* res = fft_smem(A, B, nr, 1, nr, Nz, T, false);
+  double2* other = res == A ? B : A;
+  const double* __restrict__ fi = I.tri_inv + kx;
+  const double* __restrict__ fm = I.tri_m + kx;
+  const double* __restrict__ fc = I.tri_c + kx;
+  const unsigned full = 0xffffffffu;
+  // ---- forward elimination: this CTA's lane maps
+  if (P > 1) {
+    for (int kz = t; kz < Nz; kz += bd) {
+      const size_t mo = (size_t)kz * Nxh;
+      double Am = 1.0;
+      double2 prev = make_double2(0.0, 0.0);
+      for (int j = lo; j < hi; ++j) {
+        double2 d = res[(j - lo) + (size_t)kz * nr];
+        const double iv = LDG(fi + (size_t)j * ps + mo), m = LDG(fm + (size_t)j * ps + mo);
+        d.x = fma(d.x, iv, -m * prev.x);
+        d.y = fma(d.y, iv, -m * prev.y);
+        prev = d;
+        Am = -m * Am;
+      }
+      fA[kz] = Am;
+      fz[kz] = prev;
+    }
+  }
+  cl.sync();
+  if (P > 1) {
+    // one thread per (kz, lane p): the inclusive scan of k_tri_scan
+    for (int base = 0; base < Nz * P; base += bd) {
+      const int w = base + t, kz = w / P, p = w % P;
+      const bool ok = kz < Nz;
+      const double* rA = cl.map_shared_rank(fA, p);
+      const double2* rz = cl.map_shared_rank(fz, p);
+      double Av = ok ? rA[kz] : 1.0;
+      double2 z = ok ? rz[kz] : make_double2(0.0, 0.0);
+      for (int off = 1; off < P; off <<= 1) {
+        const double Ao = __shfl_up_sync(full, Av, off, P);
+        const double bx = __shfl_up_sync(full, z.x, off, P), by = __shfl_up_sync(full, z.y, off, P);
+        if (p >= off) { z.x = fma(Av, bx, z.x); z.y = fma(Av, by, z.y); Av *= Ao; }
+      }
+      double2 y;
+      y.x = __shfl_up_sync(full, z.x, 1, P);
+      y.y = __shfl_up_sync(full, z.y, 1, P);
+      if (p == 0) y = make_double2(0.0, 0.0);
+      if (ok && p == r) yin[kz] = y;
+    }
+  }
+  __syncthreads();
+  for (int kz = t; kz < Nz; kz += bd) {
+    const size_t mo = (size_t)kz * Nxh;
+    double2 prev = P > 1 ? yin[kz] : make_double2(0.0, 0.0);
+    for (int j = lo; j < hi; ++j) {
+      double2 d = res[(j - lo) + (size_t)kz * nr];
+      const double iv = LDG(fi + (size_t)j * ps + mo), m = LDG(fm + (size_t)j * ps + mo);
+      d.x = fma(d.x, iv, -m * prev.x);   // m = 0 on the first row
+      d.y = fma(d.y, iv, -m * prev.y);
+      prev = d;
+      res[(j - lo) + (size_t)kz * nr] = d;
+    }
+  }
+  // ---- back substitution from the top
+  if (P > 1) {
+    for (int kz = t; kz < Nz; kz += bd) {
+      const size_t mo = (size_t)kz * Nxh;
+      double Am = 1.0;
+      double2 prev = make_double2(0.0, 0.0);
+      for (int j = hi - 1; j >= lo; --j) {
+        double2 d = res[(j - lo) + (size_t)kz * nr];
+        const double c = LDG(fc + (size_t)j * ps + mo);
+        d.x = fma(-c, prev.x, d.x);
+        d.y = fma(-c, prev.y, d.y);
+        prev = d;
+        Am = -c * Am;
+      }
+      bA[kz] = Am;
+      bw[kz] = prev;
+    }
+  }
+  cl.sync();
+  if (P > 1) {
+    for (int base = 0; base < Nz * P; base += bd) {
+      const int w = base + t, kz = w / P, p = w % P;
+      const bool ok = kz < Nz;
+      const double* rA = cl.map_shared_rank(bA, p);
+      const double2* rw = cl.map_shared_rank(bw, p);
+      double Av = ok ? rA[kz] : 1.0;
+      double2 v = ok ? rw[kz] : make_double2(0.0, 0.0);
+      for (int off = 1; off < P; off <<= 1) {
+        const double Ao = __shfl_down_sync(full, Av, off, P);
+        const double bx = __shfl_down_sync(full, v.x, off, P), by = __shfl_down_sync(full, v.y, off, P);
+        if (p + off < P) { v.x = fma(Av, bx, v.x); v.y = fma(Av, by, v.y); Av *= Ao; }
+      }
+      double2 x;
+      x.x = __shfl_down_sync(full, v.x, 1, P);
+      x.y = __shfl_down_sync(full, v.y, 1, P);
+      if (p == P - 1) x = make_double2(0.0, 0.0);
+      if (ok && p == r) xin[kz] = x;
+    }
+  }
+  __syncthreads();
+  for (int kz = t; kz < Nz; kz += bd) {
+    const size_t mo = (size_t)kz * Nxh;
+    double2 prev = P > 1 ? xin[kz] : make_double2(0.0, 0.0);
+    for (int j = hi - 1; j >= lo; --j) {
+      double2 d = res[(j - lo) + (size_t)kz * nr];
+      const double c = LDG(fc + (size_t)j * ps + mo);
+      d.x = fma(-c, prev.x, d.x);        // c = 0 on the last row
+      d.y = fma(-c, prev.y, d.y);
+      prev = d;
+      res[(j - lo) + (size_t)kz * nr] = d;
+    }
+  }
+  double2* out = fft_smem(res, other, nr, 1, nr, Nz, T, true);
+  for (int w = t; w < nr * Nz; w += bd) {
+    const int l = w % nr, kz = w / nr;
+    spec[(size_t)(lo + l) * ps + (size_t)kz * Nxh] = out[l + (size_t)kz * nr];
+  }
+  cl.sync();   // no CTA leaves while another may still read its lane values
+}
+
 // ------------------------------------------------------------ inverse x -> pressure field
 __global__ void __launch_bounds__(256)
 k_fftx_inv(ChlMap map, int dst, int xmb) {
@@ -611,6 +780,31 @@ size_t chl_smem_tri(int maxNy, long modes, int mode) {
   return blocks <= per_sm * CHL_SMS ? b : 0;
 }
 int chl_tri_modes_per_block(size_t smem) { return smem ? TRI_W : 128; }
+// Fused z solve: shared memory of a CTA for an instance (0 if its block does
+// not fit, or its lane count is not a cluster size of 1, 2, 4 or 8), and its
+// launch: cluster (P, 1, 1), Nxh x P CTAs per instance.
+size_t chl_smem_zsolve(int Nx, int Ny, int Nz) {
+  const int Nxh = Nx / 2 + 1;
+  const int P = chl_tri_lanes((long)Nz * Nxh, Ny);
+  if (P != 1 && P != 2 && P != 4 && P != 8) return 0;
+  const int L = (Ny + P - 1) / P;
+  const size_t b = (size_t)2 * L * Nz * sizeof(double2) + (size_t)5 * Nz * sizeof(double2) + (size_t)2 * Nz * sizeof(double);
+  return b <= (size_t)227 * 1024 ? b : 0;
+}
+int chl_zsolve_setup(size_t smem) {
+  return cudaFuncSetAttribute(k_zsolve, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) == cudaSuccess ? 0 : 1;
+}
+void chl_launch_zsolve(const ChlMap& m, int nb, int P, size_t smem, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nb); cfg.blockDim = dim3(256); cfg.dynamicSmemBytes = smem; cfg.stream = st;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  at[1].id = cudaLaunchAttributeClusterDimension;
+  at[1].val.clusterDim.x = P; at[1].val.clusterDim.y = 1; at[1].val.clusterDim.z = 1;
+  cfg.attrs = at; cfg.numAttrs = 2;
+  cudaLaunchKernelEx(&cfg, k_zsolve, m);
+}
 void chl_launch_tri_scan(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_tri_scan, dim3(nb), dim3(128), 0, st, m); }
 void chl_launch_fftx_inv(const ChlMap& m, int nb, int nt, size_t smem, int dst, int xmb, cudaStream_t st) { chl_launch_pdl(k_fftx_inv, dim3(nb), dim3(nt), smem, st, m, dst, xmb); }
 void chl_launch_project(const ChlMap& m, int nb, int s, cudaStream_t st) { chl_launch_pdl(k_project, dim3(nb), dim3(m.tb), 0, st, m, s); }

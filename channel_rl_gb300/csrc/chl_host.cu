@@ -39,6 +39,9 @@ void chl_launch_div_fftx(const ChlMap&, int, int, size_t, int, int, int, cudaStr
 void chl_launch_fftz(const ChlMap&, int, int, size_t, int, int, cudaStream_t);
 void chl_launch_tri(const ChlMap&, int, size_t, cudaStream_t);
 void chl_launch_tri_scan(const ChlMap&, int, cudaStream_t);
+size_t chl_smem_zsolve(int, int, int);
+int chl_zsolve_setup(size_t);
+void chl_launch_zsolve(const ChlMap&, int, int, size_t, cudaStream_t);
 void chl_launch_fftx_inv(const ChlMap&, int, int, size_t, int, int, cudaStream_t);
 void chl_launch_project(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_pbc(const ChlMap&, int, int, cudaStream_t);
@@ -48,8 +51,8 @@ void chl_launch_unpack3(const ChlFields3&, int, int, cudaStream_t);
 void chl_launch_pack3(const ChlFields3&, int, int, cudaStream_t);
 void chl_launch_pack_unique(double*, const double*, int, int, int, int, int, cudaStream_t);
 void chl_launch_minabs(const ChlMap&, int, int, cudaStream_t);
+void chl_launch_minabs_init(const ChlMap&, cudaStream_t);
 void chl_launch_nonfinite(const ChlMap&, int, int, cudaStream_t);
-void chl_launch_dt(const ChlMap&, cudaStream_t);
 void chl_launch_massflow(const ChlMap&, cudaStream_t, int, int);
 void chl_launch_shift(const ChlMap&, int, int, cudaStream_t);
 void chl_launch_tadvance(const ChlMap&, cudaStream_t);
@@ -67,7 +70,7 @@ namespace {
 constexpr double RK_T[3] = {8.0 / 15.0, 2.0 / 3.0, 1.0};
 
 enum { M_PT, M_EDGE, M_FULL, M_DSMF, M_WALL, M_PLANE, M_FFTX, M_FFTZ, M_TRI, M_MINABS, M_ROWS, M_MLP, M_WALLN,
-       M_ZPLANE, NMAP };
+       M_ZPLANE, M_ZSOLVE, NMAP };
 constexpr int MLP_NPARAM = 4545;
 
 // Grid constants of one instance (host, FP64), in the device index
@@ -207,7 +210,10 @@ struct Arena {
   size_t take(size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; }
 };
 
-int dsm_npart(int Nx, int Ny, int Nz) { const int p = chl_dsm_ppt(Nx, Ny, Nz); return (Nx * Nz + 256 * p - 1) / (256 * p); }
+int dsm_npart(int Nx, int Ny, int Nz) {
+  const int p = chl_dsm_ppt(Nx, Ny, Nz);
+  return (Nx * Nz + CHL_DSMF_THREADS * p - 1) / (CHL_DSMF_THREADS * p);
+}
 
 }  // namespace
 
@@ -228,8 +234,14 @@ struct chl_handle {
   int zcw = 16;                       // kx columns per z-transform block
   int tx = 256, tz = 256;             // threads of the x and z transform blocks
   // projection tile shapes (chl_autotune): block-count targets of the x and
-  // z transforms and the tridiagonal form (chl_smem_tri's mode)
+  // z transforms and the tridiagonal form: 0 row-batched, 1 staged, 2 the
+  // default rule, 3 the fused z solve (z transform, tridiagonal and inverse
+  // z transform in one cluster launch; bit-identical to the others)
   int x_min_blocks = CHL_FFT_MIN_BLOCKS, z_min_blocks = CHL_FFT_MIN_BLOCKS, tri_mode = 2;
+  bool zsolve_ok = false;             // every instance has the same lane count and fits (chl_smem_zsolve)
+  bool zsolve = false;                // the fused form is in use
+  int zlanes = 1;                     // its cluster size
+  size_t smem_zs = 0;
   int tb_pt = 256;                    // threads per block of the point maps (stencils, updates)
   bool tri_scan = false;              // some instance splits its tridiagonal columns (chl_tri_lanes)
   int LES_model = 0, wall_model = 0, any_mass = 0;
@@ -297,6 +309,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   size_t o_part = A.take(8 * 2 * (size_t)(Ny + 2) * npart);
   size_t o_coef = A.take(8 * (Ny + 2)), o_scal = A.take(8 * CHL_S_NSCAL);
   size_t o_min = A.take(8 * (size_t)(Nx + Ny + 1 + Nz)), o_status = A.take(64);
+  size_t o_dcnt = A.take(4 * (size_t)(Ny + 2));
   size_t o_red = A.take(8 * 2 * (size_t)Nz);
   size_t o_trace = A.take(4 * (size_t)MLP_NPARAM);
   const bool mlp = I.d.wall_model == CHL_WM_MLP;
@@ -315,6 +328,13 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.fk[FK_ONE] = 1.0; D.fk[FK_MZERO] = -0.0; D.fk[FK_FOUR] = 4.0;
   D.nu = I.d.nu; D.CFL = I.d.CFL; D.Cs = I.d.Cs;
   D.dxmin = c.dxmin; D.dymin = c.dymin; D.dzmin = c.dzmin;
+  {
+    // the viscous limit of compute_dt, CFL*dxmin**2/nu (time_integration.f90:
+    // 131-134), in the reference's order of operations, once per instance
+    const double C = I.d.CFL, nu = I.d.nu;
+    const double vx = C * (c.dxmin * c.dxmin) / nu, vy = C * (c.dymin * c.dymin) / nu, vz = C * (c.dzmin * c.dzmin) / nu;
+    D.dt_vis = std::fmin(std::fmin(vx, vy), vz);
+  }
   D.dyw = c.yg[2] - c.yg[1];
   D.hb = c.yg[4] - c.yf[1];
   D.ht = c.yf[c.ny] - c.yg[c.nyg - 3];
@@ -348,6 +368,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.alpha = P(o_alpha); D.bc = P(o_bc); D.part = P(o_part); D.npart = npart; D.dsm_ppt = chl_dsm_ppt(Nx, Ny, Nz);
   D.coef = P(o_coef); D.scal = P(o_scal);
   D.minabs = (unsigned long long*)(base + o_min); D.red = P(o_red); D.status = (int*)(base + o_status);
+  D.dsm_cnt = (int*)(base + o_dcnt);
   D.retau = I.d.Re_tau;
   D.mlp_trace = (float*)(base + o_trace);
   D.mlp_theta = h->d_mlp_theta;
@@ -437,6 +458,18 @@ static int build_maps(chl_handle* h) {
   }
   h->tri_scan = false;
   for (auto& I : h->in) h->tri_scan = h->tri_scan || chl_tri_lanes((long)I.c.Nz * I.c.Nxh, I.c.Ny) > 1;
+  // fused z solve: needs one lane count for the whole launch (the cluster
+  // size) and every instance's row block in shared memory; by default it is
+  // used where the tridiagonal solve splits its columns (few modes)
+  h->zsolve_ok = true;
+  h->smem_zs = 0;
+  h->zlanes = chl_tri_lanes((long)h->in[0].c.Nz * h->in[0].c.Nxh, h->in[0].c.Ny);
+  for (auto& I : h->in) {
+    const size_t b = chl_smem_zsolve(I.c.Nx, I.c.Ny, I.c.Nz);
+    h->zsolve_ok = h->zsolve_ok && b > 0 && chl_tri_lanes((long)I.c.Nz * I.c.Nxh, I.c.Ny) == h->zlanes;
+    h->smem_zs = std::max(h->smem_zs, b);
+  }
+  h->zsolve = h->zsolve_ok && (h->tri_mode == 3 || (h->tri_mode == 2 && h->zlanes > 1));
   h->smem_t = h->tri_scan ? 0 : chl_smem_tri(my, modes, h->tri_mode);
   const int tri_w = chl_tri_modes_per_block(h->smem_t);
   for (int m = 0; m < NMAP; ++m) {
@@ -461,6 +494,7 @@ static int build_maps(chl_handle* h) {
         case M_MLP: b = cdiv(2L * Nx * Nz, 128); break;
         case M_WALLN: b = cdiv(2L * Nx * Nz, CHL_WALL_THREADS); break;
         case M_ZPLANE: b = Nz; break;
+        case M_ZSOLVE: b = Nxh * h->zlanes; break;
       }
       off[q + 1] = off[q] + b;
     }
@@ -476,6 +510,7 @@ static int build_maps(chl_handle* h) {
   h->smem_x = sx;
   h->smem_z = chl_smem_fftz(mz, h->zcw);
   if (chl_fft_setup(h->smem_x, h->smem_z, h->smem_t)) { h->err = "FFT shared-memory size not supported"; return CHL_E_ARG; }
+  if (h->zsolve && chl_zsolve_setup(h->smem_zs)) { h->err = "fused z solve: shared-memory size not supported"; return CHL_E_ARG; }
   if (chl_mlp_setup()) { h->err = "wall-model network shared-memory size not supported"; return CHL_E_ARG; }
   return CHL_OK;
 }
@@ -509,9 +544,9 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
   } else if (h->LES_model == CHL_LES_VREMAN) {
     KL("vreman", chl_launch_vreman(h->map(M_PT), h->nblk[M_PT], s, with_wm ? 1 : 0, st));
   }
-  // the row coefficient exists for the Smagorinsky models only
-  if (h->LES_model == CHL_LES_DYNAMIC || h->LES_model == CHL_LES_SMAGORINSKY)
-    KL("nut_coef", chl_launch_coef(h->map(M_PT), st));
+  // the static model's row coefficient (the dynamic model's is formed by
+  // the last block of each row of its plane sums)
+  if (h->LES_model == CHL_LES_SMAGORINSKY) KL("nut_coef", chl_launch_coef(h->map(M_PT), st));
   if (!fused) {
     wall_stress();
     KL("nut", chl_launch_nut(h->map(M_FULL), h->nblk[M_FULL], s, with_wm ? 1 : 0, st));
@@ -528,22 +563,28 @@ static int enqueue_projection(chl_handle* h, int s, int mode) {
   const bool correct = mode == 0;
   if (mode == 2) mode = 0;
   KL("div_fft_x", chl_launch_div_fftx(h->map(M_FFTX), h->nblk[M_FFTX], h->tx, h->smem_x, s, mode, h->x_min_blocks, st));
-  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->tz, h->smem_z, 0, h->zcw, st));
-  if (h->tri_scan) KL("tridiag", chl_launch_tri_scan(h->map(M_TRI), h->nblk[M_TRI], st));
-  else KL("tridiag", chl_launch_tri(h->map(M_TRI), h->nblk[M_TRI], h->smem_t, st));
-  KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->tz, h->smem_z, 1, h->zcw, st));
+  if (h->zsolve) {
+    KL("z_solve", chl_launch_zsolve(h->map(M_ZSOLVE), h->nblk[M_ZSOLVE], h->zlanes, h->smem_zs, st));
+  } else {
+    KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->tz, h->smem_z, 0, h->zcw, st));
+    if (h->tri_scan) KL("tridiag", chl_launch_tri_scan(h->map(M_TRI), h->nblk[M_TRI], st));
+    else KL("tridiag", chl_launch_tri(h->map(M_TRI), h->nblk[M_TRI], h->smem_t, st));
+    KL("fft_z", chl_launch_fftz(h->map(M_FFTZ), h->nblk[M_FFTZ], h->tz, h->smem_z, 1, h->zcw, st));
+  }
   KL("ifft_x", chl_launch_fftx_inv(h->map(M_FFTX), h->nblk[M_FFTX], h->tx, h->smem_x, mode == 0 ? 0 : 1, h->x_min_blocks, st));
   if (correct) KL("project", chl_launch_project(h->map(M_PT), h->nblk[M_PT], s, st));
   LAUNCHED();
   return CHL_OK;
 }
 
+// compute_dt: one launch.  k_minabs's last block per instance forms dt
+// (and resets the minima); with every instance on a fixed step only the
+// non-finite check runs, and it stores dt = -CFL.
 static int enqueue_dt(chl_handle* h) {
   bool fixed = true;   // every instance on a fixed step: only the non-finite check
   for (auto& I : h->in) fixed = fixed && I.d.CFL < 0.0;
   if (fixed) KL("dt_minabs", chl_launch_nonfinite(h->map(M_PT), h->nblk[M_PT], 0, h->st));
   else KL("dt_minabs", chl_launch_minabs(h->map(M_MINABS), h->nblk[M_MINABS], 0, h->st));
-  KL("dt", chl_launch_dt(h->map(M_PT), h->st));
   LAUNCHED();
   return CHL_OK;
 }
@@ -562,9 +603,10 @@ static int enqueue_rk3(chl_handle* h) {
   }
   if (h->any_mass) {
     KL("massflow", chl_launch_massflow(h->map(M_PT), h->st, 0, 0));
-    KL("massflow_shift", chl_launch_shift(h->map(M_PT), h->nblk[M_PT], 0, h->st));
+    KL("massflow_shift", chl_launch_shift(h->map(M_PT), h->nblk[M_PT], 0, h->st));   // and t += dt
+  } else {
+    KL("t_advance", chl_launch_tadvance(h->map(M_PT), h->st));
   }
-  KL("t_advance", chl_launch_tadvance(h->map(M_PT), h->st));
   LAUNCHED();
   (void)RK_T;
   return CHL_OK;
@@ -693,6 +735,9 @@ int chl_batch_create(int n, const chl_grid_desc* descs, chl_handle** out) {
   if (e != cudaSuccess) { h->err = "device allocation failed"; *out = h; return CHL_E_NOMEM; }
   int rc = build_maps(h);
   if (rc) { *out = h; return rc; }
+  chl_launch_minabs_init(h->map(M_PT), h->st);   // the minima start every step at their initial value
+  cudaError_t le = cudaGetLastError();
+  if (le != cudaSuccess) { h->err = std::string("CUDA launch: ") + cudaGetErrorString(le); *out = h; return CHL_E_CUDA; }
   *out = h;
   return finish(h);
 }
@@ -1122,16 +1167,19 @@ int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
     long modes = 0;
     for (auto& I : h->in) { my = std::max(my, I.c.Ny); modes += (long)I.c.Nz * I.c.Nxh; }
     const bool fits = !h->tri_scan && chl_smem_tri(my, modes, 1) > 0;
+    const bool fused = h->zsolve_ok;
     int best_v = 0;
     double best_t = 1e30;
-    for (int v = 0; v <= (fits ? 1 : 0); ++v) {
+    for (int v = 0; v <= 3; ++v) {
+      if ((v == 1 && !fits) || v == 2 || (v == 3 && !fused)) continue;
       h->tri_mode = v;
       if ((rc2 = time_group(h, 1, reps, ea, eb, &t))) return rc2;
       if (t < best_t) { best_t = t; best_v = v; }
     }
     h->tri_mode = best_v;
     std::snprintf(buf, sizeof buf, " tridiag %s (%.4f ms)",
-                  h->tri_scan ? "lane-split" : (best_v == 1 ? "staged" : "row-batched"), best_t);
+                  best_v == 3 ? "fused z solve" : (h->tri_scan ? "lane-split" : (best_v == 1 ? "staged" : "row-batched")),
+                  best_t);
     rep += buf;
   }
   if ((rc2 = build_maps(h))) return rc2;
@@ -1150,12 +1198,12 @@ int chl_autotune(chl_handle* h, int reps, char* report, int report_len) {
 int chl_get_tile_shapes(chl_handle* h, int* out7) {
   if (!h || !out7) return CHL_E_ARG;
   out7[0] = h->x_min_blocks; out7[1] = h->z_min_blocks; out7[2] = h->tri_mode; out7[3] = h->tb_pt;
-  out7[4] = h->zcw; out7[5] = h->tri_scan ? 2 : (h->smem_t ? 1 : 0); out7[6] = h->tx;
+  out7[4] = h->zcw; out7[5] = h->zsolve ? 3 : (h->tri_scan ? 2 : (h->smem_t ? 1 : 0)); out7[6] = h->tx;
   return CHL_OK;
 }
 
 int chl_set_tile_shapes(chl_handle* h, int x_min_blocks, int z_min_blocks, int tri_mode, int point_threads) {
-  if (!h || x_min_blocks < 1 || z_min_blocks < 1 || tri_mode < 0 || tri_mode > 2) return CHL_E_ARG;
+  if (!h || x_min_blocks < 1 || z_min_blocks < 1 || tri_mode < 0 || tri_mode > 3) return CHL_E_ARG;
   if (point_threads != 64 && point_threads != 128 && point_threads != 256) return CHL_E_ARG;
   h->x_min_blocks = x_min_blocks; h->z_min_blocks = z_min_blocks; h->tri_mode = tri_mode;
   h->tb_pt = point_threads;

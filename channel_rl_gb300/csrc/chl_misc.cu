@@ -94,11 +94,59 @@ __device__ __forceinline__ unsigned long long absbits(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFULL;
 }
 
-// Blocks per instance: Nz planes x MINABS_CHUNKS(Ny) row chunks.  Threads
-// run over x (coalesced); each keeps its own minimum of |U| at its x-face
-// and of |W|, and the per-row minimum of |V| is formed by warp shuffles.
-// Mins of non-negative doubles are mins of their bit patterns, so the
-// reductions are exact and order-free.
+// dt of one instance from the minima of |U|, |V|, |W| (compute_dt,
+// time_integration.f90:102-150), by one whole block of up to 1024 threads;
+// thread 0 stores it.  With a fixed time step (CFL < 0) the step is -CFL
+// whatever the velocities, so nothing is reduced.  The maxima are formed by
+// warp shuffles and one pass over the warps' results.  The minima are read
+// from L2 (other blocks formed them with atomics).
+__device__ __forceinline__ double warp_fmax(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+__device__ void dt_from_minima(const ChlInst& I) {
+  if (I.CFL < 0.0) {
+    if (threadIdx.x == 0) chl_put_dt(I.scal, -I.CFL);
+    return;
+  }
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const unsigned long long* g = I.minabs;
+  __shared__ double r[3][32];
+  double lu = 0.0, lv = 0.0, lw = 0.0;
+  // U: faces i_f = 2..nxg-1 (my 0..Nx, face Nx is the copy of face 0)
+  for (int i = threadIdx.x; i <= Nx; i += blockDim.x)
+    lu = fmax(lu, I.dxf[i] / __longlong_as_double((long long)__ldcg(g + (i == Nx ? 0 : i))));
+  // V: face rows j_f = 2..nyg-1 (my 1..Ny; row Ny is the wall, |V| = 0)
+  for (int j = 1 + threadIdx.x; j <= Ny; j += blockDim.x)
+    lv = fmax(lv, I.dyf[j] / __longlong_as_double((long long)__ldcg(g + Nx + j)));
+  // W: faces k_f = 2..nzg-1 (my 0..Nz)
+  for (int k = threadIdx.x; k <= Nz; k += blockDim.x)
+    lw = fmax(lw, I.dzf[k] / __longlong_as_double((long long)__ldcg(g + Nx + Ny + 1 + (k == Nz ? 0 : k))));
+  lu = warp_fmax(lu); lv = warp_fmax(lv); lw = warp_fmax(lw);
+  const int warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  if ((threadIdx.x & 31) == 0) { r[0][warp] = lu; r[1][warp] = lv; r[2][warp] = lw; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < nw; ++w) {
+      lu = fmax(lu, r[0][w]); lv = fmax(lv, r[1][w]); lw = fmax(lw, r[2][w]);
+    }
+    const double C = I.CFL;
+    const double dt_conv = fmin(fmin(C * lu, C * lv), C * lw);
+    double dt = fmin(dt_conv, I.dt_vis);
+    dt = fmin(dt, 1e-3);
+    chl_put_dt(I.scal, dt);
+  }
+}
+
+// Blocks per instance: Nz planes x MINABS_CHUNKS(Ny) row chunks.  The
+// block's threads run over (x, row) with x fastest in whole warps (x padded
+// to a multiple of 32), so a warp covers 32 x-points of one row and every
+// warp of the block has work even when Nx is 32.  Each thread keeps its
+// minima of |U| at its x-face and of |W|; the per-row minimum of |V| is
+// formed by warp shuffles.  Mins of non-negative doubles are mins of their
+// bit patterns, so the reductions are exact and order-free.
 #define MINABS_ROWS 16
 __device__ __forceinline__ int minabs_chunks(int Ny) { return (Ny + MINABS_ROWS - 1) / MINABS_ROWS; }
 
@@ -121,28 +169,32 @@ k_minabs(ChlMap map, int s) {
   unsigned long long mw = CHL_BIG_BITS;
   bool bad = false;                      // a non-finite velocity (|x| bits >= those of inf)
   const int nxr = (Nx + 31) & ~31;       // whole warps take part in the shuffles
-  for (int i = threadIdx.x; i < nxr; i += blockDim.x) {
+  const int nw = nxr * (j1 - j0 + 1);    // a multiple of 32: loop exits are warp-uniform
+  // a thread's x is the same in every iteration when the block size is a
+  // multiple of the padded row: its U minimum then goes out once at the end
+  const bool fixed_x = blockDim.x % nxr == 0;
+  unsigned long long mu = CHL_BIG_BITS;
+  for (int w = threadIdx.x; w < nw; w += blockDim.x) {
+    const int i = w % nxr, jc = j0 + w / nxr;
     const bool ok = i < Nx;
-    unsigned long long mu = CHL_BIG_BITS;
-    for (int jc = j0; jc <= j1; ++jc) {
-      unsigned long long bv = CHL_BIG_BITS;
-      if (ok) {
-        const unsigned long long bu = absbits(U[cidx(I, i, jc, k)]);
-        const unsigned long long bw = absbits(W[cidx(I, i, jc, k)]);
-        bv = absbits(V[vidx(I, i, jc, k)]);
-        mu = bu < mu ? bu : mu;
-        mw = bw < mw ? bw : mw;
-        bad |= (bu >= CHL_BIG_BITS) | (bw >= CHL_BIG_BITS) | (bv >= CHL_BIG_BITS);
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long x = __shfl_xor_sync(0xffffffffu, bv, o);
-        bv = x < bv ? x : bv;
-      }
-      if (lane == 0) atomicMin(sv + (jc - j0), bv);
+    unsigned long long bv = CHL_BIG_BITS;
+    if (ok) {
+      const unsigned long long bu = absbits(U[cidx(I, i, jc, k)]);
+      const unsigned long long bw = absbits(W[cidx(I, i, jc, k)]);
+      bv = absbits(V[vidx(I, i, jc, k)]);
+      mu = bu < mu ? bu : mu;
+      mw = bw < mw ? bw : mw;
+      bad |= (bu >= CHL_BIG_BITS) | (bw >= CHL_BIG_BITS) | (bv >= CHL_BIG_BITS);
     }
-    if (ok) atomicMin(g + i, mu);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long x = __shfl_xor_sync(0xffffffffu, bv, o);
+      bv = x < bv ? x : bv;
+    }
+    if (lane == 0) atomicMin(sv + (jc - j0), bv);
+    if (!fixed_x && ok) { atomicMin(g + i, mu); mu = CHL_BIG_BITS; }
   }
+  if (fixed_x && (int)(threadIdx.x % nxr) < Nx && (int)threadIdx.x < nw) atomicMin(g + threadIdx.x % nxr, mu);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     const unsigned long long x = __shfl_xor_sync(0xffffffffu, mw, o);
@@ -157,6 +209,21 @@ k_minabs(ChlMap map, int s) {
     atomicMin(g + Nx + Ny + 1 + k, m);
   }
   if (threadIdx.x <= j1 - j0) atomicMin(g + Nx + j0 + threadIdx.x, sv[threadIdx.x]);
+  // the instance's last block to finish forms dt from the minima and
+  // resets them for the next step
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(I.status + CHL_CNT_DT, 1) == I.Nz * nch - 1;
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    dt_from_minima(I);
+    __syncthreads();
+    const int n = Nx + Ny + 1 + I.Nz;
+    for (int w = threadIdx.x; w < n; w += blockDim.x) g[w] = CHL_BIG_BITS;
+    if (threadIdx.x == 0) I.status[CHL_CNT_DT] = 0;
+  }
 }
 
 // With a fixed time step the minima are not needed (compute_dt reduces them
@@ -170,6 +237,7 @@ k_nonfinite(ChlMap map, int s) {
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
   const long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t == 0) chl_put_dt(I.scal, -I.CFL);   // fixed step (compute_dt, time_integration.f90:146-148)
   bool bad = false;
   if (t < (long)Nx * Ny * Nz) {
     const int i = (int)(t % Nx);
@@ -188,54 +256,6 @@ __global__ void k_minabs_init(ChlMap map) {
   const ChlInst& I = map.inst[blockIdx.x];
   const int n = I.Nx + I.Ny + 1 + I.Nz;
   for (int w = threadIdx.x; w < n; w += blockDim.x) I.minabs[w] = CHL_BIG_BITS;
-}
-
-// One block of 128 threads per instance.  With a fixed time step (CFL < 0)
-// the step is -CFL whatever the velocities, so nothing is reduced.  The
-// maxima are formed by warp shuffles and one pass over the four warps'
-// results (a serial pass over 128 entries costs more than the whole rest).
-__device__ __forceinline__ double warp_fmax(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-  return v;
-}
-
-__global__ void __launch_bounds__(128)
-k_dt(ChlMap map) {
-  chl_pdl_wait();
-  const ChlInst& I = map.inst[blockIdx.x];
-  if (I.CFL < 0.0) {
-    if (threadIdx.x == 0) chl_put_dt(I.scal, -I.CFL);
-    return;
-  }
-  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  const unsigned long long* g = I.minabs;
-  __shared__ double r[3][4];
-  double lu = 0.0, lv = 0.0, lw = 0.0;
-  // U: faces i_f = 2..nxg-1 (my 0..Nx, face Nx is the copy of face 0)
-  for (int i = threadIdx.x; i <= Nx; i += blockDim.x)
-    lu = fmax(lu, I.dxf[i] / __longlong_as_double((long long)g[i == Nx ? 0 : i]));
-  // V: face rows j_f = 2..nyg-1 (my 1..Ny; row Ny is the wall, |V| = 0)
-  for (int j = 1 + threadIdx.x; j <= Ny; j += blockDim.x)
-    lv = fmax(lv, I.dyf[j] / __longlong_as_double((long long)g[Nx + j]));
-  // W: faces k_f = 2..nzg-1 (my 0..Nz)
-  for (int k = threadIdx.x; k <= Nz; k += blockDim.x)
-    lw = fmax(lw, I.dzf[k] / __longlong_as_double((long long)g[Nx + Ny + 1 + (k == Nz ? 0 : k)]));
-  lu = warp_fmax(lu); lv = warp_fmax(lv); lw = warp_fmax(lw);
-  const int warp = threadIdx.x >> 5;
-  if ((threadIdx.x & 31) == 0) { r[0][warp] = lu; r[1][warp] = lv; r[2][warp] = lw; }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    for (int w = 1; w < 4; ++w) {
-      lu = fmax(lu, r[0][w]); lv = fmax(lv, r[1][w]); lw = fmax(lw, r[2][w]);
-    }
-    const double C = I.CFL, nu = I.nu;
-    const double dt_conv = fmin(fmin(C * lu, C * lv), C * lw);
-    const double dt_vis = fmin(fmin(C * I.dxmin * I.dxmin / nu, C * I.dymin * I.dymin / nu), C * I.dzmin * I.dzmin / nu);
-    double dt = fmin(dt_conv, dt_vis);
-    dt = fmin(dt, 1e-3);
-    chl_put_dt(I.scal, dt);
-  }
 }
 
 // ------------------------------------------------------------ constant mass flow
@@ -270,6 +290,13 @@ __global__ void k_massflow(ChlMap map, int s, int force) {
   }
 }
 
+__device__ __forceinline__ void time_advance(const ChlInst& I) {
+  I.scal[CHL_S_T] = I.scal[CHL_S_T] + 1.0 * I.scal[CHL_S_DT];
+}
+
+// The shift of the constant-mass-flow instances, and the time advance of
+// every instance (its first block; k_tadvance's work when no instance of
+// the batch has a constant mass flow and the shift is not launched).
 __global__ void __launch_bounds__(256)
 k_shift(ChlMap map, int s) {
   chl_pdl_wait();
@@ -277,6 +304,11 @@ k_shift(ChlMap map, int s) {
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
   long t = (long)lb * blockDim.x + threadIdx.x;
+  if (t == 0) {
+    time_advance(I);
+    // step counter of the wall-model exploration noise (shared by the batch)
+    if (blockIdx.x == 0 && I.mlp_cfg) atomicAdd(I.mlp_cfg + 4, 1u);
+  }
   if (t >= (long)Nx * Ny * Nz) return;
   const int i = (int)(t % Nx), jc = 1 + (int)((t / Nx) % Ny), k = (int)(t / ((long)Nx * Ny));
   if (!I.x_mass_cte) return;
@@ -292,7 +324,7 @@ k_shift(ChlMap map, int s) {
 __global__ void k_tadvance(ChlMap map) {
   chl_pdl_wait();
   const ChlInst& I = map.inst[blockIdx.x];
-  if (threadIdx.x == 0) I.scal[CHL_S_T] = I.scal[CHL_S_T] + 1.0 * I.scal[CHL_S_DT];
+  if (threadIdx.x == 0) time_advance(I);
   // step counter of the wall-model exploration noise (shared by the batch)
   if (blockIdx.x == 0 && threadIdx.x == 0 && I.mlp_cfg) atomicAdd(I.mlp_cfg + 4, 1u);
 }
@@ -383,15 +415,19 @@ __global__ void k_qflow_final(const ChlInst* inst, int slot) {
 }
 
 extern "C" {
-void chl_launch_minabs(const ChlMap& m, int nb, int s, cudaStream_t st) {
+// the minima hold CHL_BIG_BITS between steps: set once here when an
+// instance is created, then by the block of k_minabs that forms dt
+void chl_launch_minabs_init(const ChlMap& m, cudaStream_t st) {
   chl_launch_pdl(k_minabs_init, dim3(m.n), dim3(128), 0, st, m);
+}
+// compute_dt: the minima and, in the instance's last block, dt itself
+void chl_launch_minabs(const ChlMap& m, int nb, int s, cudaStream_t st) {
   chl_launch_pdl(k_minabs, dim3(nb), dim3(256), 0, st, m, s);
 }
 // nb: blocks of 256 centres (the point map)
 void chl_launch_nonfinite(const ChlMap& m, int nb, int s, cudaStream_t st) {
   chl_launch_pdl(k_nonfinite, dim3(nb), dim3(m.tb), 0, st, m, s);
 }
-void chl_launch_dt(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_dt, dim3(m.n), dim3(128), 0, st, m); }
 void chl_launch_massflow(const ChlMap& m, cudaStream_t st, int s, int force) { chl_launch_pdl(k_massflow, dim3(m.n), dim3(256), 0, st, m, s, force); }
 void chl_launch_shift(const ChlMap& m, int nb, int s, cudaStream_t st) { chl_launch_pdl(k_shift, dim3(nb), dim3(m.tb), 0, st, m, s); }
 void chl_launch_tadvance(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_tadvance, dim3(m.n), dim3(32), 0, st, m); }

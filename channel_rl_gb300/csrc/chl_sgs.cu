@@ -245,10 +245,39 @@ k_filter_xz(ChlMap map, int from_r) {
 }
 
 // ------------------------------------------------------------ L:M, M:M
-// One block per (centre row jc, chunk of the x-z plane); each thread sums its
-// points in a fixed order, then a fixed-order block reduction writes
-// part[0|1][jc][chunk].  Filtered fields live in r after the three passes.
-__global__ void __launch_bounds__(256)
+// One block of CHL_DSMF_THREADS per (centre row jc, chunk of the x-z plane);
+// each thread sums its points in a fixed order, then a fixed-order block
+// reduction writes part[0|1][jc][chunk].  Filtered fields live in r after
+// the three passes.  The last block of a row to finish (a counter per row)
+// adds the row's partials - thread t the chunks t, t + CHL_DSMF_THREADS, ...
+// in order, then the same block tree - and writes the row's coefficient
+// -1/2 <LM>/<MM>, then returns the counter to 0.
+__device__ __forceinline__ void block_sum2(double* sl, double* sm, double& a, double& b) {
+  sl[threadIdx.x] = a; sm[threadIdx.x] = b;
+  __syncthreads();
+  for (int w = CHL_DSMF_THREADS / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) { sl[threadIdx.x] += sl[threadIdx.x + w]; sm[threadIdx.x] += sm[threadIdx.x + w]; }
+    __syncthreads();
+  }
+  a = sl[0]; b = sm[0];
+}
+
+// -1/2 <LM>/<MM>: the filter and average scales give 1/8 (see the scaling
+// note above); L and M are both stored / 216, so <LM>/<MM> = lm/mm (times
+// the sqrt(2) that the strain leaves out).  Whole block; every thread gets it.
+__device__ __forceinline__ double dsm_row_coef(const ChlInst& I, int jc, double* sl, double* sm) {
+  const int np = I.npart, Ny = I.Ny;
+  double lm = 0.0, mm = 0.0;
+  for (int q = threadIdx.x; q < np; q += CHL_DSMF_THREADS) {
+    lm += __ldcg(I.part + (size_t)jc * np + q);
+    mm += __ldcg(I.part + (size_t)(Ny + 2) * np + (size_t)jc * np + q);
+  }
+  __syncthreads();
+  block_sum2(sl, sm, lm, mm);
+  return -0.125 * (lm / mm);
+}
+
+__global__ void __launch_bounds__(CHL_DSMF_THREADS)
 k_dsm_final(ChlMap map) {
   chl_pdl_wait();
   int lb;
@@ -261,7 +290,7 @@ k_dsm_final(ChlMap map) {
   const double* const* R = I.r;
   const int ppt = I.dsm_ppt;
   for (int m = 0; m < ppt; ++m) {
-    const int pidx = chunk * (256 * ppt) + m * 256 + threadIdx.x;
+    const int pidx = chunk * (CHL_DSMF_THREADS * ppt) + m * CHL_DSMF_THREADS + threadIdx.x;
     if (pidx >= plane) break;
     const int i = pidx % Nx, k = pidx / Nx;
     const size_t c = cidx(I, i, jc, k);
@@ -300,38 +329,35 @@ k_dsm_final(ChlMap map) {
     lm = fma(wgt, lmp, lm);
     mm = fma(wgt, mmp, mm);
   }
-  __shared__ double sl[256], sm[256];
-  sl[threadIdx.x] = lm; sm[threadIdx.x] = mm;
-  __syncthreads();
-  for (int w = 128; w > 0; w >>= 1) {
-    if (threadIdx.x < w) { sl[threadIdx.x] += sl[threadIdx.x + w]; sm[threadIdx.x] += sm[threadIdx.x + w]; }
-    __syncthreads();
-  }
+  __shared__ double sl[CHL_DSMF_THREADS], sm[CHL_DSMF_THREADS];
+  __shared__ int last;
+  block_sum2(sl, sm, lm, mm);
   if (threadIdx.x == 0) {
-    I.part[(size_t)jc * np + chunk] = sl[0];
-    I.part[(size_t)(Ny + 2) * np + (size_t)jc * np + chunk] = sm[0];
+    I.part[(size_t)jc * np + chunk] = lm;
+    I.part[(size_t)(Ny + 2) * np + (size_t)jc * np + chunk] = mm;
+    __threadfence();
+    last = atomicAdd(I.dsm_cnt + jc, 1) == np - 1;     // the row's last block
+  }
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    const double c = dsm_row_coef(I, jc, sl, sm);
+    if (threadIdx.x == 0) { I.coef[jc] = c; I.dsm_cnt[jc] = 0; }
   }
 }
 
 // ------------------------------------------------------------ nu_t coefficient per row
+// The static model's row coefficient (the dynamic model's is written by
+// k_dsm_final, and this kernel leaves it alone).
 __global__ void k_coef(ChlMap map) {
   chl_pdl_wait();
   const ChlInst& I = map.inst[blockIdx.x];
-  const int Ny = I.Ny, np = I.npart;
+  const int Ny = I.Ny;
+  if (I.LES_model == 2) return;
   for (int jc = threadIdx.x; jc < Ny + 2; jc += blockDim.x) {
     double c = 0.0;
     if (jc >= 1 && jc <= Ny) {
-      if (I.LES_model == 2) {
-        double lm = 0.0, mm = 0.0;
-        for (int q = 0; q < np; ++q) {
-          lm += I.part[(size_t)jc * np + q];
-          mm += I.part[(size_t)(Ny + 2) * np + (size_t)jc * np + q];
-        }
-        // -1/2 <LM>/<MM>: the filter and average scales give 1/8 (see the
-        // scaling note above); L and M are both stored / 216, so
-        // <LM>/<MM> = lm/mm (times the sqrt(2) that the strain leaves out)
-        c = -0.125 * (lm / mm);
-      } else if (I.LES_model == 1) {
+      if (I.LES_model == 1) {
         // van Driest: f = 1 - exp(-d/25/(nu/utau)), utau = dPdx^0.5 (subgrid.f90:581-599)
         const double ut = sqrt(I.scal[CHL_S_DPDX]);
         double f = 1.0 - exp(-I.smag_dwall[jc] / 25.0 / (I.nu / ut));
@@ -453,7 +479,9 @@ void chl_launch_centre(const ChlMap& m, int nb, int s_in, int dsm, cudaStream_t 
 void chl_launch_filter_y(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_filter_y, dim3(nb), dim3(m.tb), 0, st, m, s_in); }
 void chl_launch_filter_x(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<0>, dim3(nb), dim3(m.tb), 0, st, m, 1); }
 void chl_launch_filter_z(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<1>, dim3(nb), dim3(m.tb), 0, st, m, 0); }
-void chl_launch_dsm_final(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_dsm_final, dim3(nb), dim3(256), 0, st, m); }
+void chl_launch_dsm_final(const ChlMap& m, int nb, cudaStream_t st) {
+  chl_launch_pdl(k_dsm_final, dim3(nb), dim3(CHL_DSMF_THREADS), 0, st, m);
+}
 void chl_launch_coef(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_coef, dim3(m.n), dim3(128), 0, st, m); }
 void chl_launch_eqwm(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_eqwm, dim3(nb), dim3(CHL_WALL_THREADS), 0, st, m, s_in); }
 void chl_launch_nut(const ChlMap& m, int nb, int s_in, int use_wm, cudaStream_t st) { chl_launch_pdl(k_nut, dim3(nb), dim3(m.tb), 0, st, m, s_in, use_wm); }

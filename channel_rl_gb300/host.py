@@ -489,7 +489,7 @@ class Channel:
 
     def tile_shapes(self):
         """{x_min_blocks, z_min_blocks, tri_mode, point_threads, z_cols, tri_form, x_threads};
-        tri_form 0 row-batched, 1 staged, 2 lane-split."""
+        tri_form 0 row-batched, 1 staged, 2 lane-split, 3 fused z solve."""
         v = (C.c_int * 7)()
         self._check(self.lib.chl_get_tile_shapes(self.h, v), "chl_get_tile_shapes")
         keys = ("x_min_blocks", "z_min_blocks", "tri_mode", "point_threads", "z_cols", "tri_form", "x_threads")

@@ -176,12 +176,17 @@ int chl_autotune(chl_handle* h, int reps, char* report, int report_len);
 /* The current tile shapes: out7 = {x_min_blocks, z_min_blocks, tri_mode,
  * point_threads, z columns per block, tridiagonal form in use (0
  * row-batched, 1 staged in shared memory, 2 lane-split for instances with
- * few modes - chosen from the instances' extents, not tuned), x-transform
- * threads}. */
+ * few modes - chosen from the instances' extents, not tuned, 3 the fused z
+ * solve: forward z transform, tridiagonal solve and inverse z transform in
+ * one launch of thread-block clusters, one cluster per (instance, kx)),
+ * x-transform threads}. */
 int chl_get_tile_shapes(chl_handle* h, int* out7);
 /* Sets the tile shapes by hand: block-count targets >= 1; tri_mode 0
- * row-batched, 1 staged where it fits, 2 the default rule; point_threads
- * 64, 128 or 256. */
+ * row-batched, 1 staged where it fits, 2 the default rule (the fused z
+ * solve where the columns are split into lanes and every instance of the
+ * handle has the same lane count and fits, else staged while one wave holds
+ * all modes), 3 the fused z solve wherever it applies; point_threads 64,
+ * 128 or 256.  Every choice gives bit-identical results. */
 int chl_set_tile_shapes(chl_handle* h, int x_min_blocks, int z_min_blocks, int tri_mode, int point_threads);
 
 /* Learned wall model (CHL_WM_MLP).  Counterpart of the smarties policy that

@@ -18,7 +18,7 @@ WORKLOADS = {
     "uneven_batch": lambda: [C.smaller(C.c2_wm64(), 32, 16, 16), C.smaller(C.c3_roofline(les=C.LES_DSM), 48, 24, 36),
                              replace(C.smaller(C.rl_case(), 24, 10, 12), name="b2", LES_model=C.LES_DSM)],
 }
-FORCED = ((1, 1, 0, 64), (1, 1, 1, 128), (16 * 152, 16 * 152, 1, 256), (16 * 152, 1, 0, 64))
+FORCED = ((1, 1, 0, 64), (1, 1, 1, 128), (16 * 152, 16 * 152, 1, 256), (16 * 152, 1, 0, 64), (152, 152, 3, 128))
 STEPS = 3
 
 
@@ -79,7 +79,7 @@ def test_tuned_and_forced_shapes_are_bit_identical(name):
     out, info, report = runs["tuned"]
     assert "point_threads" in report and "x_min_blocks" in report and "tridiag" in report
     assert info["x_min_blocks"] in (1, 152, 304, 608, 1216, 2432)
-    assert info["point_threads"] in (64, 128, 256) and info["tri_mode"] in (0, 1)
+    assert info["point_threads"] in (64, 128, 256) and info["tri_mode"] in (0, 1, 3)
 
 
 def test_autotune_needs_fields():

@@ -273,3 +273,28 @@ def test_non_finite_instance_is_isolated_in_a_batch():
             assert np.array_equal(a[f], b[f]), (q, f)
         ch.close()
     chb.close()
+
+
+def test_viscous_limit_of_dt():
+    """compute_dt's viscous limit CFL*dymin**2/nu (time_integration.f90:131-137)
+    binding: a viscous small channel (nu = 0.2 on a stretched 16x24x16 mesh)
+    where it lies below both the convective limit and the 1e-3 cap.  dt equals
+    the oracle's bit for bit over three steps."""
+    case = replace(C.smaller(C.c1_small(), 16, 24, 16), nu=0.2)
+    U, V, W = C.initial_fields(case)
+    o = oracle_for(case)
+    o.set_fields(U, V, W)
+    g = o.g
+    vis = min(case.CFL * g.dxmin ** 2.0 / case.nu, case.CFL * g.dymin ** 2.0 / case.nu,
+              case.CFL * g.dzmin ** 2.0 / case.nu)
+    ch = _channel(case)
+    ch.upload(U, V, W)
+    for s in range(3):
+        o.step()
+        ch.step(1)
+        assert o.dt == vis < 1e-3, (o.dt, vis)
+        assert ch.scalars()["dt"] == o.dt, s
+    d = ch.download(fields=("U", "V", "W"))
+    for f, e in _cmp_fields(d, o).items():
+        assert e < FIELD_RTOL, (f, e)
+    ch.close()
