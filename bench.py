@@ -69,6 +69,7 @@ KERNEL_BYTES = {
     "project": 8 * 7.0,
     "massflow_shift": 8 * 2.0,
     "dt_minabs": 8 * 3.0,
+    "z_solve": 8 * 3.5,          # half spectrum in and out (8 B per point each), tridiagonal factors (12 B)
     "amd": 8 * 4.0,              # U, V, W in, nu_t out
     "vreman": 8 * 4.0,           # U, V, W in, nu_t out
 }
@@ -336,7 +337,7 @@ def roofline_of(args, prof, points, step_ms, workload_name):
     peaks = load_json(os.path.join(HERE, "MEASURED_PEAKS.json"), {})
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     hbm_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
-    fp64 = load_json(os.path.join(HERE, "profiles", "fp64_peak.json"), {})
+    fp64 = live_fp64_peak() or load_json(os.path.join(HERE, "profiles", "fp64_peak.json"), {})
     traffic = load_json(os.path.join(HERE, "profiles", "kernel_traffic.json"), {})
     byt = KERNEL_BYTES.get(dom, 0.0) * points
     ach = byt / per_launch_s / 1e9
@@ -348,6 +349,10 @@ def roofline_of(args, prof, points, step_ms, workload_name):
     hbm["step_hbm_gbs_vs_fused_minimum"] = 8 * STEP_STREAMS[sgs] * points / (step_ms * 1e-3) / 1e9
     fl = (traffic or {}).get("fp64_instr_per_point", {}).get(workload_name, {})
     peak_gops = fp64.get("fp64_peak_gops")
+    peak_src = ("measured live on this GPU before the timed steps (bench_peaks.cu fp64: best FP64 issue rate, "
+                "a DFMA loop on register operands)" if fp64.get("live") else
+                "measured on this pool's GB300 (profiles/fp64_peak.json from bench.py --measure-peaks: best FP64 "
+                "issue rate, a DFMA loop on register operands)")
     if not (peak_gops and dom in fl):
         return hbm
     achf = fl[dom] * points / per_launch_s / 1e9
@@ -358,8 +363,7 @@ def roofline_of(args, prof, points, step_ms, workload_name):
            "fp64_instr_per_point": fl[dom],
            "step_achieved": step_ach, "step_frac": step_ach / peak_gops,
            "step_fp64_instr_per_point": step_instr / points,
-           "peak_source": "measured on this pool's GB300 (profiles/fp64_peak.json from bench.py --measure-peaks: "
-                          "best FP64 issue rate, a DFMA loop on register operands)"}
+           "peak_source": peak_src}
     if f64["frac"] >= hbm["frac"]:
         f64["hbm"] = hbm
         return f64
@@ -610,6 +614,30 @@ def _barrier_record(out):
     res["how"] = ("bench_peaks.cu barrier: 49152-double update per phase; 2000 phases in one cooperative kernel "
                   "(grid barrier: arrival counter and generation word) vs 200 kernels in one CUDA graph, CUDA events")
     return res
+
+
+_LIVE_FP64 = None
+
+
+def live_fp64_peak():
+    """The FP64 issue rates of this GPU from bench_peaks.cu, run once per
+    process (about a second of GPU time), or None where the probe binary was
+    not built."""
+    global _LIVE_FP64
+    if _LIVE_FP64 is None:
+        _LIVE_FP64 = {}
+        try:
+            from channel_rl_gb300 import build as b
+            exe = b.PEAKS_BIN
+            if os.path.exists(exe):
+                out = subprocess.run([exe, "fp64"], check=True, capture_output=True, text=True, timeout=120).stdout
+                rec = _fp64_record(out)
+                if rec.get("fp64_peak_gops"):
+                    rec["live"] = True
+                    _LIVE_FP64 = rec
+        except Exception:
+            _LIVE_FP64 = {}
+    return _LIVE_FP64 or None
 
 
 def measure_peaks():

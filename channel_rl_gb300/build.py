@@ -76,5 +76,27 @@ def build(force: bool = False, verbose: bool = False, extra=None, variant=None) 
     return lib
 
 
+PEAKS_SRC = os.path.join(HERE, "..", "bench_peaks.cu")
+PEAKS_BIN = os.path.join(OUT, "bench_peaks")
+
+
+def build_peaks(force: bool = False) -> str:
+    """The peak probes of bench.py (bench_peaks.cu at the repository root),
+    next to the library: bench.py measures the FP64 issue rate of the GPU it
+    runs on with them.  Returns the binary's path, or "" where the source is
+    absent."""
+    if not os.path.exists(PEAKS_SRC):
+        return ""
+    if not force and os.path.exists(PEAKS_BIN) and os.path.getmtime(PEAKS_BIN) >= os.path.getmtime(PEAKS_SRC):
+        return PEAKS_BIN
+    os.makedirs(OUT, exist_ok=True)
+    cmd = [nvcc(), *ARCH, "-O3", "-o", PEAKS_BIN + ".tmp", PEAKS_SRC]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for bench_peaks.cu:\n{r.stderr}")
+    os.replace(PEAKS_BIN + ".tmp", PEAKS_BIN)
+    return PEAKS_BIN
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
