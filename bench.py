@@ -11,7 +11,9 @@ iteration of the reference's solver loop: compute_dt + compute_time_step_RK3
           stream), fields resident in HBM; per-step working set >> L2.
   e2e     same metric through the C ABI with host buffers: every step uploads
           U, V, W from pinned host memory (chl_set_fields), steps, and reads
-          U, V, W back (chl_download_async), timed on the host clock.
+          U, V, W back (chl_download_async), timed on the host clock; the
+          library's copy streams overlap each step's copies with the
+          neighbouring steps, and the host synchronises once at the end.
   --impl reference
           the reference algorithm on all host cores: the oracle's C++/OpenMP
           restatement of the step (the Fortran reference cannot be built: no
@@ -547,21 +549,28 @@ def e2e_rate(ch, case, args):
         ch.download_async(out[0][1], out[1][1], out[2][1])
     ch.synchronize()
     n = max(1, args.e2e_steps)
+    # every step copies its inputs in and its result out; the library runs
+    # the copies on its copy streams, so one step's upload and the previous
+    # step's download overlap the step in between; the host waits for all of
+    # it once, at the end of the timed region
     t0 = time.perf_counter()
     for _ in range(n):
         ch.set_fields_ptr(pin[0][1], pin[1][1], pin[2][1])
         ch.step(1)
         ch.download_async(out[0][1], out[1][1], out[2][1])
-        ch.synchronize()
+    ch.synchronize()
     secs = time.perf_counter() - t0
     out = {"value": case.points * n / secs, "unit": UNIT, "h2d_bytes_per_step": hb, "d2h_bytes_per_step": hb,
            "steps": n, "ms_per_step": 1e3 * secs / n,
-           "path": "chl_set_fields + chl_rk3_step + chl_download_async, pinned host U,V,W"}
+           "path": "chl_set_fields + chl_rk3_step + chl_download_async per step, pinned host U,V,W; copies on the "
+                   "library's copy streams overlap the neighbouring steps; one chl_synchronize at the end"}
     c2c = load_json(os.path.join(HERE, "profiles", "c2c_bandwidth.json"), {})
     if c2c.get("memcpy_h2d_gbs") and c2c.get("memcpy_d2h_gbs"):
-        # the copies cannot overlap the step they feed or read: their time is a floor
-        out["transfer_floor_ms_per_step"] = 1e3 * (hb / (c2c["memcpy_h2d_gbs"] * 1e9) + hb / (c2c["memcpy_d2h_gbs"] * 1e9))
-        out["transfer_floor_source"] = "profiles/c2c_bandwidth.json (measured pinned-copy bandwidth)"
+        # the copies run beside the neighbouring steps; their time per step
+        # (the two directions use separate copy engines) is the floor when it
+        # exceeds the step's own
+        out["transfer_ms_per_step"] = 1e3 * max(hb / (c2c["memcpy_h2d_gbs"] * 1e9), hb / (c2c["memcpy_d2h_gbs"] * 1e9))
+        out["transfer_source"] = "profiles/c2c_bandwidth.json (measured pinned-copy bandwidth)"
     return out
 
 

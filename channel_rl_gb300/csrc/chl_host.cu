@@ -200,8 +200,11 @@ struct Inst {
   ChlInst dev{};
   void* arena = nullptr;
   bool uploaded = false;
-  double* staging = nullptr;   // Fortran-layout staging (largest field)
+  double* staging = nullptr;   // Fortran-layout staging: 3 fields in, then 3 fields out
   size_t nstage = 0;
+  // ordering of the host-buffer round trip (chl_set_fields, chl_download_async)
+  // between the compute stream and the two copy streams; created on first use
+  cudaEvent_t ev_h2d = nullptr, ev_unpacked = nullptr, ev_packed = nullptr, ev_d2h = nullptr;
 };
 
 struct Arena {
@@ -227,6 +230,10 @@ struct chl_handle {
   std::vector<ProfRec> rec;
   ChlInst* d_inst = nullptr;
   cudaStream_t st = nullptr;
+  // copy streams of the host-buffer round trip: the next step's upload and
+  // the previous step's download run on the copy engines while a step
+  // computes (created on the first chl_set_fields / chl_download_async)
+  cudaStream_t st_h2d = nullptr, st_d2h = nullptr;
   std::string err;
   int* d_off[NMAP] = {};
   int nblk[NMAP] = {};
@@ -315,7 +322,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   const bool mlp = I.d.wall_model == CHL_WM_MLP;
   size_t o_rec = mlp ? A.take(4 * (size_t)CHL_MLP_REC * 3 * 2 * Nx * Nz) : 0;
   I.nstage = (size_t)c.nxg * c.nyg * c.nzg;
-  size_t o_stage = A.take(3 * 8 * I.nstage);   // three Fortran-layout fields (chl_set_fields)
+  size_t o_stage = A.take(6 * 8 * I.nstage);   // Fortran-layout fields: 3 in, 3 out (chl_set_fields, chl_download_async)
   cudaError_t e = cudaMalloc(&I.arena, A.off);
   if (e != cudaSuccess) { h->err = "device allocation failed (" + std::to_string(A.off) + " bytes)"; return CHL_E_NOMEM; }
   CK(cudaMemsetAsync(I.arena, 0, A.off, h->st));
@@ -620,6 +627,19 @@ static int check_ready(chl_handle* h) {
 
 static int finish(chl_handle* h) {
   cudaError_t e = cudaStreamSynchronize(h->st);
+  if (e == cudaSuccess && h->st_h2d) e = cudaStreamSynchronize(h->st_h2d);
+  if (e == cudaSuccess && h->st_d2h) e = cudaStreamSynchronize(h->st_d2h);
+  if (e != cudaSuccess) { h->err = std::string("CUDA: ") + cudaGetErrorString(e); return CHL_E_CUDA; }
+  return CHL_OK;
+}
+
+// Waits for the copy streams: the synchronous entry points use the staging
+// area on the compute stream only after any round-trip copy into or out of
+// it has finished.
+static int drain_copies(chl_handle* h) {
+  cudaError_t e = cudaSuccess;
+  if (h->st_h2d) e = cudaStreamSynchronize(h->st_h2d);
+  if (e == cudaSuccess && h->st_d2h) e = cudaStreamSynchronize(h->st_d2h);
   if (e != cudaSuccess) { h->err = std::string("CUDA: ") + cudaGetErrorString(e); return CHL_E_CUDA; }
   return CHL_OK;
 }
@@ -747,6 +767,8 @@ int chl_create(const chl_grid_desc* desc, chl_handle** out) { return chl_batch_c
 int chl_destroy(chl_handle* h) {
   if (!h) return CHL_OK;
   if (h->st) cudaStreamSynchronize(h->st);
+  if (h->st_h2d) cudaStreamSynchronize(h->st_h2d);   // no copy may still target the arena
+  if (h->st_d2h) cudaStreamSynchronize(h->st_d2h);
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
   if (h->graph) cudaGraphDestroy(h->graph);
   for (auto& I : h->in) if (I.arena) cudaFree(I.arena);
@@ -759,6 +781,10 @@ int chl_destroy(chl_handle* h) {
   if (h->d_mlp_cfg) cudaFree(h->d_mlp_cfg);
   if (h->d_mlp_status) cudaFree(h->d_mlp_status);
   for (auto& e : h->ev) cudaEventDestroy(e);
+  for (auto& I : h->in)
+    for (cudaEvent_t e : {I.ev_h2d, I.ev_unpacked, I.ev_packed, I.ev_d2h}) if (e) cudaEventDestroy(e);
+  if (h->st_h2d) cudaStreamDestroy(h->st_h2d);
+  if (h->st_d2h) cudaStreamDestroy(h->st_d2h);
   if (h->st) cudaStreamDestroy(h->st);
   delete h;
   return CHL_OK;
@@ -772,10 +798,11 @@ static Inst* get_inst(chl_handle* h, int inst) {
   return &h->in[inst];
 }
 
-// U, V, W of velocity set 0 and their Fortran-layout slots in the staging area
-static ChlFields3 fields3(Inst* I) {
+// U, V, W of velocity set 0 and their Fortran-layout slots in the staging
+// area (out = false: the input half, true: the output half)
+static ChlFields3 fields3(Inst* I, bool out = false) {
   const Consts& c = I->c;
-  double* s = I->staging;
+  double* s = I->staging + (out ? 3 * I->nstage : 0);
   const size_t n = I->nstage;
   ChlFields3 f;
   f.f[0] = ChlField1{s, I->dev.U[0], c.nx, c.nyg, c.nzg, c.Ny + 2, 0};
@@ -788,6 +815,7 @@ int chl_upload(chl_handle* h, int inst, const double* U, const double* V, const 
   Inst* I = get_inst(h, inst);
   if (!I) return CHL_E_ARG;
   if (!U || !V || !W) { h->err = "null field"; return CHL_E_ARG; }
+  if (int rc = drain_copies(h)) return rc;
   const ChlFields3 f3 = fields3(I);
   const double* src[3] = {U, V, W};
   for (int q = 0; q < 3; ++q) {
@@ -807,6 +835,7 @@ int chl_upload(chl_handle* h, int inst, const double* U, const double* V, const 
 
 static int download_field(chl_handle* h, Inst* I, double* dst, const double* src, int n1, int n2, int n3, int nrow,
                           double sub = 0.0) {
+  if (int rc = drain_copies(h)) return rc;
   chl_launch_pack(I->staging, src, I->c.Nx, nrow, I->c.Nz, n1, n2, n3, sub, h->st);
   LAUNCHED();
   CK(cudaMemcpyAsync(dst, I->staging, 8 * (size_t)n1 * n2 * n3, cudaMemcpyDeviceToHost, h->st));
@@ -1240,6 +1269,7 @@ int chl_compute_rhs(chl_handle* h, int inst, double* Fu, double* Fv, double* Fw)
   int rc = check_ready(h); if (rc) return rc;
   Inst* I = get_inst(h, inst);
   if (!I) return CHL_E_ARG;
+  if ((rc = drain_copies(h))) return rc;
   chl_launch_flux(h->map(M_EDGE), h->nblk[M_EDGE], 0, h->st);
   chl_launch_update(h->map(M_PT), h->nblk[M_PT], 0, 0, 0, 2, h->st);
   LAUNCHED();
@@ -1305,20 +1335,43 @@ int chl_check_divergence(chl_handle* h, int inst, double* max_div, double* max_a
   return CHL_OK;
 }
 
+// The copy streams and the instance's ordering events, on first use.
+static int round_trip_setup(chl_handle* h, Inst* I) {
+  if (!h->st_h2d) CK(cudaStreamCreateWithFlags(&h->st_h2d, cudaStreamNonBlocking));
+  if (!h->st_d2h) CK(cudaStreamCreateWithFlags(&h->st_d2h, cudaStreamNonBlocking));
+  cudaEvent_t* ev[4] = {&I->ev_h2d, &I->ev_unpacked, &I->ev_packed, &I->ev_d2h};
+  for (cudaEvent_t* e : ev)
+    if (!*e) CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  return CHL_OK;
+}
+
+// Host-buffer round trip.  The input half of the staging area receives the
+// three copies on the H2D stream, once the previous conversion out of it on
+// the compute stream is done; the compute stream converts them into
+// velocity set 0 once they have arrived.  The output half is filled on the
+// compute stream, once the previous download out of it is done, and copied
+// to the host on the D2H stream.  So with calls in the order set_fields,
+// step, download_async for step after step, step n+1's upload and step
+// n-1's download run on the copy engines while step n computes; each step
+// still copies its own inputs in and its own result out.
 int chl_set_fields(chl_handle* h, int inst, const double* U, const double* V, const double* W) {
   Inst* I = get_inst(h, inst);
   if (!I) return CHL_E_ARG;
   if (!I->uploaded) { h->err = "chl_set_fields before chl_upload"; return CHL_E_STATE; }
   if (!U || !V || !W) { h->err = "null field"; return CHL_E_ARG; }
-  // the three copies back to back into the staging area, one conversion
-  const ChlFields3 f3 = fields3(I);
+  if (int rc = round_trip_setup(h, I)) return rc;
+  const ChlFields3 f3 = fields3(I, false);
   const double* src[3] = {U, V, W};
+  CK(cudaStreamWaitEvent(h->st_h2d, I->ev_unpacked, 0));
   for (int q = 0; q < 3; ++q) {
     const ChlField1& d = f3.f[q];
-    CK(cudaMemcpyAsync(d.fort, src[q], 8 * (size_t)d.n1 * d.n2 * d.n3, cudaMemcpyHostToDevice, h->st));
+    CK(cudaMemcpyAsync(d.fort, src[q], 8 * (size_t)d.n1 * d.n2 * d.n3, cudaMemcpyHostToDevice, h->st_h2d));
   }
+  CK(cudaEventRecord(I->ev_h2d, h->st_h2d));
+  CK(cudaStreamWaitEvent(h->st, I->ev_h2d, 0));
   chl_launch_unpack3(f3, I->c.Nx, I->c.Nz, h->st);
   LAUNCHED();
+  CK(cudaEventRecord(I->ev_unpacked, h->st));
   CK(cudaMemsetAsync(I->dev.status, 0, sizeof(int), h->st));
   return CHL_OK;   // stream-ordered; no synchronisation
 }
@@ -1326,16 +1379,20 @@ int chl_set_fields(chl_handle* h, int inst, const double* U, const double* V, co
 int chl_download_async(chl_handle* h, int inst, double* U, double* V, double* W) {
   Inst* I = get_inst(h, inst);
   if (!I) return CHL_E_ARG;
-  // one conversion into the staging area, then the copies back to back
-  const ChlFields3 f3 = fields3(I);
+  if (int rc = round_trip_setup(h, I)) return rc;
+  const ChlFields3 f3 = fields3(I, true);
   double* dst[3] = {U, V, W};
+  CK(cudaStreamWaitEvent(h->st, I->ev_d2h, 0));
   chl_launch_pack3(f3, I->c.Nx, I->c.Nz, h->st);
   LAUNCHED();
+  CK(cudaEventRecord(I->ev_packed, h->st));
+  CK(cudaStreamWaitEvent(h->st_d2h, I->ev_packed, 0));
   for (int q = 0; q < 3; ++q) {
     if (!dst[q]) continue;
     const ChlField1& d = f3.f[q];
-    CK(cudaMemcpyAsync(dst[q], d.fort, 8 * (size_t)d.n1 * d.n2 * d.n3, cudaMemcpyDeviceToHost, h->st));
+    CK(cudaMemcpyAsync(dst[q], d.fort, 8 * (size_t)d.n1 * d.n2 * d.n3, cudaMemcpyDeviceToHost, h->st_d2h));
   }
+  CK(cudaEventRecord(I->ev_d2h, h->st_d2h));
   return CHL_OK;
 }
 

@@ -144,10 +144,16 @@ int chl_stats_profiles(chl_handle* h, int inst, double* Umean, double* Vmean, do
 int chl_synchronize(chl_handle* h);
 
 /* Replace U, V, W of a running instance (no new Qflow_x_0, no sync): the
- * host-buffer round trip of a Fortran caller that keeps its own copy. */
+ * host-buffer round trip of a Fortran caller that keeps its own copy.  The
+ * copies run on a copy stream of the handle, ordered against the steps by
+ * events: with set_fields, chl_rk3_step, download_async called step after
+ * step, one step's upload and the previous step's download overlap the
+ * computation in between.  The host buffers must stay valid and unchanged
+ * until the next chl_synchronize (or a later call that synchronises). */
 int chl_set_fields(chl_handle* h, int inst, const double* U, const double* V, const double* W);
-/* Stream-ordered download of U, V, W into (pinned) host buffers; completes
- * at the next chl_synchronize. */
+/* Download of U, V, W after the work queued so far, into (pinned) host
+ * buffers, on the handle's other copy stream; completes at the next
+ * chl_synchronize. */
 int chl_download_async(chl_handle* h, int inst, double* U, double* V, double* W);
 
 /* Measurement: device time (CUDA events on the handle's stream) of nsteps
