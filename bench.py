@@ -323,7 +323,7 @@ def config_of(args, cases_, world=1):
             "l2": l2}
 
 
-def roofline_of(args, prof, points, step_ms, workload_name):
+def roofline_of(args, prof, points, step_ms, workload_name, rank=0, dev_index=0):
     """Roofline of the dominant kernel (largest share of the profiled step).
 
     Both ceilings are computed: HBM bytes (algorithmic bytes per point of the
@@ -339,7 +339,9 @@ def roofline_of(args, prof, points, step_ms, workload_name):
     peaks = load_json(os.path.join(HERE, "MEASURED_PEAKS.json"), {})
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     hbm_src = "measured (MEASURED_PEAKS.json hbm_gbs)" if "hbm_gbs" in peaks else "fallback 6.8 TB/s"
-    fp64 = live_fp64_peak() or load_json(os.path.join(HERE, "profiles", "fp64_peak.json"), {})
+    # measured live by rank 0 (the rank that prints) on its own GPU
+    fp64 = (live_fp64_peak(dev_index) if rank == 0 else None) or \
+        load_json(os.path.join(HERE, "profiles", "fp64_peak.json"), {})
     traffic = load_json(os.path.join(HERE, "profiles", "kernel_traffic.json"), {})
     byt = KERNEL_BYTES.get(dom, 0.0) * points
     ach = byt / per_launch_s / 1e9
@@ -427,7 +429,7 @@ def run_ours(args):
     # per-kernel breakdown (event-bracketed, un-graphed steps)
     prof = ch.profile_step(reps=args.prof_reps)
     tot_prof = sum(v[0] for v in prof.values())
-    roof = roofline_of(args, prof, points, tmax_ms / args.steps, args.workload)
+    roof = roofline_of(args, prof, points, tmax_ms / args.steps, args.workload, rank, dev_index)
     # e2e through the C ABI with pinned host buffers
     e2e = None
     if not args.no_e2e and len(cases_) == 1:
@@ -628,10 +630,10 @@ def _barrier_record(out):
 _LIVE_FP64 = None
 
 
-def live_fp64_peak():
-    """The FP64 issue rates of this GPU from bench_peaks.cu, run once per
-    process (about a second of GPU time), or None where the probe binary was
-    not built."""
+def live_fp64_peak(dev_index=0):
+    """The FP64 issue rates of this rank's GPU (dev_index among the visible
+    ones) from bench_peaks.cu, run once per process (about a second of GPU
+    time), or None where the probe binary was not built."""
     global _LIVE_FP64
     if _LIVE_FP64 is None:
         _LIVE_FP64 = {}
@@ -639,7 +641,11 @@ def live_fp64_peak():
             from channel_rl_gb300 import build as b
             exe = b.PEAKS_BIN
             if os.path.exists(exe):
-                out = subprocess.run([exe, "fp64"], check=True, capture_output=True, text=True, timeout=120).stdout
+                env = dict(os.environ)
+                vis = [v for v in env.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+                env["CUDA_VISIBLE_DEVICES"] = vis[dev_index] if dev_index < len(vis) else str(dev_index)
+                out = subprocess.run([exe, "fp64"], check=True, capture_output=True, text=True, timeout=120,
+                                     env=env).stdout
                 rec = _fp64_record(out)
                 if rec.get("fp64_peak_gops"):
                     rec["live"] = True
