@@ -407,7 +407,7 @@ def run_ours(args):
     # the ones reported
     barrier(dist)
     torch.cuda.synchronize()
-    with ClockSampler(dev_index) as clk:
+    with ClockSampler(physical_gpu(dev_index)) as clk:
         t0 = time.perf_counter()
         ms = ch.time_steps(args.steps)
         wall = time.perf_counter() - t0
@@ -630,6 +630,13 @@ def _barrier_record(out):
 _LIVE_FP64 = None
 
 
+def physical_gpu(dev_index):
+    """The GPU (index or UUID as nvidia-smi and CUDA_VISIBLE_DEVICES name it)
+    behind visible device dev_index."""
+    vis = [v.strip() for v in os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
+    return vis[dev_index] if dev_index < len(vis) else str(dev_index)
+
+
 def live_fp64_peak(dev_index=0):
     """The FP64 issue rates of this rank's GPU (dev_index among the visible
     ones) from bench_peaks.cu, run once per process (about a second of GPU
@@ -642,8 +649,7 @@ def live_fp64_peak(dev_index=0):
             exe = b.PEAKS_BIN
             if os.path.exists(exe):
                 env = dict(os.environ)
-                vis = [v for v in env.get("CUDA_VISIBLE_DEVICES", "").split(",") if v.strip()]
-                env["CUDA_VISIBLE_DEVICES"] = vis[dev_index] if dev_index < len(vis) else str(dev_index)
+                env["CUDA_VISIBLE_DEVICES"] = physical_gpu(dev_index)
                 out = subprocess.run([exe, "fp64"], check=True, capture_output=True, text=True, timeout=120,
                                      env=env).stdout
                 rec = _fp64_record(out)
