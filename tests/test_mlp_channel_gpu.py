@@ -11,8 +11,8 @@ Tolerances:
   features        |x_gpu - x_oracle| <= 1e-6 (FP32 values of O(1); the FP64
                   inputs agree to ~1e-12, so at most an FP32 rounding flip)
   trust flags     identical
-  mu              <= 4e-3 (BF16 activations: a last-bit flip of one hidden
-                  unit moves mu by ~1e-3, as in tests/test_mlp_gpu.py)
+  mu              <= 1e-3 (BF16 activations: a last-bit flip of one hidden
+                  unit moves mu by up to ~1e-4, tests/test_mlp_gpu.py)
   alpha_x, U, V, W  <= FIELD_RTOL (1e-12) relative, after each of 3 steps
 """
 import os
@@ -28,7 +28,7 @@ pytestmark = pytest.mark.gpu
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 FEATURE_ATOL = 1e-6
-MU_ATOL = 4e-3
+MU_ATOL = 1e-3
 
 
 def _theta():

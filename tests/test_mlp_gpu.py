@@ -28,11 +28,20 @@ def _channel(case):
     return Channel(case)
 
 
-def test_network_and_trace_match_reference():
+# Tolerances against the BF16 oracle, from measurement on GB300 over five
+# seeds: mu max 8e-5 (a BF16 rounding flip of one hidden unit; tanhf and the
+# host tanh differ in the last FP32 bit), mu 99th percentile 9e-8, trace
+# 3.6e-5 relative in norm, any parameter block 1.7e-4.
+MU_MAX, MU_P99 = 5e-4, 1e-6
+TRACE_REL, BLOCK_REL = 5e-4, 1e-3
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_network_and_trace_match_reference(seed):
     case = C.smaller(C.c2_wm64(), 32, 32, 32)
     ch = _channel(case)
-    rng = np.random.default_rng(1)
-    theta = M.xavier_init(7)
+    rng = np.random.default_rng(1 + seed)
+    theta = M.xavier_init(7 + seed)
     theta[M.H * M.NIN:M.H * M.NIN + M.H] = rng.standard_normal(M.H).astype(np.float32) * 0.1
     ch.mlp_set_params(theta)
     assert np.array_equal(ch.mlp_params(), theta)
@@ -41,11 +50,13 @@ def test_network_and_trace_match_reference():
     g = rng.standard_normal(P).astype(np.float32)
     mu, tr = ch.mlp_eval(x, g)
     ref = M.forward(theta, x)["mu"]
-    assert np.abs(mu - ref).max() < 4e-3          # BF16 activations: a last-bit flip of h1 moves mu by ~1e-3
+    err = np.abs(mu - ref)
+    assert err.max() < MU_MAX and np.quantile(err, 0.99) < MU_P99, (err.max(), np.quantile(err, 0.99))
     rt = M.trace_grad(theta, x, g)
-    assert np.linalg.norm(tr - rt) / np.linalg.norm(rt) < 2e-2
-    for name, sl in (("W2", slice(320, 4416)), ("W1", slice(0, 256)), ("w3", slice(4480, 4544))):
-        assert np.linalg.norm(tr[sl] - rt[sl]) / np.linalg.norm(rt[sl]) < 3e-2, name
+    assert np.linalg.norm(tr - rt) / np.linalg.norm(rt) < TRACE_REL
+    for name, sl in (("W1", slice(0, 256)), ("b1", slice(256, 320)), ("W2", slice(320, 4416)),
+                     ("b2", slice(4416, 4480)), ("w3", slice(4480, 4544))):
+        assert np.linalg.norm(tr[sl] - rt[sl]) <= BLOCK_REL * np.linalg.norm(rt[sl]), name
     ch.close()
 
 
