@@ -1243,6 +1243,10 @@ int chl_set_tile_shapes(chl_handle* h, int x_min_blocks, int z_min_blocks, int t
   return CHL_OK;
 }
 
+int chl_device_reset(void) {
+  return cudaDeviceReset() == cudaSuccess ? CHL_OK : CHL_E_CUDA;
+}
+
 int chl_synchronize(chl_handle* h) {
   if (!h) return CHL_E_ARG;
   int rc = finish(h);

@@ -74,7 +74,7 @@ EXPORTS = (
     "chl_grid_constants", "chl_set_fields", "chl_download_async", "chl_time_steps",
     "chl_graph_kernel_count", "chl_profile_step",
     "chl_autotune", "chl_get_tile_shapes", "chl_set_tile_shapes",
-    "chl_check_divergence_noalloc", "chl_noalloc_last_error",
+    "chl_check_divergence_noalloc", "chl_noalloc_last_error", "chl_device_reset",
     "chl_mlp_set_params", "chl_mlp_get_params", "chl_mlp_configure", "chl_mlp_read_trace",
     "chl_mlp_eval", "chl_mlp_debug", "chl_mlp_read_record", "chl_tc_selftest",
     "chl_snapshot_dims", "chl_snapshot_read", "chl_snapshot_write", "chl_io_last_error",

@@ -143,6 +143,15 @@ int chl_stats_profiles(chl_handle* h, int inst, double* Umean, double* Vmean, do
 
 int chl_synchronize(chl_handle* h);
 
+/* Resets the current device in the library's own CUDA runtime (it is linked
+ * statically, so a caller's cudaDeviceReset does not reach it): everything
+ * the library holds on that device is released, including every handle's
+ * memory, so those handles must not be used again, not even destroyed.  For
+ * callers that reset the device themselves, e.g. at the end of a run or
+ * before handing the device to other work.  No counterpart in the
+ * reference. */
+int chl_device_reset(void);
+
 /* Replace U, V, W of a running instance (no new Qflow_x_0, no sync): the
  * host-buffer round trip of a Fortran caller that keeps its own copy.  The
  * copies run on a copy stream of the handle, ordered against the steps by

@@ -143,17 +143,28 @@ r2 = call(case, 99)                         # a second context: the array has an
 ck(cu.cuCtxDestroy_v2(other), "cuCtxDestroy")
 ck(cu.cuCtxSetCurrent(prim), "cuCtxSetCurrent")
 r3 = call(case, 7)                          # back in the primary context, fresh buffers
-ck(cu.cuDevicePrimaryCtxRelease_v2(dev), "cuDevicePrimaryCtxRelease")
-print("ok", r1, r2, r3)
+# a device reset through the library's own runtime: the primary context and
+# every allocation in it go; the next call finds the array in the new one
+lib.chl_device_reset.restype = C.c_int
+if lib.chl_device_reset() != 0:
+    raise SystemExit("chl_device_reset failed")
+again = C.c_void_p()
+ck(cu.cuDevicePrimaryCtxRetain(C.byref(again), dev), "cuDevicePrimaryCtxRetain after the reset")
+ck(cu.cuCtxSetCurrent(again), "cuCtxSetCurrent after the reset")
+r4 = call(case, 5)                          # fresh buffers in the reset context
+cu.cuDevicePrimaryCtxRelease_v2(dev)
+cu.cuDevicePrimaryCtxRelease_v2(dev)
+print("ok", r1, r2, r3, r4)
 """
 
 
 @pytest.mark.gpu
-def test_noalloc_in_a_second_context():
+def test_noalloc_in_a_second_context_and_after_a_reset():
     """A caller may run the library in a context it created with the driver
-    API.  The scratch array then sits at another address than in the primary
-    context, and each call must find it there: the primary context, a
-    second context with fresh buffers, then the primary context again, each
+    API, or reset the device between calls.  The scratch array then sits at
+    another address, and each call must find it there: the primary context,
+    a second context with fresh buffers, the primary context again, and,
+    after chl_device_reset, the new primary context with fresh buffers, each
     checked against the divergence computed on the host."""
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
     r = subprocess.run([sys.executable, "-c", _CONTEXTS, root], capture_output=True, text=True, timeout=300)
