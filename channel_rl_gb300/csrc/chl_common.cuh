@@ -131,7 +131,8 @@ struct ChlInst {
   float *mlp_trace;               // policy-gradient trace of this instance (4545)
   const float *mlp_theta;         // network parameters, shared by the batch (4545)
   unsigned int *mlp_cfg;          // shared: sigma bits, train, seed lo/hi, evaluation counter,
-                                  //   record flag, withheld-commit poll limit (chl_mlp_debug)
+                                  //   record flag, withheld-commit poll limit (chl_mlp_debug),
+                                  //   shared-exploration flag (chl_mlp_set_exploration)
   float *mlp_rec;                 // [3 stages][2 Nx Nz][8] per-point record (chl_mlp_debug), or null
 };
 

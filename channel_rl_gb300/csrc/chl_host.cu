@@ -253,7 +253,7 @@ struct chl_handle {
   bool tri_scan = false;              // some instance splits its tridiagonal columns (chl_tri_lanes)
   int LES_model = 0, wall_model = 0, any_mass = 0;
   float* d_mlp_theta = nullptr;       // learned wall model parameters (shared)
-  unsigned int* d_mlp_cfg = nullptr;  // sigma, train, seed lo/hi, evaluation counter
+  unsigned int* d_mlp_cfg = nullptr;  // sigma, train, seed lo/hi, evaluation counter, debug [5..6], shared draws [7]
   int* d_mlp_status = nullptr;
   double* d_divout = nullptr;
   double* d_stats = nullptr;
@@ -1498,6 +1498,13 @@ int chl_mlp_read_trace(chl_handle* h, int inst, float* trace, int zero_after) {
   int rc = finish(h);
   if (rc) return rc;
   return check_mlp(h);
+}
+
+int chl_mlp_set_exploration(chl_handle* h, int shared) {
+  if (!h) return CHL_E_ARG;
+  const unsigned int c = shared ? 1u : 0u;
+  CK(cudaMemcpyAsync(h->d_mlp_cfg + 7, &c, sizeof(c), cudaMemcpyHostToDevice, h->st));
+  return finish(h);
 }
 
 int chl_mlp_debug(chl_handle* h, int record, int withhold_polls) {

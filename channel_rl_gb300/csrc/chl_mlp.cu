@@ -222,8 +222,12 @@ k_mlp(ChlMap map, MlpArgs A) {
         float eps = 0.f;
         if (sigma > 0.f) {
           const unsigned long long seed = ((unsigned long long)cfg[3] << 32) | cfg[2];
-          const unsigned long long ctr = ((unsigned long long)cfg[4] * 4ULL + (unsigned long long)A.stage) * 0x100000000ULL
-                                         + (unsigned long long)(I - map.inst) * 0x1000000ULL + (unsigned long long)gp;
+          // cfg[7] != 0: one draw per instance, the same for every wall
+          // point, stage and step until the seed changes (chl_mlp_set_exploration)
+          const unsigned long long inst = (unsigned long long)(I - map.inst);
+          const unsigned long long ctr = cfg[7] != 0u ? inst * 0x1000000ULL
+              : ((unsigned long long)cfg[4] * 4ULL + (unsigned long long)A.stage) * 0x100000000ULL
+                + inst * 0x1000000ULL + (unsigned long long)gp;
           eps = gauss(seed, ctr);
         }
         a = fminf(0.5f, fmaxf(-0.5f, mu + sigma * eps));

@@ -76,7 +76,7 @@ EXPORTS = (
     "chl_autotune", "chl_get_tile_shapes", "chl_set_tile_shapes",
     "chl_check_divergence_noalloc", "chl_noalloc_last_error", "chl_device_reset",
     "chl_mlp_set_params", "chl_mlp_get_params", "chl_mlp_configure", "chl_mlp_read_trace",
-    "chl_mlp_eval", "chl_mlp_debug", "chl_mlp_read_record", "chl_tc_selftest",
+    "chl_mlp_eval", "chl_mlp_set_exploration", "chl_mlp_debug", "chl_mlp_read_record", "chl_tc_selftest",
     "chl_snapshot_dims", "chl_snapshot_read", "chl_snapshot_write", "chl_io_last_error",
     "chl_read_parameters", "chl_save_snapshot", "chl_load_snapshot",
     "chl_agent_observe", "chl_agent_act", "chl_status_flags",
@@ -141,6 +141,7 @@ def load(build_if_missing=True):
     lib.chl_mlp_configure.argtypes = [H, C.c_float, C.c_ulonglong, C.c_int]
     lib.chl_mlp_read_trace.argtypes = [H, C.c_int, _F32P, C.c_int]
     lib.chl_mlp_eval.argtypes = [H, _F32P, _F32P, C.c_int, _F32P, _F32P]
+    lib.chl_mlp_set_exploration.argtypes = [H, C.c_int]
     lib.chl_mlp_debug.argtypes = [H, C.c_int, C.c_int]
     lib.chl_mlp_read_record.argtypes = [H, C.c_int, _F32P]
     lib.chl_tc_selftest.argtypes = [C.POINTER(C.c_ushort), C.POINTER(C.c_ushort), _F32P, C.c_int]
@@ -426,6 +427,11 @@ class Channel:
         t = np.zeros(MLP_NPARAM, np.float32)
         self._check(self.lib.chl_mlp_read_trace(self.h, inst, t.ctypes.data_as(_F32P), int(zero)), "chl_mlp_read_trace")
         return t
+
+    def mlp_set_exploration(self, shared=False):
+        """One exploration draw per instance and rollout (shared=True) or per
+        wall point, stage and step (the default)."""
+        self._check(self.lib.chl_mlp_set_exploration(self.h, int(bool(shared))), "chl_mlp_set_exploration")
 
     def mlp_debug(self, record=False, withhold_polls=0):
         """Checking hooks: per-point record of every evaluation, or MMAs

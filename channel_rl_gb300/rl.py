@@ -93,10 +93,13 @@ class Adam:
 class Trainer:
     """Batched channels with the learned wall model and its REINFORCE loop."""
 
-    def __init__(self, cases_, seed=0, sigma=0.1, lr=3e-3, spinup=200):
+    def __init__(self, cases_, seed=0, sigma=0.1, lr=3e-3, spinup=200, shared_noise=False):
         self.cases = [replace(c, wall_model=C.WM_MLP) for c in cases_]
         self.ch = Channel(self.cases)
         self.sigma = sigma
+        # shared_noise: one exploration draw per channel and rollout
+        # (chl_mlp_set_exploration), so that the per-channel reward sees it
+        self.shared_noise = shared_noise
         self.seed = seed
         self.theta = init_params(seed)
         self.opt = Adam(lr=lr)
@@ -142,6 +145,7 @@ class Trainer:
         self.restore()
         self.ch.mlp_set_params(self.theta)
         self.ch.mlp_configure(sigma=self.sigma, seed=self.seed * 1000003 + it, train=True)
+        self.ch.mlp_set_exploration(self.shared_noise)
         for q in range(len(self.cases)):
             self.ch.mlp_trace(q, zero=True)
         err = self.rollout_reward(steps)
@@ -160,6 +164,7 @@ class Trainer:
         self.baseline = 0.8 * self.baseline + 0.2 * R
         self.history.append(float(err.mean()))
         self.ch.mlp_configure(sigma=0.0, seed=0, train=False)
+        self.ch.mlp_set_exploration(False)
         return float(err.mean())
 
     def evaluate(self, theta, steps=200, chunks=4):

@@ -36,8 +36,8 @@ def summarise(cases_, eq, ml):
 
 
 def train(cases_, iters=120, steps=60, spinup=300, sigma=0.1, lr=3e-3, seed=7, eval_steps=120,
-          eval_every=10, log=print):
-    tr = Trainer(cases_, seed=seed, sigma=sigma, lr=lr, spinup=spinup)
+          eval_every=10, shared_noise=False, log=print):
+    tr = Trainer(cases_, seed=seed, sigma=sigma, lr=lr, spinup=spinup, shared_noise=shared_noise)
     eq = tr.evaluate(None, steps=eval_steps)
     best = (float(eq[0].mean()), tr.theta.copy(), eq, 0)
     log(f"equilibrium: profile err {eq[0].mean():.5f}, u_tau err {eq[1].mean():.5f}")
@@ -53,6 +53,7 @@ def train(cases_, iters=120, steps=60, spinup=300, sigma=0.1, lr=3e-3, seed=7, e
     theta, ml, it_best = best[1], best[2], best[3]
     report = {"instances": [c.name for c in cases_], "iterations": iters, "rollout_steps": steps,
               "spinup_steps": spinup, "sigma": sigma, "lr": lr, "seed": seed, "eval_steps": eval_steps,
+              "shared_noise": shared_noise,
               "best_iteration": it_best, "train_seconds": time.perf_counter() - t0,
               "equilibrium": {"profile_err": eq[0].tolist(), "utau_err": eq[1].tolist()},
               "learned": {"profile_err": ml[0].tolist(), "utau_err": ml[1].tolist()},
@@ -71,12 +72,14 @@ def main():
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--eval-steps", type=int, default=120)
     ap.add_argument("--eval-every", type=int, default=10)
+    ap.add_argument("--shared-noise", action="store_true",
+                    help="one exploration draw per channel and rollout instead of one per wall point and step")
     ap.add_argument("--out", default=None, help="where to write the kept parameters (.npy, float32)")
     ap.add_argument("--report", default=None, help="where to write the JSON report")
     args = ap.parse_args()
     theta, report = train(C.c5_learned(), iters=args.iters, steps=args.steps, spinup=args.spinup,
                           sigma=args.sigma, lr=args.lr, seed=args.seed, eval_steps=args.eval_steps,
-                          eval_every=args.eval_every)
+                          eval_every=args.eval_every, shared_noise=args.shared_noise)
     if args.out:
         np.save(args.out, theta.astype(np.float32))
     if args.report:

@@ -215,6 +215,12 @@ int chl_mlp_get_params(chl_handle* h, float* theta);
 /* Gaussian exploration noise sigma on the log-stress action, its seed, and
  * whether steps accumulate the policy-gradient trace sum_t eps/sigma dmu/dtheta. */
 int chl_mlp_configure(chl_handle* h, float sigma, unsigned long long seed, int train);
+/* Exploration draws: shared = 0 (default) draws eps per wall point, stage
+ * and step; shared != 0 draws one eps per instance, used by every wall point,
+ * stage and step until chl_mlp_configure sets another seed - a perturbation
+ * of the whole wall's log-stress per rollout, whose effect on the plane-
+ * averaged profile a per-instance reward can resolve. */
+int chl_mlp_set_exploration(chl_handle* h, int shared);
 /* Trace of one instance (4545 floats); zero it afterwards if zero_after. */
 int chl_mlp_read_trace(chl_handle* h, int inst, float* trace, int zero_after);
 /* Network on given points (no channel): x[P][4] normalised features,

@@ -160,3 +160,56 @@ def test_wall_model_wait_timeout_is_reported_and_cleared():
     assert (r[..., 6] == 1.0).any()
     a.close()
     b.close()
+
+
+def _exploration(rec, sigma):
+    """(eps of the trusted points whose action is not clipped, per stage)."""
+    out = []
+    for s in range(3):
+        r = rec[s]
+        m = (r[..., 6] == 1.0) & (np.abs(r[..., 5]) < 0.5)
+        out.append((r[..., 5][m].astype(np.float64) - r[..., 4][m]) / sigma)
+    return out
+
+
+def test_shared_exploration_is_one_draw_per_instance():
+    """chl_mlp_set_exploration(1): every unclipped trusted wall point of an
+    instance, every stage and every step, explores with the same eps (action
+    minus mu, over sigma, to FP32 rounding); the two instances draw different
+    eps; a new seed draws a new one.  With the default per-point draws the
+    same points carry unit-variance noise."""
+    src = C.c5_learned()
+    batch = [C.smaller(src[0], 32, 32, 32), C.smaller(src[1], 48, 32, 32)]
+    sigma = 0.1
+    b = _channel(batch)
+    for q, c in enumerate(batch):
+        b.upload(*C.initial_fields(c), inst=q)
+    b.mlp_set_params(_theta())
+    b.mlp_debug(record=True)
+    b.step(1)                                   # nu + nu_t of a finished stage
+    b.mlp_configure(sigma=sigma, seed=21, train=True)
+    b.mlp_set_exploration(True)
+    draws = {}
+    for seed in (21, 22):
+        b.mlp_configure(sigma=sigma, seed=seed, train=True)
+        for step in range(2):
+            b.step(1)
+            b.synchronize()
+            for q in range(len(batch)):
+                for s, e in enumerate(_exploration(b.mlp_record(inst=q), sigma)):
+                    assert e.size > 100, (seed, step, q, s)
+                    assert np.ptp(e) <= 1e-5, (seed, step, q, s, np.ptp(e))
+                    draws.setdefault((seed, q), []).append(float(e.mean()))
+    for key, d in draws.items():
+        assert max(d) - min(d) <= 1e-5, key   # the same draw for every stage and step
+    assert abs(draws[(21, 0)][0] - draws[(21, 1)][0]) > 1e-3
+    assert abs(draws[(21, 0)][0] - draws[(22, 0)][0]) > 1e-3
+    b.mlp_set_exploration(False)
+    b.step(1)
+    b.synchronize()
+    e = _exploration(b.mlp_record(inst=0), sigma)[0]
+    assert e.size > 100 and 0.8 < e.std() < 1.2
+    for q in range(len(batch)):
+        assert np.any(b.mlp_trace(q, zero=True) != 0)
+    b.mlp_configure(sigma=0.0, seed=0, train=False)
+    b.close()
