@@ -46,10 +46,32 @@ __host__ __device__ inline int chl_tri_lanes(long modes, int Ny) {
 // one point per thread, 5 per SM, where 256-thread blocks left 2 blocks on
 // some SMs and 1 on most.  A function of the instance's own extents only,
 // so an instance sums its planes in the same order alone and in a batch.
+// Stockham FFT passes (chl_fft.cu): radix 4 while the remaining length
+// allows, then 3, then 2.  Each pass with twiddles (sub-transform size
+// Ns > 1) has CHL_TW_F fields of Ns doubles in the length's pass table.
+#define CHL_TW_F 7
+__host__ __device__ inline int chl_fft_radix(int rem) { return rem % 4 == 0 ? 4 : (rem % 3 == 0 ? 3 : 2); }
+__host__ __device__ inline int chl_tw_len(int N) {
+  int Ns = 1, rem = N, len = 0;
+  while (rem > 1) {
+    const int R = chl_fft_radix(rem);
+    if (Ns > 1) len += CHL_TW_F * Ns;
+    Ns *= R; rem /= R;
+  }
+  return len;
+}
+// bytes of a pass table in shared memory, kept a multiple of 16
+__host__ __device__ inline size_t chl_tw_bytes(int len) { return ((size_t)len * 8 + 15) & ~(size_t)15; }
+
 #define CHL_DSMF_THREADS 64
+// Points of one plane sum: the Nx x Nz plane, then the reference's
+// duplicated periodic column (i = 0, every k) and plane (k = 0, every i) and
+// one more (0, 0) - its weights 2 and 4 as extra points of weight 1.
+__host__ __device__ inline int chl_dsm_points(int Nx, int Nz) { return Nx * Nz + Nx + Nz + 1; }
 __host__ __device__ inline int chl_dsm_ppt(int Nx, int Ny, int Nz) {
+  const int n = chl_dsm_points(Nx, Nz);
   int ppt = 4;
-  while (ppt > 1 && (long)Ny * ((Nx * Nz + CHL_DSMF_THREADS * ppt - 1) / (CHL_DSMF_THREADS * ppt)) < CHL_MIN_BLOCKS)
+  while (ppt > 1 && (long)Ny * ((n + CHL_DSMF_THREADS * ppt - 1) / (CHL_DSMF_THREADS * ppt)) < CHL_MIN_BLOCKS)
     ppt >>= 1;
   return ppt;
 }
@@ -103,7 +125,7 @@ struct ChlInst {
   const double *smag_csdelta;     // Cs*Delta_j by centre row (static Smagorinsky)
   const double *smag_dwall;       // distance of centre row to the nearer wall (van Driest)
   // Fourier / tridiagonal
-  const double2 *twx, *twz;       // exp(-2 pi i m/N), m in [0,N)
+  const double *twx, *twz;        // pass tables of the x and z transforms (chl_tw_len doubles)
   const double *tri_inv, *tri_m, *tri_c;   // [Ny][Nz][Nxh] Thomas factors
   // state: three velocity sets (start-of-step / stage 1 / stage 2)
   double *U[3], *V[3], *W[3];
@@ -118,7 +140,7 @@ struct ChlInst {
   double *P;                      // actual pressure (centres)
   double *alpha;                  // wall stress [2][Nz][Nx]
   double *bc;                     // pressure BC planes [2][Nz][Nx]
-  double *part;                   // DSM plane partial sums [2][Ny+2][npart]
+  double *part;                   // DSM plane partial sums [2][Ny+2][npart][CHL_DSMF_THREADS]
   int npart, dsm_ppt;             // chunks per plane, points per thread (chl_dsm_ppt)
   double *coef;                   // nu_t coefficient per centre row [Ny+2]
   double *scal;                   // device scalars (CHL_S_*)
@@ -154,6 +176,49 @@ struct F64 {
   __device__ __forceinline__ double mul(double a, double b) const { return fma(a, b, mz); }
 };
 __device__ __forceinline__ F64 f64_of(const ChlInst& I) { return F64{I.fk[FK_ONE], I.fk[FK_MZERO]}; }
+
+// fmax(x, 0.0) on the integer pipe: x where its bit pattern is that of a
+// positive finite number or +inf, else +0 (negative numbers, zeros and NaN,
+// for which fmax returns its other operand, 0).  The FP64 pipe, which bounds
+// the per-point kernels, would otherwise spend an instruction on the clip.
+__device__ __forceinline__ double chl_pos(double x) {
+  long long r;
+  asm("{\n\t.reg .pred p;\n\t"
+      "setp.gt.s64 p, %1, 0;\n\t"
+      "setp.le.and.s64 p, %1, 0x7FF0000000000000, p;\n\t"
+      "selp.b64 %0, %1, 0, p;\n\t}"
+      : "=l"(r) : "l"(__double_as_longlong(x)));
+  return __longlong_as_double(r);
+}
+
+// Square root for the per-point strain magnitudes: Heron's iteration
+// x <- x + (a - x^2) / (2x), in the coupled form with a reciprocal square
+// root y ~ 1/sqrt(a) (Markstein, IBM J. Res. Dev. 34 (1990) 111), seeded by
+// the GPU's approximate reciprocal square root (rsqrt.approx.f64, relative
+// error below 2^-20): x = a y, then twice x += (a - x^2) y/2.  The error
+// after the first step is about (2^-20)^2, after the second below an ulp.
+// Five FP64-pipe instructions (one multiply, four FMAs) against eight for
+// the correctly rounded sqrt(), and within one ulp of it
+// (chl_sqrt_selftest).  y/2 is an exponent decrement on the integer pipe.
+// Only positive normal a take this path (one unsigned compare); zero,
+// subnormal, negative, infinite and NaN a go to sqrt(), so every special
+// case is IEEE's (a negative argument gives NaN, as the reference's ** 0.5).
+// The special arguments' sqrt() is a call, not inlined: inlined, the
+// compiler may predicate its instructions into the common path, where every
+// warp would issue them.
+static __device__ __noinline__ double chl_sqrt_special(double a) { return sqrt(a); }
+__device__ __forceinline__ double chl_sqrt(double a) {
+  const unsigned long long ub = (unsigned long long)__double_as_longlong(a);
+  if (ub - (1ULL << 52) >= 0x7FF0000000000000ULL - (1ULL << 52)) return chl_sqrt_special(a);
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(a));
+  const double h = __longlong_as_double(__double_as_longlong(y) - (1LL << 52));
+  double x = a * y;
+  double r = fma(-x, x, a);
+  x = fma(r, h, x);
+  r = fma(-x, x, a);
+  return fma(r, h, x);
+}
 
 // device scalar slots
 enum {

@@ -56,17 +56,70 @@ __device__ __forceinline__ void dft_small(double2* v, bool inv) {
   }
 }
 
+// Twiddle multiplications in tangent form (E. Linzer and E. Feig, Modified
+// FFTs for fused multiply-add architectures, Math. Comp. 60 (1993) 347): a
+// twiddle w = C + iS
+// is kept as a scale sigma and a multiplier m with |m| <= 1 - sigma = C,
+// m = S/C where |C| >= |S|, else sigma = S, m = C/S - so v w = sigma y with
+// y two FMAs away from v, and each sigma is folded into an FMA of the
+// butterfly instead of costing a multiplication.  A radix-4 butterfly with
+// twiddles then takes 22 FP64 instructions instead of 28, a radix-3 one 16
+// instead of 22, a radix-2 one 6 instead of 8.  The choice of form and the
+// sign flips of the inverse transform (conjugate twiddles) are integer
+// operations on bit patterns, which the FP64-bound passes get for free.
+//
+// Pass table of a length N, per pass with twiddles (sub-transform size
+// Ns > 1, radix R), CHL_TW_F fields of Ns entries, entry jm being the
+// butterflies j with j mod Ns = jm (twiddles w_r = exp(-2 pi i jm r/(Ns R)),
+// r = 1..R-1, in the forward direction):
+//   0 m1, 1 m2, 2 m3 (radix 4) or sin(2 pi/3) sigma1 (radix 3), 3 sigma1,
+//   4 sigma2 (radix 4) or sigma1 / 2 (radix 3), 5 sigma3/sigma1 (radix 4)
+//   or sigma2/sigma1 (radix 3), 6 form bits (bit r set: w_r in the S form),
+//   stored as the bit pattern of a double.
+// The sign flips and operand selects are inline PTX: written as C++ the
+// compiler folds "FMA of two selects on one condition" into two FMAs and a
+// select, which doubles the FP64 work these forms exist to save.
+__device__ __forceinline__ double flip(double x, unsigned f) {
+  long long r;
+  asm("{\n\t.reg .b64 t;\n\tcvt.u64.u32 t, %2;\n\tshl.b64 t, t, 63;\n\txor.b64 %0, %1, t;\n\t}"
+      : "=l"(r) : "l"(__double_as_longlong(x)), "r"(f));
+  return __longlong_as_double(r);
+}
+// v w / sigma: (a - b m, b + a m) in the C form, (a m - b, b m + a) =
+// (-(b - a m), a + b m) in the S form.  With (p, q) = (b, a) in the C form
+// and (a, b) in the S form both are (+/- fma(p, -m, q), fma(q, m, p)): two
+// selects and, in the S form, a sign flip of the first component.  The flip
+// XORs a mask chosen between 0 and sgn, the bit pattern of -0.0 read from
+// device memory: were the mask visibly the sign bit, ptxas would turn the
+// flip into a pair of predicated FMAs, one per form, and every warp would
+// issue both.
+__device__ __forceinline__ double2 tw_apply(double2 v, double m, unsigned sform, long long sgn) {
+  long long p, q, t;
+  asm("{\n\t.reg .pred s;\n\t"
+      "setp.ne.u32 s, %5, 0;\n\t"
+      "selp.b64 %0, %3, %4, s;\n\t"     // p = S form ? a : b
+      "selp.b64 %1, %4, %3, s;\n\t"     // q = S form ? b : a
+      "selp.b64 %2, %6, 0, s;\n\t}"     // t = S form ? sgn : 0
+      : "=l"(p), "=l"(q), "=l"(t)
+      : "l"(__double_as_longlong(v.x)), "l"(__double_as_longlong(v.y)), "r"(sform), "l"(sgn));
+  const double P = __longlong_as_double(p), Q = __longlong_as_double(q);
+  return make_double2(__longlong_as_double(__double_as_longlong(fma(P, -m, Q)) ^ t), fma(Q, m, P));
+}
+__device__ __forceinline__ double2 fma2(double s, double2 y, double2 v) {
+  return make_double2(fma(s, y.x, v.x), fma(s, y.y, v.y));
+}
+
 // Work items (row, butterfly j) are numbered so that consecutive threads
 // touch neighbouring shared-memory words: j fastest when a row is contiguous
 // (es = 1, the x lines), the row fastest when rows are interleaved (rs = 1,
 // the z columns), which keeps the 16-byte accesses free of bank conflicts.
-// tw is the N-entry twiddle table, staged in shared memory by the caller.
+// tab: this pass's table (Ns > 1), staged in shared memory by the caller.
 template <int R>
 __device__ void stockham_pass(const double2* __restrict__ x, double2* __restrict__ y, int nrows, int rs, int es,
-                              int N, int Ns, const double2* __restrict__ tw, bool inv) {
+                              int N, int Ns, const double* __restrict__ tab, bool inv, long long sgn) {
   const int nb = N / R;
-  const int tstep = N / (Ns * R);
   const bool rowfast = rs < es;
+  const unsigned iv = inv ? 1u : 0u;
   for (int w = threadIdx.x; w < nrows * nb; w += blockDim.x) {
     int row, j;
     if (rowfast) { j = w / nrows; row = w - j * nrows; }
@@ -77,38 +130,73 @@ __device__ void stockham_pass(const double2* __restrict__ x, double2* __restrict
     double2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = xr[(j + r * nb) * es];
-    if (Ns > 1) {
-#pragma unroll
-      for (int r = 1; r < R; ++r) {
-        double2 t = tw[jm * r * tstep];
-        if (inv) t.y = -t.y;
-        v[r] = cmul(v[r], t);
+    if (Ns == 1) {
+      dft_small<R>(v, inv);
+    } else {
+      const unsigned fb = (unsigned)__double_as_longlong(tab[6 * Ns + jm]);
+      const unsigned f1 = (fb >> 1) & 1u, f2 = (fb >> 2) & 1u;
+      const double s1 = flip(tab[3 * Ns + jm], iv & f1);
+      const double2 y1 = tw_apply(v[1], flip(tab[jm], iv), f1, sgn);
+      if (R == 2) {
+        const double2 v0 = v[0];
+        v[0] = fma2(s1, y1, v0);
+        v[1] = fma2(-s1, y1, v0);
+      } else if (R == 4) {
+        const unsigned f3 = (fb >> 3) & 1u;
+        const double2 y2 = tw_apply(v[2], flip(tab[Ns + jm], iv), f2, sgn);
+        const double2 y3 = tw_apply(v[3], flip(tab[2 * Ns + jm], iv), f3, sgn);
+        const double s2 = flip(tab[4 * Ns + jm], iv & f2);
+        const double rho = flip(tab[5 * Ns + jm], iv & (f1 ^ f3));
+        const double2 a = fma2(s2, y2, v[0]), b = fma2(-s2, y2, v[0]);
+        const double2 c = fma2(rho, y3, y1), e = fma2(-rho, y3, y1);
+        // (v1 w1 - v3 w3) times -i (forward) or +i (inverse) is s1 e times it
+        const double si = flip(s1, iv);
+        v[0] = fma2(s1, c, a);
+        v[2] = fma2(-s1, c, a);
+        v[1] = make_double2(fma(si, e.y, b.x), fma(-si, e.x, b.y));
+        v[3] = make_double2(fma(-si, e.y, b.x), fma(si, e.x, b.y));
+      } else {   // R == 3
+        const double2 y2 = tw_apply(v[2], flip(tab[Ns + jm], iv), f2, sgn);
+        const double h1 = flip(tab[4 * Ns + jm], iv & f1);
+        const double rho = flip(tab[5 * Ns + jm], iv & (f1 ^ f2));
+        // forward: out1,2 = t -/+ i sin(2pi/3) (v1 w1 - v2 w2); inverse +/-
+        const double k1 = flip(tab[2 * Ns + jm], iv & (f1 ^ 1u));
+        const double2 sp = fma2(rho, y2, y1), dp = fma2(-rho, y2, y1);
+        const double2 v0 = v[0];
+        const double2 t = fma2(-h1, sp, v0);
+        v[0] = fma2(s1, sp, v0);
+        v[1] = make_double2(fma(k1, dp.y, t.x), fma(-k1, dp.x, t.y));
+        v[2] = make_double2(fma(-k1, dp.y, t.x), fma(k1, dp.x, t.y));
       }
     }
-    dft_small<R>(v, inv);
     const int idxD = (j / Ns) * Ns * R + jm;
 #pragma unroll
     for (int r = 0; r < R; ++r) yr[(idxD + r * Ns) * es] = v[r];
   }
 }
 
-// Copies the N-entry twiddle table into shared memory; the first barrier of
-// fft_smem orders it before any use.
-__device__ __forceinline__ void stage_twiddles(double2* tws, const double2* __restrict__ tw, int N) {
-  for (int w = threadIdx.x; w < N; w += blockDim.x) tws[w] = LDG(tw + w);
+// Copies a length's pass table (len doubles) into shared memory; the first
+// barrier of fft_smem orders it before any use.
+__device__ __forceinline__ void stage_twiddles(double* tws, const double* __restrict__ tab, int len) {
+  for (int w = threadIdx.x; w < len; w += blockDim.x) tws[w] = LDG(tab + w);
 }
 
-// Full transform; returns the buffer holding the result (a or b).  tw: the
-// twiddle table in shared memory (stage_twiddles).
+// Full transform; returns the buffer holding the result (a or b).  tab: the
+// length's pass table in shared memory (stage_twiddles); sgn: the bit
+// pattern of -0.0 from the instance's constants (see tw_apply).
 __device__ double2* fft_smem(double2* a, double2* b, int nrows, int rs, int es, int N,
-                             const double2* tw, bool inv) {
-  int Ns = 1, rem = N;
+                             const double* tab, bool inv, long long sgn) {
+  int Ns = 1, rem = N, off = 0;
   double2 *src = a, *dst = b;
   while (rem > 1) {
     __syncthreads();
-    if (rem % 4 == 0) { stockham_pass<4>(src, dst, nrows, rs, es, N, Ns, tw, inv); Ns *= 4; rem /= 4; }
-    else if (rem % 3 == 0) { stockham_pass<3>(src, dst, nrows, rs, es, N, Ns, tw, inv); Ns *= 3; rem /= 3; }
-    else { stockham_pass<2>(src, dst, nrows, rs, es, N, Ns, tw, inv); Ns *= 2; rem /= 2; }
+    const int R = chl_fft_radix(rem);
+    const double* tp = tab + off;
+    if (R == 4) stockham_pass<4>(src, dst, nrows, rs, es, N, Ns, tp, inv, sgn);
+    else if (R == 3) stockham_pass<3>(src, dst, nrows, rs, es, N, Ns, tp, inv, sgn);
+    else stockham_pass<2>(src, dst, nrows, rs, es, N, Ns, tp, inv, sgn);
+    if (Ns > 1) off += CHL_TW_F * Ns;
+    Ns *= R; rem /= R;
     double2* t = src; src = dst; dst = t;
   }
   __syncthreads();
@@ -133,8 +221,8 @@ k_div_fftx(ChlMap map, int s_in, int mode, int xmb) {
   const int cr_n = min(CR, nrow - g0);
   double2* A = sm;
   double2* B = sm + CR * Nx;
-  double2* T = sm + 2 * CR * Nx;        // twiddles
-  stage_twiddles(T, I.twx, Nx);
+  double* T = reinterpret_cast<double*>(sm + 2 * CR * Nx);   // pass table
+  stage_twiddles(T, I.twx, chl_tw_len(Nx));
   const double *U, *V, *W;
   if (mode == 0) { U = I.U[s_in]; V = I.V[s_in]; W = I.W[s_in]; }
   else { U = I.Fp[0]; V = I.Fp[1]; W = I.Fp[2]; }
@@ -163,7 +251,7 @@ k_div_fftx(ChlMap map, int s_in, int mode, int xmb) {
     }
     A[cr * Nx + i] = make_double2(dv[0], dv[1]);
   }
-  double2* res = fft_smem(A, B, cr_n, Nx, 1, Nx, T, false);
+  double2* res = fft_smem(A, B, cr_n, Nx, 1, Nx, T, false, __double_as_longlong(I.fk[FK_MZERO]));
   // split the packed spectrum into the two half-spectra (each times 2)
   for (int w = threadIdx.x; w < cr_n * Nxh; w += blockDim.x) {
     const int cr = w / Nxh, kx = w - cr * Nxh;
@@ -200,14 +288,14 @@ k_fftz(ChlMap map, int inv, int zcw) {
   __syncthreads();
   double2* A = sm;
   double2* B = sm + Nz * zcw;
-  double2* T = sm + 2 * Nz * zcw;       // twiddles
-  stage_twiddles(T, I.twz, Nz);
+  double* T = reinterpret_cast<double*>(sm + 2 * Nz * zcw);   // pass table
+  stage_twiddles(T, I.twz, chl_tw_len(Nz));
   double2* spec = I.spec;
   for (int w = threadIdx.x; w < Nz * cw; w += blockDim.x) {
     const int k = w / cw, c = w - k * cw;
     A[k * zcw + c] = spec[coff[c] + (size_t)k * Nxh];
   }
-  double2* res = fft_smem(A, B, cw, 1, zcw, Nz, T, inv != 0);
+  double2* res = fft_smem(A, B, cw, 1, zcw, Nz, T, inv != 0, __double_as_longlong(I.fk[FK_MZERO]));
   for (int w = threadIdx.x; w < Nz * cw; w += blockDim.x) {
     const int k = w / cw, c = w - k * cw;
     spec[coff[c] + (size_t)k * Nxh] = res[k * zcw + c];
@@ -488,22 +576,23 @@ k_zsolve(ChlMap map) {
   const size_t ps = (size_t)modes;              // row pitch of spec and factors
   double2* A = sm;
   double2* B = sm + (size_t)L * Nz;
-  double2* T = sm + (size_t)2 * L * Nz;
-  double2* fz = T + Nz;                         // forward lane values
+  double* T = reinterpret_cast<double*>(sm + (size_t)2 * L * Nz);   // pass table
+  double2* fz = reinterpret_cast<double2*>(reinterpret_cast<char*>(T) + chl_tw_bytes(chl_tw_len(Nz)));
+                                                // forward lane values
   double2* bw = fz + Nz;                        // backward lane values
   double2* yin = bw + Nz;
   double2* xin = yin + Nz;
   double* fA = reinterpret_cast<double*>(xin + Nz);
   double* bA = fA + Nz;
   const int t = threadIdx.x, bd = blockDim.x;
-  stage_twiddles(T, I.twz, Nz);
+  stage_twiddles(T, I.twz, chl_tw_len(Nz));
   // rows [lo, hi) of column kx: element (row l, kz) at l + kz*nr
   double2* spec = I.spec + ps + kx;             // row jc = 1
   for (int w = t; w < nr * Nz; w += bd) {
     const int l = w % nr, kz = w / nr;
     A[l + (size_t)kz * nr] = spec[(size_t)(lo + l) * ps + (size_t)kz * Nxh];
   }
-  double2* res = fft_smem(A, B, nr, 1, nr, Nz, T, false);
+  double2* res = fft_smem(A, B, nr, 1, nr, Nz, T, false, __double_as_longlong(I.fk[FK_MZERO]));
   double2* other = res == A ? B : A;
   const double* __restrict__ fi = I.tri_inv + kx;
   const double* __restrict__ fm = I.tri_m + kx;
@@ -614,7 +703,7 @@ k_zsolve(ChlMap map) {
       res[(j - lo) + (size_t)kz * nr] = d;
     }
   }
-  double2* out = fft_smem(res, other, nr, 1, nr, Nz, T, true);
+  double2* out = fft_smem(res, other, nr, 1, nr, Nz, T, true, __double_as_longlong(I.fk[FK_MZERO]));
   for (int w = t; w < nr * Nz; w += bd) {
     const int l = w % nr, kz = w / nr;
     spec[(size_t)(lo + l) * ps + (size_t)kz * Nxh] = out[l + (size_t)kz * nr];
@@ -636,8 +725,8 @@ k_fftx_inv(ChlMap map, int dst, int xmb) {
   const int cr_n = min(CR, nrow - g0);
   double2* A = sm;
   double2* B = sm + CR * Nx;
-  double2* T = sm + 2 * CR * Nx;        // twiddles
-  stage_twiddles(T, I.twx, Nx);
+  double* T = reinterpret_cast<double*>(sm + 2 * CR * Nx);   // pass table
+  stage_twiddles(T, I.twx, chl_tw_len(Nx));
   for (int w = threadIdx.x; w < cr_n * Nx; w += blockDim.x) {
     const int cr = w / Nx, kx = w - cr * Nx;
     const int g = g0 + cr;
@@ -649,7 +738,7 @@ k_fftx_inv(ChlMap map, int dst, int xmb) {
     A[cr * Nx + kx] = lo ? make_double2(pa.x - pb.y, pa.y + pb.x)
                          : make_double2(pa.x + pb.y, pb.x - pa.y);
   }
-  double2* res = fft_smem(A, B, cr_n, Nx, 1, Nx, T, true);
+  double2* res = fft_smem(A, B, cr_n, Nx, 1, Nx, T, true, __double_as_longlong(I.fk[FK_MZERO]));
   double* out = dst == 0 ? I.p : I.P;
   for (int w = threadIdx.x; w < cr_n * Nx; w += blockDim.x) {
     const int cr = w / Nx, i = w - cr * Nx;
@@ -737,17 +826,20 @@ __global__ void k_pghost(ChlMap map) {
 }
 
 extern "C" {
-// two ping-pong tiles plus the twiddle table
-size_t chl_smem_fftx(int Nx, int nrow, int xmb) { return ((size_t)2 * chl_fftx_rows(Nx, nrow, xmb) + 1) * Nx * sizeof(double2); }
-size_t chl_smem_fftz(int maxNz, int zcw) { return ((size_t)2 * zcw + 1) * maxNz * sizeof(double2); }
+// two ping-pong tiles plus the pass table (twz: the longest z pass table
+// of the launch's instances, in doubles)
+size_t chl_smem_fftx(int Nx, int nrow, int xmb) {
+  return (size_t)2 * chl_fftx_rows(Nx, nrow, xmb) * Nx * sizeof(double2) + chl_tw_bytes(chl_tw_len(Nx));
+}
+size_t chl_smem_fftz(int maxNz, int zcw, int twz) { return (size_t)2 * zcw * maxNz * sizeof(double2) + chl_tw_bytes(twz); }
 // kx columns staged per z-transform block: 16, halved while two Nz x cols
 // complex tiles would exceed the 227 KB a block may use, and halved (down
 // to 2) while the grid over all `ncols` columns would have fewer than
 // min_blocks blocks (CHL_FFT_MIN_BLOCKS, about four per SM, unless the
 // tuner chose another)
-int chl_fftz_cols(int maxNz, long ncols, int min_blocks) {
+int chl_fftz_cols(int maxNz, long ncols, int min_blocks, int twz) {
   int c = 16;
-  while (c > 1 && chl_smem_fftz(maxNz, c) > (size_t)227 * 1024) c /= 2;
+  while (c > 1 && chl_smem_fftz(maxNz, c, twz) > (size_t)227 * 1024) c /= 2;
   while (c > 2 && (ncols + c - 1) / c < min_blocks) c /= 2;
   return c;
 }
@@ -788,7 +880,8 @@ size_t chl_smem_zsolve(int Nx, int Ny, int Nz) {
   const int P = chl_tri_lanes((long)Nz * Nxh, Ny);
   if (P != 1 && P != 2 && P != 4 && P != 8) return 0;
   const int L = (Ny + P - 1) / P;
-  const size_t b = (size_t)2 * L * Nz * sizeof(double2) + (size_t)5 * Nz * sizeof(double2) + (size_t)2 * Nz * sizeof(double);
+  const size_t b = (size_t)2 * L * Nz * sizeof(double2) + chl_tw_bytes(chl_tw_len(Nz)) + (size_t)4 * Nz * sizeof(double2) +
+                   (size_t)2 * Nz * sizeof(double);
   return b <= (size_t)227 * 1024 ? b : 0;
 }
 int chl_zsolve_setup(size_t smem) {

@@ -30,8 +30,8 @@ void chl_launch_amd(const ChlMap&, int, int, int, cudaStream_t);
 void chl_launch_vreman(const ChlMap&, int, int, int, cudaStream_t);
 void chl_launch_agent_obs(const ChlInst*, int, int, double, const int*, const double*, double*, double*, cudaStream_t);
 size_t chl_smem_fftx(int, int, int);
-size_t chl_smem_fftz(int, int);
-int chl_fftz_cols(int, long, int);
+size_t chl_smem_fftz(int, int, int);
+int chl_fftz_cols(int, long, int, int);
 int chl_fft_setup(size_t, size_t, size_t);
 size_t chl_smem_tri(int, long, int);
 int chl_tri_modes_per_block(size_t);
@@ -63,6 +63,7 @@ int chl_mlp_setup();
 void chl_launch_mlp(const ChlMap&, int, int, int, int*, cudaStream_t);
 void chl_launch_mlp_test(const float*, const float*, const float*, int, float*, float*, int*, cudaStream_t);
 int chl_tc_selftest_launch(const void*, const void*, float*, int, int*, cudaStream_t);
+void chl_launch_sqrt_selftest(const double*, double*, long, cudaStream_t);
 }
 
 namespace {
@@ -213,9 +214,49 @@ struct Arena {
   size_t take(size_t bytes) { size_t o = off; off += (bytes + 255) & ~(size_t)255; return o; }
 };
 
+// Pass table of the length-N Stockham FFT (layout in chl_fft.cu): per pass
+// with twiddles and butterfly class jm, the twiddles w_r = C + iS =
+// exp(-2 pi i m/N), m = jm r N/(Ns R), each as sigma (C or S, the larger in
+// magnitude) and m (S/C or C/S), and the butterfly's combined scales.
+std::vector<double> fft_pass_table(int N) {
+  std::vector<double> t((size_t)chl_tw_len(N));
+  const double pi = 4.0 * std::atan(1.0);
+  const double s3 = 0.86602540378443864676;   // sin(2 pi/3)
+  int Ns = 1, rem = N;
+  size_t off = 0;
+  while (rem > 1) {
+    const int R = chl_fft_radix(rem);
+    if (Ns > 1) {
+      const int tstep = N / (Ns * R);
+      for (int jm = 0; jm < Ns; ++jm) {
+        double sg[4] = {1.0, 1.0, 1.0, 1.0}, mu[4] = {0.0, 0.0, 0.0, 0.0};
+        long long forms = 0;
+        for (int r = 1; r < R; ++r) {
+          const int m = jm * r * tstep;
+          const double C = std::cos(2.0 * pi * m / N), S = -std::sin(2.0 * pi * m / N);
+          const bool sform = std::fabs(S) > std::fabs(C);
+          sg[r] = sform ? S : C;
+          mu[r] = sform ? C / S : S / C;
+          if (sform) forms |= 1LL << r;
+        }
+        auto put = [&](int f, double v) { t[off + (size_t)f * Ns + jm] = v; };
+        put(0, mu[1]); put(1, mu[2]); put(3, sg[1]);
+        if (R == 4) { put(2, mu[3]); put(4, sg[2]); put(5, sg[3] / sg[1]); }
+        else if (R == 3) { put(2, s3 * sg[1]); put(4, 0.5 * sg[1]); put(5, sg[2] / sg[1]); }
+        double fd;
+        std::memcpy(&fd, &forms, 8);
+        put(6, fd);
+      }
+      off += (size_t)CHL_TW_F * Ns;
+    }
+    Ns *= R; rem /= R;
+  }
+  return t;
+}
+
 int dsm_npart(int Nx, int Ny, int Nz) {
   const int p = chl_dsm_ppt(Nx, Ny, Nz);
-  return (Nx * Nz + CHL_DSMF_THREADS * p - 1) / (CHL_DSMF_THREADS * p);
+  return (chl_dsm_points(Nx, Nz) + CHL_DSMF_THREADS * p - 1) / (CHL_DSMF_THREADS * p);
 }
 
 }  // namespace
@@ -249,6 +290,7 @@ struct chl_handle {
   bool zsolve = false;                // the fused form is in use
   int zlanes = 1;                     // its cluster size
   size_t smem_zs = 0;
+  int twz = 0;                        // longest z pass table of the instances (doubles)
   int tb_pt = 256;                    // threads per block of the point maps (stencils, updates)
   bool tri_scan = false;              // some instance splits its tridiagonal columns (chl_tri_lanes)
   int LES_model = 0, wall_model = 0, any_mass = 0;
@@ -297,7 +339,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   size_t o_rdxc2 = A.take(8 * (Nx + 3)), o_rdyc2 = A.take(8 * (Ny + 2)), o_rdzc2 = A.take(8 * (Nz + 3));
   size_t o_w0u = A.take(8 * (Ny + 2)), o_w1u = A.take(8 * (Ny + 2));
   size_t o_csd = A.take(8 * (Ny + 2)), o_dw = A.take(8 * (Ny + 2));
-  size_t o_twx = A.take(16 * Nx), o_twz = A.take(16 * Nz);
+  size_t o_twx = A.take(8 * (size_t)chl_tw_len(Nx)), o_twz = A.take(8 * (size_t)chl_tw_len(Nz));
   size_t o_ti = A.take(8 * ntri), o_tm = A.take(8 * ntri), o_tc = A.take(8 * ntri);
   // state
   size_t o_U[3], o_V[3], o_W[3], o_F1[3], o_Fp[3];
@@ -313,7 +355,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   for (int m = 0; m < 3; ++m) o_E[m] = A.take(8 * nc);
   size_t o_spec = A.take(16 * nspec), o_p = A.take(8 * nc), o_P = A.take(8 * nc);
   size_t o_alpha = A.take(8 * 2 * (size_t)Nx * Nz), o_bc = A.take(8 * 2 * (size_t)Nx * Nz);
-  size_t o_part = A.take(8 * 2 * (size_t)(Ny + 2) * npart);
+  size_t o_part = A.take(8 * 2 * (size_t)(Ny + 2) * npart * CHL_DSMF_THREADS);   // one partial per DSM thread
   size_t o_coef = A.take(8 * (Ny + 2)), o_scal = A.take(8 * CHL_S_NSCAL);
   size_t o_min = A.take(8 * (size_t)(Nx + Ny + 1 + Nz)), o_status = A.take(64);
   size_t o_dcnt = A.take(4 * (size_t)(Ny + 2));
@@ -364,7 +406,7 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.rdxc2 = P(o_rdxc2) + 1; D.rdyc2 = P(o_rdyc2); D.rdzc2 = P(o_rdzc2) + 1;
   D.w0 = P(o_w0u); D.w1 = P(o_w1u);
   D.smag_csdelta = P(o_csd); D.smag_dwall = P(o_dw);
-  D.twx = (const double2*)(base + o_twx); D.twz = (const double2*)(base + o_twz);
+  D.twx = (const double*)(base + o_twx); D.twz = (const double*)(base + o_twz);
   D.tri_inv = P(o_ti); D.tri_m = P(o_tm); D.tri_c = P(o_tc);
   for (int s = 0; s < 3; ++s) { D.U[s] = P(o_U[s]); D.V[s] = P(o_V[s]); D.W[s] = P(o_W[s]); D.F1[s] = P(o_F1[s]); D.Fp[s] = P(o_Fp[s]); }
   D.nut = P(o_nut); D.S = P(o_S);
@@ -406,12 +448,11 @@ static int upload_consts(chl_handle* h, Inst& I) {
   CK(put(o_rdxc4, times(c.rdxc, 4.0))); CK(put(o_rdyc4, times(c.rdyc, 4.0))); CK(put(o_rdzc4, times(c.rdzc, 4.0)));
   CK(put(o_rdxc2, times(c.rdxc, 2.0))); CK(put(o_rdyc2, times(c.rdyc, 2.0))); CK(put(o_rdzc2, times(c.rdzc, 2.0)));
   CK(put(o_csd, c.csdelta)); CK(put(o_dw, c.dwall));
-  const double pi = 4.0 * std::atan(1.0);
-  std::vector<double> tw(2 * (size_t)std::max(Nx, Nz));
-  for (int m = 0; m < Nx; ++m) { tw[2 * m] = std::cos(2.0 * pi * m / Nx); tw[2 * m + 1] = -std::sin(2.0 * pi * m / Nx); }
-  CK(cudaMemcpy(base + o_twx, tw.data(), 16 * Nx, cudaMemcpyHostToDevice));
-  for (int m = 0; m < Nz; ++m) { tw[2 * m] = std::cos(2.0 * pi * m / Nz); tw[2 * m + 1] = -std::sin(2.0 * pi * m / Nz); }
-  CK(cudaMemcpy(base + o_twz, tw.data(), 16 * Nz, cudaMemcpyHostToDevice));
+  {
+    const std::vector<double> tx = fft_pass_table(Nx), tz = fft_pass_table(Nz);
+    if (!tx.empty()) CK(cudaMemcpy(base + o_twx, tx.data(), 8 * tx.size(), cudaMemcpyHostToDevice));
+    if (!tz.empty()) CK(cudaMemcpy(base + o_twz, tz.data(), 8 * tz.size(), cudaMemcpyHostToDevice));
+  }
   // Thomas factors per mode: denominators of the elimination of
   // Dyy + kxx + kzz (the zgtsv system of projection.f90:97-110), with the
   // 1/(2 Nx Nz) of the packed inverse transform folded into inv.
@@ -456,7 +497,9 @@ static int build_maps(chl_handle* h) {
     zcols += (long)I.c.Ny * I.c.Nxh;
     modes += (long)I.c.Nz * I.c.Nxh;
   }
-  h->zcw = chl_fftz_cols(mz, zcols, h->z_min_blocks);
+  h->twz = 0;
+  for (auto& I : h->in) h->twz = std::max(h->twz, chl_tw_len(I.c.Nz));
+  h->zcw = chl_fftz_cols(mz, zcols, h->z_min_blocks, h->twz);
   h->tz = chl_fft_threads(h->zcw, mz);
   h->tx = 64;
   for (auto& I : h->in) {
@@ -515,7 +558,7 @@ static int build_maps(chl_handle* h) {
   size_t sx = 0;
   for (auto& I : h->in) sx = std::max(sx, chl_smem_fftx(I.c.Nx, I.c.Ny * (I.c.Nz / 2), h->x_min_blocks));
   h->smem_x = sx;
-  h->smem_z = chl_smem_fftz(mz, h->zcw);
+  h->smem_z = chl_smem_fftz(mz, h->zcw, h->twz);
   if (chl_fft_setup(h->smem_x, h->smem_z, h->smem_t)) { h->err = "FFT shared-memory size not supported"; return CHL_E_ARG; }
   if (h->zsolve && chl_zsolve_setup(h->smem_zs)) { h->err = "fused z solve: shared-memory size not supported"; return CHL_E_ARG; }
   if (chl_mlp_setup()) { h->err = "wall-model network shared-memory size not supported"; return CHL_E_ARG; }
@@ -1576,6 +1619,22 @@ int chl_tc_selftest(const unsigned short* A, const unsigned short* B, float* D, 
     else if (st) rc = CHL_E_TIMEOUT;
   }
   cudaFree(dA); cudaFree(dB); cudaFree(dD); cudaFree(ds);
+  return rc;
+}
+
+int chl_sqrt_selftest(const double* a, double* y, long n) {
+  if (!a || !y || n < 0 || n > (1L << 26)) return CHL_E_ARG;
+  if (n == 0) return CHL_OK;
+  double *da = nullptr, *dy = nullptr;
+  int rc = CHL_OK;
+  if (cudaMalloc(&da, 8 * (size_t)n) != cudaSuccess || cudaMalloc(&dy, 8 * (size_t)n) != cudaSuccess) rc = CHL_E_NOMEM;
+  if (!rc) {
+    cudaError_t e = cudaMemcpy(da, a, 8 * (size_t)n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) { chl_launch_sqrt_selftest(da, dy, n, 0); e = cudaGetLastError(); }
+    if (e == cudaSuccess) e = cudaMemcpy(y, dy, 8 * (size_t)n, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) rc = CHL_E_CUDA;
+  }
+  cudaFree(da); cudaFree(dy);
   return rc;
 }
 

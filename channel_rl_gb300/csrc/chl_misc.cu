@@ -414,7 +414,16 @@ __global__ void k_qflow_final(const ChlInst* inst, int slot) {
   I.scal[slot] = q / n;
 }
 
+// chl_sqrt on given values, for its check against correctly rounded roots
+__global__ void k_sqrt_selftest(const double* __restrict__ a, double* __restrict__ y, long n) {
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < n) y[t] = chl_sqrt(a[t]);
+}
+
 extern "C" {
+void chl_launch_sqrt_selftest(const double* a, double* y, long n, cudaStream_t st) {
+  if (n > 0) k_sqrt_selftest<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a, y, n);
+}
 // the minima hold CHL_BIG_BITS between steps: set once here when an
 // instance is created, then by the block of k_minabs that forms dt
 void chl_launch_minabs_init(const ChlMap& m, cudaStream_t st) {

@@ -96,7 +96,7 @@ __device__ __forceinline__ Strain centre_strain(const ChlInst& I, const Faces& f
   // |S|^2 = 2 (d.d) + 4 (S12^2+S13^2+S23^2) = 2 (d.d + (o.o)/32)
   double dd = s.d1 * s.d1; dd = fma(s.d2, s.d2, dd); dd = fma(s.d3, s.d3, dd);
   double oo = s.o12 * s.o12; oo = fma(s.o13, s.o13, oo); oo = fma(s.o23, s.o23, oo);
-  s.s = sqrt(fma(oo, 0.03125, dd));   // |S| / sqrt(2)
+  s.s = chl_sqrt(fma(oo, 0.03125, dd));   // |S| / sqrt(2)
   return s;
 }
 
@@ -245,12 +245,14 @@ k_filter_xz(ChlMap map, int from_r) {
 }
 
 // ------------------------------------------------------------ L:M, M:M
-// One block of CHL_DSMF_THREADS per (centre row jc, chunk of the x-z plane);
-// each thread sums its points in a fixed order, then a fixed-order block
-// reduction writes part[0|1][jc][chunk].  Filtered fields live in r after
-// the three passes.  The last block of a row to finish (a counter per row)
-// adds the row's partials - thread t the chunks t, t + CHL_DSMF_THREADS, ...
-// in order, then the same block tree - and writes the row's coefficient
+// One block of CHL_DSMF_THREADS per (centre row jc, chunk of the row's
+// chl_dsm_points points); each thread sums its points in a fixed order and
+// writes its partials to part[0|1][jc][chunk][thread] (no reduction tree in
+// every block: its mostly idle warps would issue an FP64 instruction per
+// level for a handful of lanes).  Filtered fields live in r after the three
+// passes.  The last block of a row to finish (a counter per row) adds the
+// row's partials - thread t the entries t, t + CHL_DSMF_THREADS, ... in
+// order, then a fixed-order block tree - and writes the row's coefficient
 // -1/2 <LM>/<MM>, then returns the counter to 0.
 __device__ __forceinline__ void block_sum2(double* sl, double* sm, double& a, double& b) {
   sl[threadIdx.x] = a; sm[threadIdx.x] = b;
@@ -266,33 +268,44 @@ __device__ __forceinline__ void block_sum2(double* sl, double* sm, double& a, do
 // note above); L and M are both stored / 216, so <LM>/<MM> = lm/mm (times
 // the sqrt(2) that the strain leaves out).  Whole block; every thread gets it.
 __device__ __forceinline__ double dsm_row_coef(const ChlInst& I, int jc, double* sl, double* sm) {
-  const int np = I.npart, Ny = I.Ny;
+  const size_t n = (size_t)I.npart * CHL_DSMF_THREADS;
+  const double* pl = I.part + (size_t)jc * n;
+  const double* pm = I.part + (size_t)(I.Ny + 2) * n + (size_t)jc * n;
   double lm = 0.0, mm = 0.0;
-  for (int q = threadIdx.x; q < np; q += CHL_DSMF_THREADS) {
-    lm += __ldcg(I.part + (size_t)jc * np + q);
-    mm += __ldcg(I.part + (size_t)(Ny + 2) * np + (size_t)jc * np + q);
+  for (size_t q = threadIdx.x; q < n; q += CHL_DSMF_THREADS) {
+    lm += __ldcg(pl + q);
+    mm += __ldcg(pm + q);
   }
   __syncthreads();
   block_sum2(sl, sm, lm, mm);
   return -0.125 * (lm / mm);
 }
 
-__global__ void __launch_bounds__(CHL_DSMF_THREADS)
-k_dsm_final(ChlMap map) {
-  chl_pdl_wait();
-  int lb;
-  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
-  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  const int np = I.npart;
-  const int jc = 1 + lb / np, chunk = lb % np;
-  const int plane = Nx * Nz;
-  double lm = 0.0, mm = 0.0;
+// One thread's points of row jc: the diagonal and off-diagonal parts of L:M
+// and M:M, each a chain of FMAs straight into its accumulator (the
+// off-diagonal scales 1/4 and 1/32 are applied once by the caller).  The
+// point set is the plane followed by the reference's duplicated periodic
+// column and plane (chl_dsm_points), so every point has weight 1.
+// WALL: row 1 or Ny, whose filtered centre velocities were filtered in their
+// own right; a template parameter rather than a per-point select, since the
+// row is the same for the whole block.
+template <bool WALL>
+__device__ __forceinline__ void dsm_sums(const ChlInst& I, int jc, int chunk, double& ald, double& alo,
+                                         double& amd, double& amo) {
+  const int Nx = I.Nx, Nz = I.Nz;
+  const int plane = Nx * Nz, npts = chl_dsm_points(Nx, Nz);
   const double* const* R = I.r;
   const int ppt = I.dsm_ppt;
   for (int m = 0; m < ppt; ++m) {
     const int pidx = chunk * (CHL_DSMF_THREADS * ppt) + m * CHL_DSMF_THREADS + threadIdx.x;
-    if (pidx >= plane) break;
-    const int i = pidx % Nx, k = pidx / Nx;
+    if (pidx >= npts) break;
+    int i, k;
+    if (pidx < plane) { i = pidx % Nx; k = pidx / Nx; }
+    else {                                   // the duplicated column, plane and (0, 0)
+      const int e = pidx - plane;
+      i = e < Nz ? 0 : (e < Nz + Nx ? e - Nz : 0);
+      k = e < Nz ? e : 0;
+    }
     const size_t c = cidx(I, i, jc, k);
     const Faces f = centre_faces(I, R[15], R[16], R[17], i, jc, k);    // 216 x filtered faces
     const Strain h = centre_strain(I, f, i, jc, k);                     // 216 x filtered strain
@@ -308,10 +321,9 @@ k_dsm_final(ChlMap map) {
     const double M6 = fma(s4, h.o23, -LDG(R[14] + c));
     // 2 x 216 x filtered centre velocities: filtered in their own right on
     // the wall rows, the centre average of the filtered faces elsewhere
-    const bool wall_row = jc == 1 || jc == Ny;
-    const double fu = wall_row ? LDG(R[0] + c) : f.u0 + f.u1;
-    const double fv = wall_row ? LDG(R[1] + c) : f.v0 + f.v1;
-    const double fw = wall_row ? LDG(R[2] + c) : f.w0 + f.w1;
+    const double fu = WALL ? LDG(R[0] + c) : f.u0 + f.u1;
+    const double fv = WALL ? LDG(R[1] + c) : f.v0 + f.v1;
+    const double fw = WALL ? LDG(R[2] + c) : f.w0 + f.w1;
     const double gu = fu * (1.0 / 216.0), gv = fv * (1.0 / 216.0);
     const double L1 = fma(-gu, fu, LDG(R[3] + c));
     const double L2 = fma(-gv, fv, LDG(R[4] + c));
@@ -319,25 +331,33 @@ k_dsm_final(ChlMap map) {
     const double L4 = fma(-gu, fv, LDG(R[6] + c));
     const double L5 = fma(-gu, fw, LDG(R[7] + c));
     const double L6 = fma(-gv, fw, LDG(R[8] + c));
-    double ld = L1 * M1; ld = fma(L2, M2, ld); ld = fma(L3, M3, ld);
-    double lo = L4 * M4; lo = fma(L5, M5, lo); lo = fma(L6, M6, lo);
-    double md = M1 * M1; md = fma(M2, M2, md); md = fma(M3, M3, md);
-    double mo = M4 * M4; mo = fma(M5, M5, mo); mo = fma(M6, M6, mo);
-    double lmp = fma(0.25, lo, ld), mmp = fma(0.03125, mo, md);
-    // duplicated periodic column i=2 and plane k=2 of the reference's sums
-    const double wgt = i == 0 ? (k == 0 ? 4.0 : 2.0) : (k == 0 ? 2.0 : 1.0);
-    lm = fma(wgt, lmp, lm);
-    mm = fma(wgt, mmp, mm);
+    ald = fma(L1, M1, ald); ald = fma(L2, M2, ald); ald = fma(L3, M3, ald);
+    alo = fma(L4, M4, alo); alo = fma(L5, M5, alo); alo = fma(L6, M6, alo);
+    amd = fma(M1, M1, amd); amd = fma(M2, M2, amd); amd = fma(M3, M3, amd);
+    amo = fma(M4, M4, amo); amo = fma(M5, M5, amo); amo = fma(M6, M6, amo);
   }
+}
+
+__global__ void __launch_bounds__(CHL_DSMF_THREADS)
+k_dsm_final(ChlMap map) {
+  chl_pdl_wait();
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Ny = I.Ny;
+  const int np = I.npart;
+  const int jc = 1 + lb / np, chunk = lb % np;
+  double ald = 0.0, alo = 0.0, amd = 0.0, amo = 0.0;
+  if (jc == 1 || jc == Ny) dsm_sums<true>(I, jc, chunk, ald, alo, amd, amo);
+  else dsm_sums<false>(I, jc, chunk, ald, alo, amd, amo);
+  const size_t n = (size_t)np * CHL_DSMF_THREADS;
+  const size_t q = (size_t)jc * n + (size_t)chunk * CHL_DSMF_THREADS + threadIdx.x;
+  I.part[q] = fma(0.25, alo, ald);
+  I.part[(size_t)(Ny + 2) * n + q] = fma(0.03125, amo, amd);
+  __threadfence();
   __shared__ double sl[CHL_DSMF_THREADS], sm[CHL_DSMF_THREADS];
   __shared__ int last;
-  block_sum2(sl, sm, lm, mm);
-  if (threadIdx.x == 0) {
-    I.part[(size_t)jc * np + chunk] = lm;
-    I.part[(size_t)(Ny + 2) * np + (size_t)jc * np + chunk] = mm;
-    __threadfence();
-    last = atomicAdd(I.dsm_cnt + jc, 1) == np - 1;     // the row's last block
-  }
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(I.dsm_cnt + jc, 1) == np - 1;     // the row's last block
   __syncthreads();
   if (last) {
     __threadfence();
@@ -465,7 +485,7 @@ k_nut(ChlMap map, int s_in, int use_wm) {
     const int js = jc == 0 ? 1 : (jc == Ny + 1 ? Ny : jc);
     // AMD and Vreman store nu_t itself in S (row coefficient 1)
     const double sv = I.S[cidx(I, i, js, k)];
-    v = fmax(I.LES_model >= 3 ? sv : I.coef[js] * sv, 0.0);
+    v = chl_pos(I.LES_model >= 3 ? sv : I.coef[js] * sv);
     if (ghost) v = nut_ghost(I, v);
   }
   // stored as nu + nu_t: every consumer adds nu (equations.f90:139-155)

@@ -110,7 +110,7 @@ __device__ __forceinline__ void write_nut_rows(const ChlInst& I, const double* U
     nt[cidx(I, i, jc == 1 ? 0 : Ny + 1, k)] = nu + w;
     return;
   }
-  const double vc = fmax(v, 0.0);
+  const double vc = chl_pos(v);
   nt[cidx(I, i, jc, k)] = nu + vc;
   if (jc == 1) nt[cidx(I, i, 0, k)] = nu + nut_ghost(I, vc);
   if (jc == Ny) nt[cidx(I, i, Ny + 1, k)] = nu + nut_ghost(I, vc);
@@ -195,7 +195,7 @@ k_vreman(ChlMap map, int s_in, int use_wm) {
   double Ao = a4 * a4;
   Ao = fma(a5, a5, Ao); Ao = fma(a6, a6, Ao); Ao = fma(a7, a7, Ao); Ao = fma(a8, a8, Ao); Ao = fma(a9, a9, Ao);
   Ab = fma(0.0625, Ao, Ab);
-  const double v = 2.5 * (0.1 * 0.1) * sqrt(Bb / Ab);
+  const double v = 2.5 * (0.1 * 0.1) * chl_sqrt(Bb / Ab);
   if (valid) I.S[cidx(I, i, jc, k)] = v;
   write_nut_rows(I, I.U[s_in], i, jc, k, v, use_wm, valid);
 }

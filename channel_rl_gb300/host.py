@@ -77,6 +77,7 @@ EXPORTS = (
     "chl_check_divergence_noalloc", "chl_noalloc_last_error", "chl_device_reset",
     "chl_mlp_set_params", "chl_mlp_get_params", "chl_mlp_configure", "chl_mlp_read_trace",
     "chl_mlp_eval", "chl_mlp_set_exploration", "chl_mlp_debug", "chl_mlp_read_record", "chl_tc_selftest",
+    "chl_sqrt_selftest",
     "chl_snapshot_dims", "chl_snapshot_read", "chl_snapshot_write", "chl_io_last_error",
     "chl_read_parameters", "chl_save_snapshot", "chl_load_snapshot",
     "chl_agent_observe", "chl_agent_act", "chl_status_flags",
@@ -145,6 +146,7 @@ def load(build_if_missing=True):
     lib.chl_mlp_debug.argtypes = [H, C.c_int, C.c_int]
     lib.chl_mlp_read_record.argtypes = [H, C.c_int, _F32P]
     lib.chl_tc_selftest.argtypes = [C.POINTER(C.c_ushort), C.POINTER(C.c_ushort), _F32P, C.c_int]
+    lib.chl_sqrt_selftest.argtypes = [_F64P, _F64P, C.c_long]
     I = C.POINTER(C.c_int)
     lib.chl_snapshot_dims.argtypes = [C.c_char_p, I, I, I]
     lib.chl_snapshot_read.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int] + [_F64P] * 6
@@ -255,6 +257,17 @@ def tc_selftest(A_bf16_bits, B_bf16_bits, variant=0):
     if rc:
         raise ChlError(f"chl_tc_selftest failed ({rc})", rc)
     return D
+
+
+def sqrt_selftest(a):
+    """The library's device square root (the strain magnitudes' root) of a."""
+    lib = load()
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    y = np.empty_like(a)
+    rc = lib.chl_sqrt_selftest(a.ctypes.data_as(_F64P), y.ctypes.data_as(_F64P), a.size)
+    if rc:
+        raise ChlError(f"chl_sqrt_selftest failed ({rc})", rc)
+    return y
 
 
 def grid_constants(case: Case):

@@ -247,6 +247,11 @@ int chl_mlp_read_record(chl_handle* h, int inst, float* rec);
  * completion barrier that nothing arrives at: it frees its TMEM and returns
  * CHL_E_TIMEOUT (the bounded-wait path of the wall-model kernel). */
 int chl_tc_selftest(const unsigned short* A, const unsigned short* B, float* D, int variant);
+/* Standalone check of the square root the strain magnitudes use (a Newton
+ * iteration seeded by the GPU's approximate reciprocal square root; IEEE
+ * results for zero, subnormal, negative, infinite and NaN arguments):
+ * y[t] = that root of a[t] for n <= 2^26 values in host memory. */
+int chl_sqrt_selftest(const double* a, double* y, long n);
 
 /* Allocation-free divergence check, for callers that must not let a
  * library allocate device memory (their device memory comes from their own
