@@ -121,6 +121,9 @@ struct ChlInst {
   const double *w0, *w1;          // weight_y_0/1 by face row jv (w1 = 1 - w0)
   const double *rdxc4, *rdyc4, *rdzc4;   // 4 x rdxc, rdyc, rdzc (centre fluxes, kept 4 x)
   const double *rdxc2, *rdyc2, *rdzc2;   // 2 x rdxc, rdyc, rdzc (xy and yz edge fluxes, kept 2 x)
+  // sqrt(4/216) x rdxc, rdyc, rdzc and rdxf, rdyf, rdzf: the dynamic model's
+  // filtered strain, whose M_ij term needs 4/216 x |S| S_ij
+  const double *rdxcs, *rdycs, *rdzcs, *rdxfs, *rdyfs, *rdzfs;
   const double *ygc;              // yg(1..nyg), centre y coordinates with the ghost rows
   const double *smag_csdelta;     // Cs*Delta_j by centre row (static Smagorinsky)
   const double *smag_dwall;       // distance of centre row to the nearer wall (van Driest)
@@ -188,6 +191,19 @@ __device__ __forceinline__ double chl_pos(double x) {
       "setp.le.and.s64 p, %1, 0x7FF0000000000000, p;\n\t"
       "selp.b64 %0, %1, 0, p;\n\t}"
       : "=l"(r) : "l"(__double_as_longlong(x)));
+  return __longlong_as_double(r);
+}
+
+// max(x, lo) for lo > 0 on the integer pipe: x where its bit pattern lies in
+// [bits(lo), bits(+inf)] (for non-negative numbers the order of the bit
+// patterns is the order of the values), else lo - also for a NaN x.
+__device__ __forceinline__ double chl_atleast(double x, double lo) {
+  long long r;
+  asm("{\n\t.reg .pred p;\n\t"
+      "setp.ge.s64 p, %1, %2;\n\t"
+      "setp.le.and.s64 p, %1, 0x7FF0000000000000, p;\n\t"
+      "selp.b64 %0, %1, %2, p;\n\t}"
+      : "=l"(r) : "l"(__double_as_longlong(x)), "l"(__double_as_longlong(lo)));
   return __longlong_as_double(r);
 }
 

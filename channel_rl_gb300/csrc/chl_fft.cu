@@ -114,12 +114,19 @@ __device__ __forceinline__ double2 fma2(double s, double2 y, double2 v) {
 // (es = 1, the x lines), the row fastest when rows are interleaved (rs = 1,
 // the z columns), which keeps the 16-byte accesses free of bank conflicts.
 // tab: this pass's table (Ns > 1), staged in shared memory by the caller.
-template <int R>
+// TW: the pass has twiddles (Ns > 1) - a template parameter, not a branch
+// on Ns inside the loop: ptxas predicates both sides of such a branch, and
+// a predicated-off FP64 instruction still takes its turn on the FP64 pipe
+// (measured: 2 extra instructions per complex point over a 128-point
+// transform).
+// INV (the inverse transform) likewise: a runtime direction would put
+// predicated sign flips into every butterfly.
+template <int R, bool TW, bool INV>
 __device__ void stockham_pass(const double2* __restrict__ x, double2* __restrict__ y, int nrows, int rs, int es,
-                              int N, int Ns, const double* __restrict__ tab, bool inv, long long sgn) {
+                              int N, int Ns, const double* __restrict__ tab, long long sgn) {
   const int nb = N / R;
   const bool rowfast = rs < es;
-  const unsigned iv = inv ? 1u : 0u;
+  constexpr unsigned iv = INV ? 1u : 0u;
   for (int w = threadIdx.x; w < nrows * nb; w += blockDim.x) {
     int row, j;
     if (rowfast) { j = w / nrows; row = w - j * nrows; }
@@ -130,8 +137,8 @@ __device__ void stockham_pass(const double2* __restrict__ x, double2* __restrict
     double2 v[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) v[r] = xr[(j + r * nb) * es];
-    if (Ns == 1) {
-      dft_small<R>(v, inv);
+    if (!TW) {
+      dft_small<R>(v, INV);
     } else {
       const unsigned fb = (unsigned)__double_as_longlong(tab[6 * Ns + jm]);
       const unsigned f1 = (fb >> 1) & 1u, f2 = (fb >> 2) & 1u;
@@ -184,23 +191,36 @@ __device__ __forceinline__ void stage_twiddles(double* tws, const double* __rest
 // Full transform; returns the buffer holding the result (a or b).  tab: the
 // length's pass table in shared memory (stage_twiddles); sgn: the bit
 // pattern of -0.0 from the instance's constants (see tw_apply).
-__device__ double2* fft_smem(double2* a, double2* b, int nrows, int rs, int es, int N,
-                             const double* tab, bool inv, long long sgn) {
+template <bool INV>
+__device__ double2* fft_smem_dir(double2* a, double2* b, int nrows, int rs, int es, int N,
+                                 const double* tab, long long sgn) {
   int Ns = 1, rem = N, off = 0;
   double2 *src = a, *dst = b;
   while (rem > 1) {
     __syncthreads();
     const int R = chl_fft_radix(rem);
     const double* tp = tab + off;
-    if (R == 4) stockham_pass<4>(src, dst, nrows, rs, es, N, Ns, tp, inv, sgn);
-    else if (R == 3) stockham_pass<3>(src, dst, nrows, rs, es, N, Ns, tp, inv, sgn);
-    else stockham_pass<2>(src, dst, nrows, rs, es, N, Ns, tp, inv, sgn);
+    if (R == 4) {
+      if (Ns == 1) stockham_pass<4, false, INV>(src, dst, nrows, rs, es, N, Ns, tp, sgn);
+      else stockham_pass<4, true, INV>(src, dst, nrows, rs, es, N, Ns, tp, sgn);
+    } else if (R == 3) {
+      if (Ns == 1) stockham_pass<3, false, INV>(src, dst, nrows, rs, es, N, Ns, tp, sgn);
+      else stockham_pass<3, true, INV>(src, dst, nrows, rs, es, N, Ns, tp, sgn);
+    } else {
+      if (Ns == 1) stockham_pass<2, false, INV>(src, dst, nrows, rs, es, N, Ns, tp, sgn);
+      else stockham_pass<2, true, INV>(src, dst, nrows, rs, es, N, Ns, tp, sgn);
+    }
     if (Ns > 1) off += CHL_TW_F * Ns;
     Ns *= R; rem /= R;
     double2* t = src; src = dst; dst = t;
   }
   __syncthreads();
   return src;
+}
+__device__ __forceinline__ double2* fft_smem(double2* a, double2* b, int nrows, int rs, int es, int N,
+                                             const double* tab, bool inv, long long sgn) {
+  return inv ? fft_smem_dir<true>(a, b, nrows, rs, es, N, tab, sgn)
+             : fft_smem_dir<false>(a, b, nrows, rs, es, N, tab, sgn);
 }
 
 

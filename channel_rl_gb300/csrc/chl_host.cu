@@ -337,6 +337,8 @@ static int upload_consts(chl_handle* h, Inst& I) {
   size_t o_w0 = A.take(8 * (Ny + 2)), o_w1 = A.take(8 * (Ny + 2)), o_ygc = A.take(8 * (Ny + 2));
   size_t o_rdxc4 = A.take(8 * (Nx + 3)), o_rdyc4 = A.take(8 * (Ny + 2)), o_rdzc4 = A.take(8 * (Nz + 3));
   size_t o_rdxc2 = A.take(8 * (Nx + 3)), o_rdyc2 = A.take(8 * (Ny + 2)), o_rdzc2 = A.take(8 * (Nz + 3));
+  size_t o_rdxcs = A.take(8 * (Nx + 3)), o_rdycs = A.take(8 * (Ny + 2)), o_rdzcs = A.take(8 * (Nz + 3));
+  size_t o_rdxfs = A.take(8 * (Nx + 3)), o_rdyfs = A.take(8 * (Ny + 2)), o_rdzfs = A.take(8 * (Nz + 3));
   size_t o_w0u = A.take(8 * (Ny + 2)), o_w1u = A.take(8 * (Ny + 2));
   size_t o_csd = A.take(8 * (Ny + 2)), o_dw = A.take(8 * (Ny + 2));
   size_t o_twx = A.take(8 * (size_t)chl_tw_len(Nx)), o_twz = A.take(8 * (size_t)chl_tw_len(Nz));
@@ -404,6 +406,8 @@ static int upload_consts(chl_handle* h, Inst& I) {
   D.rdyc = P(o_rdyc); D.rdyf = P(o_rdyf); D.dyf = P(o_dyf); D.w0x2 = P(o_w0); D.w1x2 = P(o_w1); D.ygc = P(o_ygc);
   D.rdxc4 = P(o_rdxc4) + 1; D.rdyc4 = P(o_rdyc4); D.rdzc4 = P(o_rdzc4) + 1;
   D.rdxc2 = P(o_rdxc2) + 1; D.rdyc2 = P(o_rdyc2); D.rdzc2 = P(o_rdzc2) + 1;
+  D.rdxcs = P(o_rdxcs) + 1; D.rdycs = P(o_rdycs); D.rdzcs = P(o_rdzcs) + 1;
+  D.rdxfs = P(o_rdxfs) + 1; D.rdyfs = P(o_rdyfs); D.rdzfs = P(o_rdzfs) + 1;
   D.w0 = P(o_w0u); D.w1 = P(o_w1u);
   D.smag_csdelta = P(o_csd); D.smag_dwall = P(o_dw);
   D.twx = (const double*)(base + o_twx); D.twz = (const double*)(base + o_twz);
@@ -442,11 +446,14 @@ static int upload_consts(chl_handle* h, Inst& I) {
     for (auto& x : scaled.back()) x *= f;
     return scaled.back();
   };
-  scaled.reserve(8);
+  scaled.reserve(16);
   CK(put(o_w0, times(c.w0, 2.0))); CK(put(o_w1, times(c.w1, 2.0)));
   CK(put(o_w0u, c.w0)); CK(put(o_w1u, c.w1));
   CK(put(o_rdxc4, times(c.rdxc, 4.0))); CK(put(o_rdyc4, times(c.rdyc, 4.0))); CK(put(o_rdzc4, times(c.rdzc, 4.0)));
   CK(put(o_rdxc2, times(c.rdxc, 2.0))); CK(put(o_rdyc2, times(c.rdyc, 2.0))); CK(put(o_rdzc2, times(c.rdzc, 2.0)));
+  const double fs = std::sqrt(4.0 / 216.0);
+  CK(put(o_rdxcs, times(c.rdxc, fs))); CK(put(o_rdycs, times(c.rdyc, fs))); CK(put(o_rdzcs, times(c.rdzc, fs)));
+  CK(put(o_rdxfs, times(c.rdxf, fs))); CK(put(o_rdyfs, times(c.rdyf, fs))); CK(put(o_rdzfs, times(c.rdzf, fs)));
   CK(put(o_csd, c.csdelta)); CK(put(o_dw, c.dwall));
   {
     const std::vector<double> tx = fft_pass_table(Nx), tz = fft_pass_table(Nz);

@@ -25,7 +25,8 @@
 // E12 at (x-face a, y-face jv, z-centre k), E13 at (x-face a, centre row jc,
 // z-face b), E23 at (x-centre i, y-face jv, z-face b): 2 x the edge strain
 // rates of compute_Sij, stored V-like (E12, E23: Ny+1 rows) and centre-like
-// (E13, rows 1..Ny).
+// (E13, rows 1..Ny).  Of the filtered faces (src 3) with the reciprocals
+// scaled by sqrt(4/216) (rdxfs ...), for the filtered strain of k_dsm_final.
 __global__ void __launch_bounds__(256)
 k_edges(ChlMap map, int src) {
   chl_pdl_wait();
@@ -41,7 +42,9 @@ k_edges(ChlMap map, int src) {
   if (src < 3) { U = I.U[src]; V = I.V[src]; W = I.W[src]; }
   else { U = I.r[15]; V = I.r[16]; W = I.r[17]; }
   const int ap = wrap(a + 1, Nx), kp = wrap(k + 1, Nz);
-  const double rxf = LDG(I.rdxf + a), rzf = LDG(I.rdzf + k), ryf = LDG(I.rdyf + j);
+  const bool filt = src == 3;
+  const double rxf = LDG((filt ? I.rdxfs : I.rdxf) + a), rzf = LDG((filt ? I.rdzfs : I.rdzf) + k);
+  const double ryf = LDG((filt ? I.rdyfs : I.rdyf) + j);
   const F64 f = f64_of(I);   // differences and products as register FMAs
   // E12 (jv = j): dU/dy + dV/dx
   const double e12 = fma(f.sub(LDG(U + cidx(I, a, j + 1, k)), LDG(U + cidx(I, a, j, k))), ryf,
@@ -80,12 +83,15 @@ __device__ __forceinline__ Faces centre_faces(const ChlInst& I, const double* U,
   return f;
 }
 
+// FILT: the filtered strain, with the sqrt(4/216)-scaled reciprocals and
+// edges, so that it comes out times sqrt(4/216)
+template <bool FILT>
 __device__ __forceinline__ Strain centre_strain(const ChlInst& I, const Faces& f, int i, int jc, int k) {
   const int im = wrap(i - 1, I.Nx), km = wrap(k - 1, I.Nz);
   Strain s;
-  s.d1 = (f.u1 - f.u0) * LDG(I.rdxc + i);
-  s.d2 = (f.v1 - f.v0) * LDG(I.rdyc + jc);
-  s.d3 = (f.w1 - f.w0) * LDG(I.rdzc + k);
+  s.d1 = (f.u1 - f.u0) * LDG((FILT ? I.rdxcs : I.rdxc) + i);
+  s.d2 = (f.v1 - f.v0) * LDG((FILT ? I.rdycs : I.rdyc) + jc);
+  s.d3 = (f.w1 - f.w0) * LDG((FILT ? I.rdzcs : I.rdzc) + k);
   const double* E12 = I.E[0]; const double* E13 = I.E[1]; const double* E23 = I.E[2];
   s.o12 = (LDG(E12 + vidx(I, im, jc - 1, k)) + LDG(E12 + vidx(I, i, jc - 1, k)))
         + (LDG(E12 + vidx(I, im, jc, k)) + LDG(E12 + vidx(I, i, jc, k)));
@@ -120,7 +126,7 @@ k_centre(ChlMap map, int s_in, int dsm) {
   const int jc = 1 + (int)((t / Nx) % Ny);
   const int k = (int)(t / ((long)Nx * Ny));
   const Faces f = centre_faces(I, I.U[s_in], I.V[s_in], I.W[s_in], i, jc, k);
-  const Strain s = centre_strain(I, f, i, jc, k);
+  const Strain s = centre_strain<false>(I, f, i, jc, k);
   const size_t c = cidx(I, i, jc, k);
   I.S[c] = s.s;
   if (!dsm) return;
@@ -308,17 +314,17 @@ __device__ __forceinline__ void dsm_sums(const ChlInst& I, int jc, int chunk, do
     }
     const size_t c = cidx(I, i, jc, k);
     const Faces f = centre_faces(I, R[15], R[16], R[17], i, jc, k);    // 216 x filtered faces
-    const Strain h = centre_strain(I, f, i, jc, k);                     // 216 x filtered strain
+    const Strain h = centre_strain<true>(I, f, i, jc, k);               // sqrt(4/216) x 216 x filtered strain
     // M_ij / 216: the 216 of the filtered |S| S_ij terms moves into the
-    // strain factor (4/216); L_ij / 216: the filtered velocities are divided
+    // strain factor (4/216, as sqrt(4/216) in each of |S| and S_ij, from the
+    // scaled reciprocals); L_ij / 216: the filtered velocities are divided
     // once, each product is then one FMA; k_coef's constant carries both
-    const double s4 = h.s * (4.0 / 216.0);
-    const double M1 = fma(s4, h.d1, -LDG(R[9] + c));
-    const double M2 = fma(s4, h.d2, -LDG(R[10] + c));
-    const double M3 = fma(s4, h.d3, -LDG(R[11] + c));
-    const double M4 = fma(s4, h.o12, -LDG(R[12] + c));
-    const double M5 = fma(s4, h.o13, -LDG(R[13] + c));
-    const double M6 = fma(s4, h.o23, -LDG(R[14] + c));
+    const double M1 = fma(h.s, h.d1, -LDG(R[9] + c));
+    const double M2 = fma(h.s, h.d2, -LDG(R[10] + c));
+    const double M3 = fma(h.s, h.d3, -LDG(R[11] + c));
+    const double M4 = fma(h.s, h.o12, -LDG(R[12] + c));
+    const double M5 = fma(h.s, h.o13, -LDG(R[13] + c));
+    const double M6 = fma(h.s, h.o23, -LDG(R[14] + c));
     // 2 x 216 x filtered centre velocities: filtered in their own right on
     // the wall rows, the centre average of the filtered faces elsewhere
     const double fu = WALL ? LDG(R[0] + c) : f.u0 + f.u1;
@@ -476,20 +482,25 @@ k_nut(ChlMap map, int s_in, int use_wm) {
   const double f = wmrow ? wm_face(I, U, i, k, wall) : 0.0;
   const double f_left = __shfl_up_sync(0xffffffffu, f, 1);
   if (!valid) return;
-  double v = 0.0;
+  // stored as nu + nu_t: every consumer adds nu (equations.f90:139-155)
+  double* out = I.nut + cidx(I, i, jc, k);
   if (wmrow) {
     const double fl = ((threadIdx.x & 31) > 0 && i > 0) ? f_left : wm_face(I, U, wrap(i - 1, Nx), k, wall);
-    v = 0.5 * (fl + f);
-  } else if (I.LES_model != 0) {
-    const bool ghost = jc == 0 || jc == Ny + 1;
-    const int js = jc == 0 ? 1 : (jc == Ny + 1 ? Ny : jc);
-    // AMD and Vreman store nu_t itself in S (row coefficient 1)
+    *out = I.nu + 0.5 * (fl + f);
+  } else if (I.LES_model == 0) {
+    *out = I.nu;
+  } else if (jc == 0 || jc == Ny + 1) {         // ghost rows: the rule of Dirichlet_nu_t
+    const int js = jc == 0 ? 1 : Ny;
     const double sv = I.S[cidx(I, i, js, k)];
-    v = chl_pos(I.LES_model >= 3 ? sv : I.coef[js] * sv);
-    if (ghost) v = nut_ghost(I, v);
+    *out = I.nu + nut_ghost(I, chl_pos(I.LES_model >= 3 ? sv : I.coef[js] * sv));
+  } else if (I.LES_model >= 3) {                // AMD and Vreman store nu_t itself in S
+    *out = I.nu + chl_pos(I.S[cidx(I, i, jc, k)]);
+  } else {
+    // nu + max(0, c |S|) as one FMA, nu + c |S|, clipped below at nu by the
+    // bit patterns (both positive; a NaN, for which max gives 0, gives nu)
+    const double nu = I.nu;
+    *out = chl_atleast(fma(I.coef[jc], I.S[cidx(I, i, jc, k)], nu), nu);
   }
-  // stored as nu + nu_t: every consumer adds nu (equations.f90:139-155)
-  I.nut[cidx(I, i, jc, k)] = I.nu + v;
 }
 
 // ------------------------------------------------------------ launchers
