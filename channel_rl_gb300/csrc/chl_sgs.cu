@@ -62,6 +62,50 @@ k_edges(ChlMap map, int src) {
   }
 }
 
+// The same edges, with the x-pair sums that every centre strain needs
+// formed once per edge: P12(a) = E12(a-1) + E12(a) and P13(a) = E13(a-1) +
+// E13(a) are stored in place of E12 and E13 (E23 as it is).  A block of 256
+// threads holds 256 / Nx whole x-rows (j, k) (Nx <= 256), so the left
+// neighbour, periodic, comes from shared memory: one addition per edge
+// instead of two per centre.  The centre strain's sums keep their order,
+// (E(i-1) + E(i)) + (E'(i-1) + E'(i)), so the result is bit-identical.
+__global__ void __launch_bounds__(256)
+k_edges_pair(ChlMap map, int src) {
+  chl_pdl_wait();
+  __shared__ double s12[256], s13[256];
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const int RB = 256 / Nx;
+  const int r = threadIdx.x / Nx, a = threadIdx.x - r * Nx;
+  const long g = (long)lb * RB + r;                  // the row (j, k), j = 0..Ny
+  const bool valid = r < RB && g < (long)(Ny + 1) * Nz;
+  const int j = valid ? (int)(g % (Ny + 1)) : 0, k = valid ? (int)(g / (Ny + 1)) : 0;
+  const double *U, *V, *W;
+  if (src < 3) { U = I.U[src]; V = I.V[src]; W = I.W[src]; }
+  else { U = I.r[15]; V = I.r[16]; W = I.r[17]; }
+  const int ap = wrap(a + 1, Nx), kp = wrap(k + 1, Nz);
+  const bool filt = src == 3;
+  const double rxf = LDG((filt ? I.rdxfs : I.rdxf) + a), rzf = LDG((filt ? I.rdzfs : I.rdzf) + k);
+  const double ryf = LDG((filt ? I.rdyfs : I.rdyf) + j);
+  const F64 f = f64_of(I);   // differences and products as register FMAs
+  const double e12 = fma(f.sub(LDG(U + cidx(I, a, j + 1, k)), LDG(U + cidx(I, a, j, k))), ryf,
+                         f.mul(f.sub(LDG(V + vidx(I, ap, j, k)), LDG(V + vidx(I, a, j, k))), rxf));
+  const double e23 = fma(f.sub(LDG(V + vidx(I, a, j, kp)), LDG(V + vidx(I, a, j, k))), rzf,
+                         f.mul(f.sub(LDG(W + cidx(I, a, j + 1, k)), LDG(W + cidx(I, a, j, k))), ryf));
+  // E13 on the centre rows 1..Ny (row 0 computes an unused value from the ghost row)
+  const double e13 = fma(f.sub(LDG(U + cidx(I, a, j, kp)), LDG(U + cidx(I, a, j, k))), rzf,
+                         f.mul(f.sub(LDG(W + cidx(I, ap, j, k)), LDG(W + cidx(I, a, j, k))), rxf));
+  s12[threadIdx.x] = e12;
+  s13[threadIdx.x] = e13;
+  __syncthreads();
+  if (!valid) return;
+  const int left = r * Nx + (a == 0 ? Nx - 1 : a - 1);
+  I.E[0][vidx(I, a, j, k)] = s12[left] + e12;
+  I.E[2][vidx(I, a, j, k)] = e23;
+  if (j >= 1) I.E[1][cidx(I, a, j, k)] = s13[left] + e13;
+}
+
 // Centre strain: diagonal D, 8*S_offdiag O (sum of four edges), and
 // s = |S|/sqrt(2).  The sqrt(2) never needs forming: nu_t = c |S| where the
 // dynamic model's c comes from L:M / M:M with M linear in |S| and |S^| (so
@@ -84,8 +128,9 @@ __device__ __forceinline__ Faces centre_faces(const ChlInst& I, const double* U,
 }
 
 // FILT: the filtered strain, with the sqrt(4/216)-scaled reciprocals and
-// edges, so that it comes out times sqrt(4/216)
-template <bool FILT>
+// edges, so that it comes out times sqrt(4/216).  PAIR: E12 and E13 hold the
+// x-pair sums of k_edges_pair.
+template <bool FILT, bool PAIR>
 __device__ __forceinline__ Strain centre_strain(const ChlInst& I, const Faces& f, int i, int jc, int k) {
   const int im = wrap(i - 1, I.Nx), km = wrap(k - 1, I.Nz);
   Strain s;
@@ -93,10 +138,15 @@ __device__ __forceinline__ Strain centre_strain(const ChlInst& I, const Faces& f
   s.d2 = (f.v1 - f.v0) * LDG((FILT ? I.rdycs : I.rdyc) + jc);
   s.d3 = (f.w1 - f.w0) * LDG((FILT ? I.rdzcs : I.rdzc) + k);
   const double* E12 = I.E[0]; const double* E13 = I.E[1]; const double* E23 = I.E[2];
-  s.o12 = (LDG(E12 + vidx(I, im, jc - 1, k)) + LDG(E12 + vidx(I, i, jc - 1, k)))
-        + (LDG(E12 + vidx(I, im, jc, k)) + LDG(E12 + vidx(I, i, jc, k)));
-  s.o13 = (LDG(E13 + cidx(I, im, jc, km)) + LDG(E13 + cidx(I, i, jc, km)))
-        + (LDG(E13 + cidx(I, im, jc, k)) + LDG(E13 + cidx(I, i, jc, k)));
+  if (PAIR) {
+    s.o12 = LDG(E12 + vidx(I, i, jc - 1, k)) + LDG(E12 + vidx(I, i, jc, k));
+    s.o13 = LDG(E13 + cidx(I, i, jc, km)) + LDG(E13 + cidx(I, i, jc, k));
+  } else {
+    s.o12 = (LDG(E12 + vidx(I, im, jc - 1, k)) + LDG(E12 + vidx(I, i, jc - 1, k)))
+          + (LDG(E12 + vidx(I, im, jc, k)) + LDG(E12 + vidx(I, i, jc, k)));
+    s.o13 = (LDG(E13 + cidx(I, im, jc, km)) + LDG(E13 + cidx(I, i, jc, km)))
+          + (LDG(E13 + cidx(I, im, jc, k)) + LDG(E13 + cidx(I, i, jc, k)));
+  }
   s.o23 = (LDG(E23 + vidx(I, i, jc - 1, km)) + LDG(E23 + vidx(I, i, jc, km)))
         + (LDG(E23 + vidx(I, i, jc - 1, k)) + LDG(E23 + vidx(I, i, jc, k)));
   // |S|^2 = 2 (d.d) + 4 (S12^2+S13^2+S23^2) = 2 (d.d + (o.o)/32)
@@ -114,8 +164,11 @@ __device__ __forceinline__ Strain centre_strain(const ChlInst& I, const Faces& f
 // forms it there); only rows 1 and Ny, where the centre filter takes its
 // one-sided rule and the face filter does not, need the centre velocity
 // filtered in its own right.
+// DSM and PAIR are template parameters: a runtime switch would leave the
+// FP64 work of the other side predicated in every warp.
+template <bool DSM, bool PAIR>
 __global__ void __launch_bounds__(256)
-k_centre(ChlMap map, int s_in, int dsm) {
+k_centre(ChlMap map, int s_in) {
   chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
@@ -126,10 +179,10 @@ k_centre(ChlMap map, int s_in, int dsm) {
   const int jc = 1 + (int)((t / Nx) % Ny);
   const int k = (int)(t / ((long)Nx * Ny));
   const Faces f = centre_faces(I, I.U[s_in], I.V[s_in], I.W[s_in], i, jc, k);
-  const Strain s = centre_strain<false>(I, f, i, jc, k);
+  const Strain s = centre_strain<false, PAIR>(I, f, i, jc, k);
   const size_t c = cidx(I, i, jc, k);
   I.S[c] = s.s;
-  if (!dsm) return;
+  if (!DSM) return;
   const double uc = f.u0 + f.u1, vc = f.v0 + f.v1, wc = f.w0 + f.w1;
   if (jc <= 2 || jc >= Ny - 1) { I.q[0][c] = uc; I.q[1][c] = vc; I.q[2][c] = wc; }
   I.q[3][c] = uc * uc; I.q[4][c] = vc * vc; I.q[5][c] = wc * wc;
@@ -295,7 +348,7 @@ __device__ __forceinline__ double dsm_row_coef(const ChlInst& I, int jc, double*
 // WALL: row 1 or Ny, whose filtered centre velocities were filtered in their
 // own right; a template parameter rather than a per-point select, since the
 // row is the same for the whole block.
-template <bool WALL>
+template <bool WALL, bool PAIR>
 __device__ __forceinline__ void dsm_sums(const ChlInst& I, int jc, int chunk, double& ald, double& alo,
                                          double& amd, double& amo) {
   const int Nx = I.Nx, Nz = I.Nz;
@@ -314,7 +367,7 @@ __device__ __forceinline__ void dsm_sums(const ChlInst& I, int jc, int chunk, do
     }
     const size_t c = cidx(I, i, jc, k);
     const Faces f = centre_faces(I, R[15], R[16], R[17], i, jc, k);    // 216 x filtered faces
-    const Strain h = centre_strain<true>(I, f, i, jc, k);               // sqrt(4/216) x 216 x filtered strain
+    const Strain h = centre_strain<true, PAIR>(I, f, i, jc, k);               // sqrt(4/216) x 216 x filtered strain
     // M_ij / 216: the 216 of the filtered |S| S_ij terms moves into the
     // strain factor (4/216, as sqrt(4/216) in each of |S| and S_ij, from the
     // scaled reciprocals); L_ij / 216: the filtered velocities are divided
@@ -344,6 +397,7 @@ __device__ __forceinline__ void dsm_sums(const ChlInst& I, int jc, int chunk, do
   }
 }
 
+template <bool PAIR>
 __global__ void __launch_bounds__(CHL_DSMF_THREADS)
 k_dsm_final(ChlMap map) {
   chl_pdl_wait();
@@ -353,8 +407,8 @@ k_dsm_final(ChlMap map) {
   const int np = I.npart;
   const int jc = 1 + lb / np, chunk = lb % np;
   double ald = 0.0, alo = 0.0, amd = 0.0, amo = 0.0;
-  if (jc == 1 || jc == Ny) dsm_sums<true>(I, jc, chunk, ald, alo, amd, amo);
-  else dsm_sums<false>(I, jc, chunk, ald, alo, amd, amo);
+  if (jc == 1 || jc == Ny) dsm_sums<true, PAIR>(I, jc, chunk, ald, alo, amd, amo);
+  else dsm_sums<false, PAIR>(I, jc, chunk, ald, alo, amd, amo);
   const size_t n = (size_t)np * CHL_DSMF_THREADS;
   const size_t q = (size_t)jc * n + (size_t)chunk * CHL_DSMF_THREADS + threadIdx.x;
   I.part[q] = fma(0.25, alo, ald);
@@ -505,13 +559,23 @@ k_nut(ChlMap map, int s_in, int use_wm) {
 
 // ------------------------------------------------------------ launchers
 extern "C" {
-void chl_launch_edges(const ChlMap& m, int nb, int src, cudaStream_t st) { chl_launch_pdl(k_edges, dim3(nb), dim3(m.tb), 0, st, m, src); }
-void chl_launch_centre(const ChlMap& m, int nb, int s_in, int dsm, cudaStream_t st) { chl_launch_pdl(k_centre, dim3(nb), dim3(m.tb), 0, st, m, s_in, dsm); }
+// pair: the x-pair form (k_edges_pair on its row map, blocks of 256)
+void chl_launch_edges(const ChlMap& m, int nb, int src, int pair, cudaStream_t st) {
+  if (pair) chl_launch_pdl(k_edges_pair, dim3(nb), dim3(256), 0, st, m, src);
+  else chl_launch_pdl(k_edges, dim3(nb), dim3(m.tb), 0, st, m, src);
+}
+void chl_launch_centre(const ChlMap& m, int nb, int s_in, int dsm, int pair, cudaStream_t st) {
+  if (dsm && pair) chl_launch_pdl(k_centre<true, true>, dim3(nb), dim3(m.tb), 0, st, m, s_in);
+  else if (dsm) chl_launch_pdl(k_centre<true, false>, dim3(nb), dim3(m.tb), 0, st, m, s_in);
+  else if (pair) chl_launch_pdl(k_centre<false, true>, dim3(nb), dim3(m.tb), 0, st, m, s_in);
+  else chl_launch_pdl(k_centre<false, false>, dim3(nb), dim3(m.tb), 0, st, m, s_in);
+}
 void chl_launch_filter_y(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_filter_y, dim3(nb), dim3(m.tb), 0, st, m, s_in); }
 void chl_launch_filter_x(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<0>, dim3(nb), dim3(m.tb), 0, st, m, 1); }
 void chl_launch_filter_z(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<1>, dim3(nb), dim3(m.tb), 0, st, m, 0); }
-void chl_launch_dsm_final(const ChlMap& m, int nb, cudaStream_t st) {
-  chl_launch_pdl(k_dsm_final, dim3(nb), dim3(CHL_DSMF_THREADS), 0, st, m);
+void chl_launch_dsm_final(const ChlMap& m, int nb, int pair, cudaStream_t st) {
+  if (pair) chl_launch_pdl(k_dsm_final<true>, dim3(nb), dim3(CHL_DSMF_THREADS), 0, st, m);
+  else chl_launch_pdl(k_dsm_final<false>, dim3(nb), dim3(CHL_DSMF_THREADS), 0, st, m);
 }
 void chl_launch_coef(const ChlMap& m, cudaStream_t st) { chl_launch_pdl(k_coef, dim3(m.n), dim3(128), 0, st, m); }
 void chl_launch_eqwm(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_eqwm, dim3(nb), dim3(CHL_WALL_THREADS), 0, st, m, s_in); }
