@@ -292,6 +292,7 @@ struct chl_handle {
   size_t smem_zs = 0;
   int twz = 0;                        // longest z pass table of the instances (doubles)
   bool epair = false;                 // edges as x-pair sums (k_edges_pair): every Nx <= 256
+  int tb_epair = 256;                 // its block: the largest Nx rounded up to a power of two, >= 64
   int tb_pt = 256;                    // threads per block of the point maps (stencils, updates)
   bool tri_scan = false;              // some instance splits its tridiagonal columns (chl_tri_lanes)
   int LES_model = 0, wall_model = 0, any_mass = 0;
@@ -529,7 +530,10 @@ static int build_maps(chl_handle* h) {
   }
   h->zsolve = h->zsolve_ok && (h->tri_mode == 3 || (h->tri_mode == 2 && h->zlanes > 1));
   h->epair = true;
-  for (auto& I : h->in) h->epair = h->epair && I.c.Nx <= 256;
+  int mx = 0;
+  for (auto& I : h->in) { h->epair = h->epair && I.c.Nx <= 256; mx = std::max(mx, I.c.Nx); }
+  h->tb_epair = 64;
+  while (h->tb_epair < mx && h->tb_epair < 256) h->tb_epair *= 2;
   h->smem_t = h->tri_scan ? 0 : chl_smem_tri(my, modes, h->tri_mode);
   const int tri_w = chl_tri_modes_per_block(h->smem_t);
   for (int m = 0; m < NMAP; ++m) {
@@ -555,7 +559,7 @@ static int build_maps(chl_handle* h) {
         case M_WALLN: b = cdiv(2L * Nx * Nz, CHL_WALL_THREADS); break;
         case M_ZPLANE: b = Nz; break;
         case M_ZSOLVE: b = Nxh * h->zlanes; break;
-        case M_EPAIR: b = Nx <= 256 ? cdiv((long)(Ny + 1) * Nz, 256 / Nx) : 1; break;   // whole x-rows per block
+        case M_EPAIR: b = Nx <= h->tb_epair ? cdiv((long)(Ny + 1) * Nz, h->tb_epair / Nx) : 1; break;   // whole x-rows
       }
       off[q + 1] = off[q] + b;
     }
@@ -591,17 +595,17 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
   if (fused) wall_stress();
   if (h->LES_model == CHL_LES_DYNAMIC) {
     KL("edges", chl_launch_edges(h->map(h->epair ? M_EPAIR : M_EDGE), h->nblk[h->epair ? M_EPAIR : M_EDGE], s,
-                                 h->epair, st));
+                                 h->epair ? h->tb_epair : 0, st));
     KL("centre_strain", chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 1, h->epair, st));
     KL("filter_y", chl_launch_filter_y(h->map(M_FULL), h->nblk[M_FULL], s, st));
     KL("filter_x", chl_launch_filter_x(h->map(M_FULL), h->nblk[M_FULL], st));
     KL("filter_z", chl_launch_filter_z(h->map(M_FULL), h->nblk[M_FULL], st));
     KL("edges", chl_launch_edges(h->map(h->epair ? M_EPAIR : M_EDGE), h->nblk[h->epair ? M_EPAIR : M_EDGE], 3,
-                                 h->epair, st));
+                                 h->epair ? h->tb_epair : 0, st));
     KL("dsm_LM_MM", chl_launch_dsm_final(h->map(M_DSMF), h->nblk[M_DSMF], h->epair, st));
   } else if (h->LES_model == CHL_LES_SMAGORINSKY) {
     KL("edges", chl_launch_edges(h->map(h->epair ? M_EPAIR : M_EDGE), h->nblk[h->epair ? M_EPAIR : M_EDGE], s,
-                                 h->epair, st));
+                                 h->epair ? h->tb_epair : 0, st));
     KL("centre_strain", chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 0, h->epair, st));
   } else if (h->LES_model == CHL_LES_AMD) {
     KL("amd", chl_launch_amd(h->map(M_PT), h->nblk[M_PT], s, with_wm ? 1 : 0, st));

@@ -64,9 +64,10 @@ k_edges(ChlMap map, int src) {
 
 // The same edges, with the x-pair sums that every centre strain needs
 // formed once per edge: P12(a) = E12(a-1) + E12(a) and P13(a) = E13(a-1) +
-// E13(a) are stored in place of E12 and E13 (E23 as it is).  A block of 256
-// threads holds 256 / Nx whole x-rows (j, k) (Nx <= 256), so the left
-// neighbour, periodic, comes from shared memory: one addition per edge
+// E13(a) are stored in place of E12 and E13 (E23 as it is).  A block (64,
+// 128 or 256 threads: the launch's largest Nx rounded up to a power of two,
+// at least 64) holds blockDim / Nx whole x-rows (j, k) (Nx <= 256), so the
+// left neighbour, periodic, comes from shared memory: one addition per edge
 // instead of two per centre.  The centre strain's sums keep their order,
 // (E(i-1) + E(i)) + (E'(i-1) + E'(i)), so the result is bit-identical.
 __global__ void __launch_bounds__(256)
@@ -76,7 +77,7 @@ k_edges_pair(ChlMap map, int src) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  const int RB = 256 / Nx;
+  const int RB = blockDim.x / Nx;
   const int r = threadIdx.x / Nx, a = threadIdx.x - r * Nx;
   const long g = (long)lb * RB + r;                  // the row (j, k), j = 0..Ny
   const bool valid = r < RB && g < (long)(Ny + 1) * Nz;
@@ -326,15 +327,28 @@ __device__ __forceinline__ void block_sum2(double* sl, double* sm, double& a, do
 // -1/2 <LM>/<MM>: the filter and average scales give 1/8 (see the scaling
 // note above); L and M are both stored / 216, so <LM>/<MM> = lm/mm (times
 // the sqrt(2) that the strain leaves out).  Whole block; every thread gets it.
+// Thread t adds the partials of chunks t mod 4 = 0..3 into four chains
+// (their loads in flight together: on a small instance this tail is
+// latency, not throughput), then the chains in a fixed order.
 __device__ __forceinline__ double dsm_row_coef(const ChlInst& I, int jc, double* sl, double* sm) {
-  const size_t n = (size_t)I.npart * CHL_DSMF_THREADS;
-  const double* pl = I.part + (size_t)jc * n;
-  const double* pm = I.part + (size_t)(I.Ny + 2) * n + (size_t)jc * n;
-  double lm = 0.0, mm = 0.0;
-  for (size_t q = threadIdx.x; q < n; q += CHL_DSMF_THREADS) {
-    lm += __ldcg(pl + q);
-    mm += __ldcg(pm + q);
+  const int np = I.npart;
+  const size_t n = (size_t)np * CHL_DSMF_THREADS;
+  const double* pl = I.part + (size_t)jc * n + threadIdx.x;
+  const double* pm = I.part + (size_t)(I.Ny + 2) * n + (size_t)jc * n + threadIdx.x;
+  double l[4] = {0.0, 0.0, 0.0, 0.0}, m[4] = {0.0, 0.0, 0.0, 0.0};
+  int c = 0;
+  for (; c + 4 <= np; c += 4) {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      l[u] += __ldcg(pl + (size_t)(c + u) * CHL_DSMF_THREADS);
+      m[u] += __ldcg(pm + (size_t)(c + u) * CHL_DSMF_THREADS);
+    }
   }
+  for (int u = 0; c < np; ++c, ++u) {
+    l[u] += __ldcg(pl + (size_t)c * CHL_DSMF_THREADS);
+    m[u] += __ldcg(pm + (size_t)c * CHL_DSMF_THREADS);
+  }
+  double lm = (l[0] + l[1]) + (l[2] + l[3]), mm = (m[0] + m[1]) + (m[2] + m[3]);
   __syncthreads();
   block_sum2(sl, sm, lm, mm);
   return -0.125 * (lm / mm);
@@ -559,9 +573,9 @@ k_nut(ChlMap map, int s_in, int use_wm) {
 
 // ------------------------------------------------------------ launchers
 extern "C" {
-// pair: the x-pair form (k_edges_pair on its row map, blocks of 256)
+// pair: the x-pair form (k_edges_pair on its row map, blocks of pair threads)
 void chl_launch_edges(const ChlMap& m, int nb, int src, int pair, cudaStream_t st) {
-  if (pair) chl_launch_pdl(k_edges_pair, dim3(nb), dim3(256), 0, st, m, src);
+  if (pair) chl_launch_pdl(k_edges_pair, dim3(nb), dim3(pair), 0, st, m, src);
   else chl_launch_pdl(k_edges, dim3(nb), dim3(m.tb), 0, st, m, src);
 }
 void chl_launch_centre(const ChlMap& m, int nb, int s_in, int dsm, int pair, cudaStream_t st) {
