@@ -24,33 +24,50 @@ __global__ void k_pack(double* __restrict__ F, const double* __restrict__ src, i
 // The same two conversions for U, V and W in one launch (blockIdx.y picks
 // the field), between the device fields and the three Fortran-layout
 // arrays of the staging area, so that the three host copies of a transfer
-// run back to back and one kernel converts them.
-__global__ void k_unpack3(ChlFields3 f3, int Nx, int Nz) {
+// run back to back and one kernel converts them.  A block is 4 rows of 64
+// lanes (threadIdx.y, threadIdx.x); a row is one (j, k) line of x, whose
+// coordinates take one 32-bit division per row, and the lanes stride along
+// it: these kernels only move memory, and a 64-bit division per element (a
+// long integer sequence) had held them to a fifth of the HBM bandwidth.
+#define CHL_CONV_ROWS 4
+#define CHL_CONV_LANES 64
+__global__ void __launch_bounds__(CHL_CONV_ROWS * CHL_CONV_LANES)
+k_unpack3(ChlFields3 f3, int Nx, int Nz) {
   const ChlField1& q = f3.f[blockIdx.y];
-  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const int nrow = q.nrow;
-  if (t >= (long)Nx * nrow * Nz) return;
-  const int i = (int)(t % Nx), j = (int)((t / Nx) % nrow), k = (int)(t / ((long)Nx * nrow));
-  const size_t d = (size_t)i + (size_t)Nx * ((size_t)j + (size_t)nrow * k);
+  const int r = blockIdx.x * CHL_CONV_ROWS + threadIdx.y;      // row (j, k) of the device field
+  if (r >= nrow * Nz) return;
+  const int j = r % nrow, k = r / nrow;
+  double* __restrict__ dst = q.dev + (size_t)Nx * r;
   const int last = nrow - 1;
-  if (q.kind == 1 && (j == 0 || j == last)) { q.dev[d] = 0.0; return; }
-  int js = j; double sg = 1.0;
-  if (q.kind == 0 && j == 0) { js = 1; sg = -1.0; }
-  if (q.kind == 0 && j == last) { js = last - 1; sg = -1.0; }
-  const size_t fi = (size_t)(i + 1) + (size_t)q.n1 * ((size_t)js + (size_t)q.n2 * (size_t)(k + 1));
-  q.dev[d] = sg * q.fort[fi];
+  if (q.kind == 1 && (j == 0 || j == last)) {
+    for (int i = threadIdx.x; i < Nx; i += CHL_CONV_LANES) dst[i] = 0.0;
+    return;
+  }
+  int js = j;
+  bool neg = false;
+  if (q.kind == 0 && j == 0) { js = 1; neg = true; }
+  if (q.kind == 0 && j == last) { js = last - 1; neg = true; }
+  const double* __restrict__ src = q.fort + 1 + (size_t)q.n1 * ((size_t)js + (size_t)q.n2 * (size_t)(k + 1));
+  if (neg) { for (int i = threadIdx.x; i < Nx; i += CHL_CONV_LANES) dst[i] = -src[i]; }
+  else { for (int i = threadIdx.x; i < Nx; i += CHL_CONV_LANES) dst[i] = src[i]; }
 }
 
-__global__ void k_pack3(ChlFields3 f3, int Nx, int Nz) {
+__global__ void __launch_bounds__(CHL_CONV_ROWS * CHL_CONV_LANES)
+k_pack3(ChlFields3 f3, int Nx, int Nz) {
   const ChlField1& q = f3.f[blockIdx.y];
-  long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const int n1 = q.n1, n2 = q.n2, nrow = q.nrow;
-  if (t >= (long)n1 * n2 * q.n3) return;
-  const int i1 = (int)(t % n1), j1 = (int)((t / n1) % n2), k1 = (int)(t / ((long)n1 * n2));
-  int i = (i1 - 1) % Nx; if (i < 0) i += Nx;
-  int k = (k1 - 1) % Nz; if (k < 0) k += Nz;
+  const int r = blockIdx.x * CHL_CONV_ROWS + threadIdx.y;      // row (j1, k1) of the Fortran array
+  if (r >= n2 * q.n3) return;
+  const int j1 = r % n2, k1 = r / n2;
+  const int k = k1 == 0 ? Nz - 1 : (k1 - 1 >= Nz ? k1 - 1 - Nz : k1 - 1);
   const int j = j1 < nrow ? j1 : nrow - 1;
-  q.fort[t] = q.dev[(size_t)i + (size_t)Nx * ((size_t)j + (size_t)nrow * k)];
+  const double* __restrict__ src = q.dev + (size_t)Nx * ((size_t)j + (size_t)nrow * k);
+  double* __restrict__ dst = q.fort + (size_t)n1 * r;
+  for (int i1 = threadIdx.x; i1 < n1; i1 += CHL_CONV_LANES) {
+    const int i = i1 == 0 ? Nx - 1 : (i1 - 1 >= Nx ? i1 - 1 - Nx : i1 - 1);
+    dst[i1] = src[i];
+  }
 }
 
 // device field (rows jlo..jhi) -> dense unique-point array (Nx, jhi-jlo+1, Nz)
@@ -68,16 +85,18 @@ void chl_launch_pack(double* F, const double* src, int Nx, int nrow, int Nz, int
   long n = (long)n1 * n2 * n3;
   k_pack<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(F, src, Nx, nrow, Nz, n1, n2, n3, sub);
 }
-// one launch for the three fields; grid x covers the largest of them
+// one launch for the three fields; grid x covers the rows of the largest
 void chl_launch_unpack3(const ChlFields3& f3, int Nx, int Nz, cudaStream_t st) {
-  long n = 0;
-  for (auto& q : f3.f) n = n > (long)Nx * q.nrow * Nz ? n : (long)Nx * q.nrow * Nz;
-  k_unpack3<<<dim3((unsigned)((n + 255) / 256), 3), 256, 0, st>>>(f3, Nx, Nz);
+  int rows = 0;
+  for (auto& q : f3.f) rows = rows > q.nrow * Nz ? rows : q.nrow * Nz;
+  k_unpack3<<<dim3((unsigned)((rows + CHL_CONV_ROWS - 1) / CHL_CONV_ROWS), 3), dim3(CHL_CONV_LANES, CHL_CONV_ROWS),
+              0, st>>>(f3, Nx, Nz);
 }
 void chl_launch_pack3(const ChlFields3& f3, int Nx, int Nz, cudaStream_t st) {
-  long n = 0;
-  for (auto& q : f3.f) n = n > (long)q.n1 * q.n2 * q.n3 ? n : (long)q.n1 * q.n2 * q.n3;
-  k_pack3<<<dim3((unsigned)((n + 255) / 256), 3), 256, 0, st>>>(f3, Nx, Nz);
+  int rows = 0;
+  for (auto& q : f3.f) rows = rows > q.n2 * q.n3 ? rows : q.n2 * q.n3;
+  k_pack3<<<dim3((unsigned)((rows + CHL_CONV_ROWS - 1) / CHL_CONV_ROWS), 3), dim3(CHL_CONV_LANES, CHL_CONV_ROWS),
+            0, st>>>(f3, Nx, Nz);
 }
 void chl_launch_pack_unique(double* F, const double* src, int Nx, int nrow, int Nz, int jlo, int nj, cudaStream_t st) {
   long n = (long)Nx * nj * Nz;
