@@ -287,6 +287,15 @@ __device__ __forceinline__ int chl_find(const ChlMap& m, int b, int& local) {
   return lo;
 }
 
+// (i, j, k) of point t of an Nx x rows x Nz block, x fastest, in 32-bit
+// unsigned arithmetic (an instance has fewer than 2^31 points, checked at
+// creation): the 64-bit divisions this replaces were long integer sequences
+// ahead of every kernel's first load.
+struct ChlIdx { int i, j, k; };
+__device__ __forceinline__ ChlIdx chl_split(unsigned t, unsigned Nx, unsigned rows) {
+  const unsigned q = t / Nx, k = q / rows;
+  return ChlIdx{(int)(t - q * Nx), (int)(q - k * rows), (int)k};
+}
 __device__ __forceinline__ int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
 // Status word bits of an instance: 1 non-finite velocity (k_minabs),

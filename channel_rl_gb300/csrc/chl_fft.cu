@@ -778,11 +778,10 @@ k_project(ChlMap map, int s) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
-  if (t >= (long)Nx * Ny * Nz) return;
-  const int i = (int)(t % Nx);
-  const int jc = 1 + (int)((t / Nx) % Ny);
-  const int k = (int)(t / ((long)Nx * Ny));
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  if (t >= (unsigned)(Nx * Ny * Nz)) return;
+  const ChlIdx ix = chl_split(t, Nx, Ny);
+  const int i = ix.i, jc = 1 + ix.j, k = ix.k;
   const double* p = I.p;
   const size_t c = cidx(I, i, jc, k);
   const double p0 = LDG(p + c);

@@ -122,6 +122,8 @@ int make_consts(const chl_grid_desc& d, Consts& c, std::string& err) {
   c.Nx = d.nx - 2; c.Ny = d.ny - 1; c.Nz = d.nz - 2; c.Nxh = c.Nx / 2 + 1;
   auto rem = [](int n) { while (n % 4 == 0) n /= 4; while (n % 3 == 0) n /= 3; while (n % 2 == 0) n /= 2; return n; };
   if (rem(c.Nx) != 1 || rem(c.Nz) != 1) { err = "grid: Nx = nx-2 and Nz = nz-2 must be of the form 2^a 3^b"; return CHL_E_ARG; }
+  // the kernels index an instance's points in 32 bits (chl_split)
+  if ((long)c.Nx * (c.Ny + 2) * c.Nz >= (1L << 31)) { err = "grid: Nx (Ny+2) Nz must be below 2^31"; return CHL_E_ARG; }
   c.xf.assign(c.nx + 1, 0.0); c.yf.assign(c.ny + 1, 0.0); c.zf.assign(c.nz + 1, 0.0);
   for (int i = 1; i <= c.nx; ++i) c.xf[i] = d.x[i - 1];
   for (int j = 1; j <= c.ny; ++j) c.yf[j] = d.y[j - 1];

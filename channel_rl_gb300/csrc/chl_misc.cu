@@ -322,15 +322,15 @@ k_shift(ChlMap map, int s) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
   if (t == 0) {
     time_advance(I);
     // step counter of the wall-model exploration noise (shared by the batch)
     if (blockIdx.x == 0 && I.mlp_cfg) atomicAdd(I.mlp_cfg + 4, 1u);
   }
-  if (t >= (long)Nx * Ny * Nz) return;
-  const int i = (int)(t % Nx), jc = 1 + (int)((t / Nx) % Ny), k = (int)(t / ((long)Nx * Ny));
-  if (!I.x_mass_cte) return;
+  if (t >= (unsigned)(Nx * Ny * Nz) || !I.x_mass_cte) return;
+  const ChlIdx p = chl_split(t, Nx, Ny);
+  const int i = p.i, jc = 1 + p.j, k = p.k;
   double* U = I.U[s];
   const double d = I.scal[CHL_S_SHIFT];
   const double un = U[cidx(I, i, jc, k)] + d;

@@ -44,11 +44,10 @@ k_flux(ChlMap map, int sin) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
-  if (t >= (long)Nx * (Ny + 1) * Nz) return;
-  const int i = (int)(t % Nx);
-  const int j = (int)((t / Nx) % (Ny + 1));
-  const int k = (int)(t / ((long)Nx * (Ny + 1)));
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  if (t >= (unsigned)(Nx * (Ny + 1) * Nz)) return;
+  const ChlIdx p = chl_split(t, Nx, Ny + 1);
+  const int i = p.i, j = p.j, k = p.k;
   const int im = wrap(i - 1, Nx), ip = wrap(i + 1, Nx);
   const int km = wrap(k - 1, Nz), kp = wrap(k + 1, Nz);
   const double* __restrict__ U = I.U[sin];
@@ -125,11 +124,10 @@ k_rhs_update(ChlMap map, RhsArgs a) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
-  if (t >= (long)Nx * Ny * Nz) return;
-  const int i = (int)(t % Nx);
-  const int jc = 1 + (int)((t / Nx) % Ny);
-  const int k = (int)(t / ((long)Nx * Ny));
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  if (t >= (unsigned)(Nx * Ny * Nz)) return;
+  const ChlIdx p = chl_split(t, Nx, Ny);
+  const int i = p.i, jc = 1 + p.j, k = p.k;
   const int im = wrap(i - 1, Nx), ip = wrap(i + 1, Nx);
   const int km = wrap(k - 1, Nz), kp = wrap(k + 1, Nz);
   const double* const* G = I.G;

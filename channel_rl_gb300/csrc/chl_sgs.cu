@@ -33,11 +33,10 @@ k_edges(ChlMap map, int src) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
-  if (t >= (long)Nx * (Ny + 1) * Nz) return;
-  const int a = (int)(t % Nx);
-  const int j = (int)((t / Nx) % (Ny + 1));
-  const int k = (int)(t / ((long)Nx * (Ny + 1)));
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  if (t >= (unsigned)(Nx * (Ny + 1) * Nz)) return;
+  const ChlIdx p = chl_split(t, Nx, Ny + 1);
+  const int a = p.i, j = p.j, k = p.k;
   const double *U, *V, *W;
   if (src < 3) { U = I.U[src]; V = I.V[src]; W = I.W[src]; }
   else { U = I.r[15]; V = I.r[16]; W = I.r[17]; }
@@ -79,9 +78,10 @@ k_edges_pair(ChlMap map, int src) {
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
   const int RB = blockDim.x / Nx;
   const int r = threadIdx.x / Nx, a = threadIdx.x - r * Nx;
-  const long g = (long)lb * RB + r;                  // the row (j, k), j = 0..Ny
-  const bool valid = r < RB && g < (long)(Ny + 1) * Nz;
-  const int j = valid ? (int)(g % (Ny + 1)) : 0, k = valid ? (int)(g / (Ny + 1)) : 0;
+  const unsigned g = (unsigned)lb * RB + r;          // the row (j, k), j = 0..Ny
+  const bool valid = r < RB && g < (unsigned)((Ny + 1) * Nz);
+  const unsigned gk = valid ? g / (unsigned)(Ny + 1) : 0u;
+  const int j = valid ? (int)(g - gk * (unsigned)(Ny + 1)) : 0, k = (int)gk;
   const double *U, *V, *W;
   if (src < 3) { U = I.U[src]; V = I.V[src]; W = I.W[src]; }
   else { U = I.r[15]; V = I.r[16]; W = I.r[17]; }
@@ -174,11 +174,10 @@ k_centre(ChlMap map, int s_in) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
-  if (t >= (long)Nx * Ny * Nz) return;
-  const int i = (int)(t % Nx);
-  const int jc = 1 + (int)((t / Nx) % Ny);
-  const int k = (int)(t / ((long)Nx * Ny));
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  if (t >= (unsigned)(Nx * Ny * Nz)) return;
+  const ChlIdx p = chl_split(t, Nx, Ny);
+  const int i = p.i, jc = 1 + p.j, k = p.k;
   const Faces f = centre_faces(I, I.U[s_in], I.V[s_in], I.W[s_in], i, jc, k);
   const Strain s = centre_strain<false, PAIR>(I, f, i, jc, k);
   const size_t c = cidx(I, i, jc, k);
@@ -239,11 +238,10 @@ k_filter_y(ChlMap map, int s_in) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
-  if (t >= (long)Nx * (Ny + 2) * Nz) return;
-  const int i = (int)(t % Nx);
-  const int j = (int)((t / Nx) % (Ny + 2));
-  const int k = (int)(t / ((long)Nx * (Ny + 2)));
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  if (t >= (unsigned)(Nx * (Ny + 2) * Nz)) return;
+  const ChlIdx p = chl_split(t, Nx, Ny + 2);
+  const int i = p.i, j = p.j, k = p.k;
   const size_t c = cidx(I, i, j, k);
   const size_t pc = (size_t)Nx;
   const F64 f = f64_of(I);
@@ -270,11 +268,10 @@ k_filter_xz(ChlMap map, int from_r) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
-  if (t >= (long)Nx * (Ny + 2) * Nz) return;
-  const int i = (int)(t % Nx);
-  const int j = (int)((t / Nx) % (Ny + 2));
-  const int k = (int)(t / ((long)Nx * (Ny + 2)));
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  if (t >= (unsigned)(Nx * (Ny + 2) * Nz)) return;
+  const ChlIdx p = chl_split(t, Nx, Ny + 2);
+  const int i = p.i, j = p.j, k = p.k;
   double* const* in = from_r ? I.r : I.q;
   double* const* out = from_r ? I.q : I.r;
   // periodic neighbours as offsets from the point (the wrap folded in), the
@@ -517,9 +514,10 @@ k_eqwm(ChlMap map, int s_in) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  long t = (long)lb * blockDim.x + threadIdx.x;
-  if (t >= 2L * Nx * Nz) return;
-  const int a = (int)(t % Nx), k = (int)((t / Nx) % Nz), wall = (int)(t / ((long)Nx * Nz));
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  if (t >= (unsigned)(2 * Nx * Nz)) return;
+  const ChlIdx p = chl_split(t, Nx, Nz);
+  const int a = p.i, k = p.j, wall = p.k;
   const double* U = I.U[s_in];
   const double u = wall == 0 ? U[cidx(I, a, 3, k)] : U[cidx(I, a, Ny - 2, k)];
   const double prev = I.alpha[t];
@@ -538,12 +536,10 @@ k_nut(ChlMap map, int s_in, int use_wm) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  const long t = (long)lb * blockDim.x + threadIdx.x;
-  const bool valid = t < (long)Nx * (Ny + 2) * Nz;
-  const long tv = valid ? t : 0;
-  const int i = (int)(tv % Nx);
-  const int jc = (int)((tv / Nx) % (Ny + 2));
-  const int k = (int)(tv / ((long)Nx * (Ny + 2)));
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  const bool valid = t < (unsigned)(Nx * (Ny + 2) * Nz);
+  const ChlIdx p = chl_split(valid ? t : 0u, Nx, Ny + 2);
+  const int i = p.i, jc = p.j, k = p.k;
   const bool wmrow = valid && use_wm && I.wall_model != 0 && (jc <= 1 || jc >= Ny);
   const int wall = jc <= 1 ? 0 : 1;
   const double* U = I.U[s_in];

@@ -124,12 +124,10 @@ k_amd(ChlMap map, int s_in, int use_wm) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  const long t = (long)lb * blockDim.x + threadIdx.x;
-  const bool valid = t < (long)Nx * Ny * Nz;
-  const long tv = valid ? t : 0;   // lanes past the end compute point 0 and write nothing
-  const int i = (int)(tv % Nx);
-  const int jc = 1 + (int)((tv / Nx) % Ny);
-  const int k = (int)(tv / ((long)Nx * Ny));
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  const bool valid = t < (unsigned)(Nx * Ny * Nz);
+  const ChlIdx p = chl_split(valid ? t : 0u, Nx, Ny);   // lanes past the end compute point 0 and write nothing
+  const int i = p.i, jc = 1 + p.j, k = p.k;
   const Grad g = gradients(I, I.U[s_in], I.V[s_in], I.W[s_in], i, jc, k);
   // centre strain: diagonal S_ii; 8 S_ij off the diagonal
   const double s11 = g.dux * g.rxc, s22 = g.dvy * g.ryc, s33 = g.dwz * g.rzc;
@@ -168,12 +166,10 @@ k_vreman(ChlMap map, int s_in, int use_wm) {
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
-  const long t = (long)lb * blockDim.x + threadIdx.x;
-  const bool valid = t < (long)Nx * Ny * Nz;
-  const long tv = valid ? t : 0;
-  const int i = (int)(tv % Nx);
-  const int jc = 1 + (int)((tv / Nx) % Ny);
-  const int k = (int)(tv / ((long)Nx * Ny));
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  const bool valid = t < (unsigned)(Nx * Ny * Nz);
+  const ChlIdx p = chl_split(valid ? t : 0u, Nx, Ny);
+  const int i = p.i, jc = 1 + p.j, k = p.k;
   const Grad g = gradients(I, I.U[s_in], I.V[s_in], I.W[s_in], i, jc, k);
   // a_ij = du_j/dx_i (reference layout 1 4 5 / 7 2 6 / 8 9 3); the
   // off-diagonal entries are kept 4 x (the 1/16 is folded below)
