@@ -81,7 +81,10 @@ typedef struct {
 } chl_stats_out;
 
 /* initialize (initialization.f90:23-497) for one instance / n instances
- * advanced together.  Allocates every device buffer once. */
+ * advanced together.  Allocates every device buffer once.  Grid limits:
+ * nx-2 and nz-2 of the form 2^a 3^b, x and z uniformly spaced, and fewer
+ * than 2^31 points (nx-2)(ny+1)(nz-2) per instance (the kernels index an
+ * instance's points in 32 bits); CHL_E_ARG otherwise. */
 int chl_create(const chl_grid_desc* desc, chl_handle** out);
 int chl_batch_create(int n, const chl_grid_desc* descs, chl_handle** out);
 /* finalize (finalization.f90:19-121). */
