@@ -768,6 +768,21 @@ int chl_grid_constants(const chl_grid_desc* d, double* out) {
   return CHL_OK;
 }
 
+int chl_fft_pass_table(int N, double* out, int cap) {
+  if (N < 1) return -1;
+  int r = N;
+  while (r % 4 == 0) r /= 4;
+  while (r % 3 == 0) r /= 3;
+  while (r % 2 == 0) r /= 2;
+  if (r != 1) return -1;
+  const std::vector<double> t = fft_pass_table(N);
+  if (out) {
+    if (cap < (int)t.size()) return -2;
+    std::copy(t.begin(), t.end(), out);
+  }
+  return (int)t.size();
+}
+
 int chl_batch_create(int n, const chl_grid_desc* descs, chl_handle** out) {
   if (!out || n <= 0 || !descs) return CHL_E_ARG;
   *out = nullptr;

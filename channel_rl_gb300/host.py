@@ -71,7 +71,7 @@ EXPORTS = (
     "chl_compute_wall_model", "chl_compute_rhs", "chl_compute_projection_step",
     "chl_compute_dPx_for_constant_mass_flow", "chl_compute_pressure", "chl_check_divergence",
     "chl_stats", "chl_stats_profiles", "chl_synchronize", "chl_grid_constants_size",
-    "chl_grid_constants", "chl_set_fields", "chl_download_async", "chl_time_steps",
+    "chl_grid_constants", "chl_fft_pass_table", "chl_set_fields", "chl_download_async", "chl_time_steps",
     "chl_graph_kernel_count", "chl_profile_step",
     "chl_autotune", "chl_get_tile_shapes", "chl_set_tile_shapes",
     "chl_check_divergence_noalloc", "chl_noalloc_last_error", "chl_device_reset",
@@ -128,6 +128,7 @@ def load(build_if_missing=True):
     lib.chl_stats.argtypes = [H, C.c_int, C.POINTER(StatsOut)]
     lib.chl_stats_profiles.argtypes = [H, C.c_int] + [_F64P] * 7
     lib.chl_grid_constants_size.argtypes = [C.POINTER(GridDesc)]
+    lib.chl_fft_pass_table.argtypes = [C.c_int, _F64P, C.c_int]
     lib.chl_grid_constants.argtypes = [C.POINTER(GridDesc), _F64P]
     lib.chl_set_fields.argtypes = [H, C.c_int, _F64P, _F64P, _F64P]
     lib.chl_download_async.argtypes = [H, C.c_int, _F64P, _F64P, _F64P]
@@ -268,6 +269,17 @@ def sqrt_selftest(a):
     if rc:
         raise ChlError(f"chl_sqrt_selftest failed ({rc})", rc)
     return y
+
+
+def fft_pass_table(N):
+    """The length-N transform's pass table (chl_fft_pass_table; no GPU needed)."""
+    lib = load()
+    n = lib.chl_fft_pass_table(int(N), None, 0)
+    if n < 0:
+        raise ChlError(f"chl_fft_pass_table: no table for length {N} ({n})", n)
+    out = np.zeros(n)
+    lib.chl_fft_pass_table(int(N), out.ctypes.data_as(_F64P), n)
+    return out
 
 
 def grid_constants(case: Case):

@@ -286,6 +286,20 @@ const char* chl_noalloc_last_error(void);
  * w0(1:ny), dxmin, dymin, dzmin, coef_bc_1, coef_bc_2]. */
 int chl_grid_constants_size(const chl_grid_desc* desc);
 int chl_grid_constants(const chl_grid_desc* desc, double* out);
+/* Host-only: the pass table of the length-N transform that chl_create
+ * stages for the x (N = nx-2) and z (N = nz-2) transforms.  Per pass with
+ * twiddles (radix R = 4 while the remaining length allows, then 3, then 2;
+ * sub-transform size Ns > 1) 7 fields of Ns doubles, entry jm for the
+ * twiddles w_r = exp(-2 pi i jm r/(Ns R)), r = 1..R-1, each kept as a scale
+ * sigma_r (C or S of w_r = C + iS, the larger in magnitude) and a
+ * multiplier m_r (S/C or C/S): 0 m1, 1 m2, 2 m3 (radix 4) or
+ * sin(2 pi/3) sigma1 (radix 3), 3 sigma1, 4 sigma2 (radix 4) or sigma1/2
+ * (radix 3), 5 sigma3/sigma1 (radix 4) or sigma2/sigma1 (radix 3), 6 the
+ * form bits (bit r set: w_r divided by S) as the bit pattern of a double.
+ * Returns the table's length in doubles and fills out when out is not NULL
+ * and cap holds it; -1 when N is not of the form 2^a 3^b, -2 when cap is
+ * too small. */
+int chl_fft_pass_table(int N, double* out, int cap);
 
 /* ---- files in the reference's formats (host only, no GPU needed) ----------
  * Snapshot: the stream layout of output_data / read_input_data
