@@ -71,7 +71,7 @@ namespace {
 constexpr double RK_T[3] = {8.0 / 15.0, 2.0 / 3.0, 1.0};
 
 enum { M_PT, M_EDGE, M_FULL, M_DSMF, M_WALL, M_PLANE, M_FFTX, M_FFTZ, M_TRI, M_MINABS, M_ROWS, M_MLP, M_WALLN,
-       M_ZPLANE, M_ZSOLVE, M_EPAIR, NMAP };
+       M_ZPLANE, M_ZSOLVE, M_EPAIR, M_FULLZ2, M_FULLX2, NMAP };
 constexpr int MLP_NPARAM = 4545;
 
 // Grid constants of one instance (host, FP64), in the device index
@@ -309,7 +309,7 @@ struct chl_handle {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
   ChlMap map(int which) const {
-    const bool pt = which == M_PT || which == M_EDGE || which == M_FULL;
+    const bool pt = which == M_PT || which == M_EDGE || which == M_FULL || which == M_FULLZ2 || which == M_FULLX2;
     return ChlMap{d_inst, d_off[which], (int)in.size(), pt ? tb_pt : 256};
   }
 };
@@ -548,6 +548,8 @@ static int build_maps(chl_handle* h) {
         case M_PT: b = cdiv((long)Nx * Ny * Nz, h->tb_pt); break;
         case M_EDGE: b = cdiv((long)Nx * (Ny + 1) * Nz, h->tb_pt); break;
         case M_FULL: b = cdiv((long)Nx * (Ny + 2) * Nz, h->tb_pt); break;
+        case M_FULLZ2: b = cdiv((long)Nx * (Ny + 2) * (Nz / 2), h->tb_pt); break;   // z planes in pairs (Nz even)
+        case M_FULLX2: b = cdiv((long)(Nx / 2) * (Ny + 2) * Nz, h->tb_pt); break;   // x points in pairs (Nx even)
         case M_DSMF: b = Ny * dsm_npart(Nx, Ny, Nz); break;
         case M_WALL: b = cdiv(2L * Nx * Nz, 256); break;
         case M_PLANE: b = cdiv((long)Nx * Nz, 256); break;
@@ -600,8 +602,8 @@ static int enqueue_sgs(chl_handle* h, int s, bool with_wm, int stage = 0) {
                                  h->epair ? h->tb_epair : 0, st));
     KL("centre_strain", chl_launch_centre(h->map(M_PT), h->nblk[M_PT], s, 1, h->epair, st));
     KL("filter_y", chl_launch_filter_y(h->map(M_FULL), h->nblk[M_FULL], s, st));
-    KL("filter_x", chl_launch_filter_x(h->map(M_FULL), h->nblk[M_FULL], st));
-    KL("filter_z", chl_launch_filter_z(h->map(M_FULL), h->nblk[M_FULL], st));
+    KL("filter_x", chl_launch_filter_x(h->map(M_FULLX2), h->nblk[M_FULLX2], st));
+    KL("filter_z", chl_launch_filter_z(h->map(M_FULLZ2), h->nblk[M_FULLZ2], st));
     KL("edges", chl_launch_edges(h->map(h->epair ? M_EPAIR : M_EDGE), h->nblk[h->epair ? M_EPAIR : M_EDGE], 3,
                                  h->epair ? h->tb_epair : 0, st));
     KL("dsm_LM_MM", chl_launch_dsm_final(h->map(M_DSMF), h->nblk[M_DSMF], h->epair, st));

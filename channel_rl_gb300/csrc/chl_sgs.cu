@@ -258,47 +258,107 @@ k_filter_y(ChlMap map, int s_in) {
   }
 }
 
-// x or z pass (periodic, weights 1-4-1) over all stored rows of each component.
-// The x pass fits 40 registers without spilling (6 blocks of 256 per SM);
-// the z pass, with its two plane offsets, keeps 48.
-template <int DIR>
-__global__ void __launch_bounds__(256, DIR == 0 ? 6 : 5)
-k_filter_xz(ChlMap map, int from_r) {
+// x pass over point pairs: thread (pair, j, k) forms x points i = 2 pair and
+// i + 1 from the 16-byte pairs to its left, at itself and to its right
+// (periodic; Nx is even and every row starts on a pair, so the pairs are
+// 16-byte aligned) and stores its two results as one pair: three vector
+// loads and one vector store per component for two points, instead of six
+// loads and two stores.  Same arithmetic and operand order as the one-point
+// pass, so bit-identical.  r -> q.
+template <int N0, int N>
+__device__ __forceinline__ void filter_x2_group(double* const* in, double* const* out, size_t cl, size_t cc,
+                                                size_t cr, const F64& f, double four) {
+  double2 l[N], c[N], r[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    const double2* g = reinterpret_cast<const double2*>(in[N0 + q]);
+    l[q] = __ldg(g + cl); c[q] = __ldg(g + cc); r[q] = __ldg(g + cr);
+  }
+#pragma unroll
+  for (int q = 0; q < N; ++q)
+    reinterpret_cast<double2*>(out[N0 + q])[cc] =
+        make_double2(fma(four, c[q].x, f.add(l[q].y, c[q].y)), fma(four, c[q].y, f.add(c[q].x, r[q].x)));
+}
+
+__global__ void __launch_bounds__(256)
+k_filter_x2(ChlMap map) {
   chl_pdl_wait();
   int lb;
   const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
   const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const int nxp = Nx / 2;
   const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
-  if (t >= (unsigned)(Nx * (Ny + 2) * Nz)) return;
-  const ChlIdx p = chl_split(t, Nx, Ny + 2);
-  const int i = p.i, j = p.j, k = p.k;
-  double* const* in = from_r ? I.r : I.q;
-  double* const* out = from_r ? I.q : I.r;
-  // periodic neighbours as offsets from the point (the wrap folded in), the
-  // same along x for the centre-like and V-like layouts; along z their
-  // plane sizes differ
-  long dm, dp, dmv, dpv;
-  if (DIR == 0) {
-    dm = i == 0 ? Nx - 1 : -1;
-    dp = i == Nx - 1 ? 1 - Nx : 1;
-    dmv = dm; dpv = dp;
-  } else {
-    const long pc = (long)Nx * (Ny + 2), pv = (long)Nx * (Ny + 1);
-    dm = k == 0 ? (Nz - 1) * pc : -pc;
-    dp = k == Nz - 1 ? -(Nz - 1) * pc : pc;
-    dmv = k == 0 ? (Nz - 1) * pv : -pv;
-    dpv = k == Nz - 1 ? -(Nz - 1) * pv : pv;
-  }
-  const size_t c = cidx(I, i, j, k), cm = c + dm, cp = c + dp;
+  if (t >= (unsigned)(nxp * (Ny + 2) * Nz)) return;
+  const ChlIdx p = chl_split(t, nxp, Ny + 2);
+  const int pi = p.i, j = p.j, k = p.k;
+  const int pl = pi == 0 ? nxp - 1 : pi - 1, pr = pi == nxp - 1 ? 0 : pi + 1;
   const F64 f = f64_of(I);
   const double four = I.fk[FK_FOUR];
-  if (j >= 1 && j <= Ny) filter_centre(in, out, c, cm, cp, j == 1 || j == Ny, f, four);
-  out[15][c] = fma(four, LDG(in[15] + c), f.add(LDG(in[15] + cm), LDG(in[15] + cp)));
-  out[17][c] = fma(four, LDG(in[17] + c), f.add(LDG(in[17] + cm), LDG(in[17] + cp)));
-  if (j <= Ny) {
-    const size_t v = vidx(I, i, j, k), vm = v + dmv, vp = v + dpv;
-    out[16][v] = fma(four, LDG(in[16] + v), f.add(LDG(in[16] + vm), LDG(in[16] + vp)));
+  double* const* in = I.r;
+  double* const* out = I.q;
+  // pair indices: row (j, k) of the centre-like layout starts at pair nxp (j + (Ny+2) k)
+  const size_t rc = (size_t)nxp * ((size_t)j + (size_t)(Ny + 2) * k);
+  if (j >= 1 && j <= Ny) {
+    filter_x2_group<3, 6>(in, out, rc + pl, rc + pi, rc + pr, f, four);
+    filter_x2_group<9, 6>(in, out, rc + pl, rc + pi, rc + pr, f, four);
+    if (j == 1 || j == Ny) filter_x2_group<0, 3>(in, out, rc + pl, rc + pi, rc + pr, f, four);
   }
+  filter_x2_group<15, 1>(in, out, rc + pl, rc + pi, rc + pr, f, four);
+  filter_x2_group<17, 1>(in, out, rc + pl, rc + pi, rc + pr, f, four);
+  if (j <= Ny) {
+    const size_t rv = (size_t)nxp * ((size_t)j + (size_t)(Ny + 1) * k);   // the V-like layout
+    filter_x2_group<16, 1>(in, out, rv + pl, rv + pi, rv + pr, f, four);
+  }
+}
+
+// z pass over plane pairs: thread (i, j, pair) forms planes k = 2 pair and
+// k + 1 from planes k - 1 .. k + 2 (periodic), so each output takes two
+// loads instead of three, all of them independent (the neighbours lie a
+// plane apart, mostly in L2).  Same arithmetic and operand order as the
+// one-plane pass, so bit-identical.  Nz is even (chl_create: nz even), so
+// the planes pair up.  q -> r.
+template <int N0, int N>
+__device__ __forceinline__ void filter_z2_group(double* const* in, double* const* out, size_t km, size_t ka,
+                                                size_t kb, size_t kc, const F64& f, double four) {
+  double a[N], b[N], c[N], d[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    const double* g = in[N0 + q];
+    a[q] = LDG(g + km); b[q] = LDG(g + ka); c[q] = LDG(g + kb); d[q] = LDG(g + kc);
+  }
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    out[N0 + q][ka] = fma(four, b[q], f.add(a[q], c[q]));
+    out[N0 + q][kb] = fma(four, c[q], f.add(b[q], d[q]));
+  }
+}
+
+__global__ void __launch_bounds__(256)
+k_filter_z2(ChlMap map) {
+  chl_pdl_wait();
+  int lb;
+  const ChlInst& I = map.inst[chl_find(map, blockIdx.x, lb)];
+  const int Nx = I.Nx, Ny = I.Ny, Nz = I.Nz;
+  const int npair = Nz / 2;
+  const unsigned t = (unsigned)lb * blockDim.x + threadIdx.x;
+  if (t >= (unsigned)(Nx * (Ny + 2) * npair)) return;
+  const ChlIdx p = chl_split(t, Nx, Ny + 2);
+  const int i = p.i, j = p.j, k0 = 2 * p.k;
+  const int km = k0 == 0 ? Nz - 1 : k0 - 1, kb = k0 + 1, kc = k0 + 2 == Nz ? 0 : k0 + 2;
+  const F64 f = f64_of(I);
+  const double four = I.fk[FK_FOUR];
+  double* const* in = I.q;
+  double* const* out = I.r;
+  const size_t c0 = cidx(I, i, j, km), c1 = cidx(I, i, j, k0), c2 = cidx(I, i, j, kb), c3 = cidx(I, i, j, kc);
+  if (j >= 1 && j <= Ny) {
+    filter_z2_group<3, 6>(in, out, c0, c1, c2, c3, f, four);
+    filter_z2_group<9, 6>(in, out, c0, c1, c2, c3, f, four);
+    if (j == 1 || j == Ny) filter_z2_group<0, 3>(in, out, c0, c1, c2, c3, f, four);
+  }
+  filter_z2_group<15, 1>(in, out, c0, c1, c2, c3, f, four);
+  filter_z2_group<17, 1>(in, out, c0, c1, c2, c3, f, four);
+  if (j <= Ny)
+    filter_z2_group<16, 1>(in, out, vidx(I, i, j, km), vidx(I, i, j, k0), vidx(I, i, j, kb), vidx(I, i, j, kc), f, four);
 }
 
 // ------------------------------------------------------------ L:M, M:M
@@ -581,8 +641,8 @@ void chl_launch_centre(const ChlMap& m, int nb, int s_in, int dsm, int pair, cud
   else chl_launch_pdl(k_centre<false, false>, dim3(nb), dim3(m.tb), 0, st, m, s_in);
 }
 void chl_launch_filter_y(const ChlMap& m, int nb, int s_in, cudaStream_t st) { chl_launch_pdl(k_filter_y, dim3(nb), dim3(m.tb), 0, st, m, s_in); }
-void chl_launch_filter_x(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<0>, dim3(nb), dim3(m.tb), 0, st, m, 1); }
-void chl_launch_filter_z(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_xz<1>, dim3(nb), dim3(m.tb), 0, st, m, 0); }
+void chl_launch_filter_x(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_x2, dim3(nb), dim3(m.tb), 0, st, m); }
+void chl_launch_filter_z(const ChlMap& m, int nb, cudaStream_t st) { chl_launch_pdl(k_filter_z2, dim3(nb), dim3(m.tb), 0, st, m); }
 void chl_launch_dsm_final(const ChlMap& m, int nb, int pair, cudaStream_t st) {
   if (pair) chl_launch_pdl(k_dsm_final<true>, dim3(nb), dim3(CHL_DSMF_THREADS), 0, st, m);
   else chl_launch_pdl(k_dsm_final<false>, dim3(nb), dim3(CHL_DSMF_THREADS), 0, st, m);
