@@ -355,7 +355,7 @@ def roofline_of(args, prof, points, step_ms, workload_name, rank=0, dev_index=0)
     peak_gops = fp64.get("fp64_peak_gops")
     peak_src = ("measured live on this GPU before the timed steps (bench_peaks.cu fp64: best FP64 issue rate, "
                 "a DFMA loop on register operands)" if fp64.get("live") else
-                "measured on this pool's GB300 (profiles/fp64_peak.json from bench.py --measure-peaks: best FP64 "
+                "measured on a GB300 (profiles/fp64_peak.json from bench.py --measure-peaks: best FP64 "
                 "issue rate, a DFMA loop on register operands)")
     if not (peak_gops and dom in fl):
         return hbm

@@ -1,7 +1,7 @@
 """Every code path through the bounds-checked build (field indices checked
 and clamped on the device, violations recorded in each instance's status
 word), on small and ragged grids: no index may leave its field.  This
-stands in for a memory checker, which is not available on the GPU pool."""
+stands in for an external memory checker, which these tests do not run."""
 import os
 import subprocess
 import sys
